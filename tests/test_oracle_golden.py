@@ -1,0 +1,100 @@
+"""The oracle (C restatement) against fixtures made by the reference itself.
+
+Every case of tests/golden/cases.py was run through the reference solver's
+own headers (tests/golden/make_golden.py); the restatement must reproduce the
+mask, the final populations, the per-node force fields, the per-step force
+sums and the wall distance BIT FOR BIT.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases as CS
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def run_oracle(O, spec):
+    s = O.Solver(spec["nx"], spec["ny"], "oracle")
+    CS.apply_setup(s, spec, naca_fn=O.naca_coords, transform_fn=O.transform_points)
+    mask = s.obstacle.copy()
+    th = spec.get("thermal")
+    hook = th.get("hook") if th else None
+    sums = []
+    for _ in range(spec["steps"]):
+        s.step(spec["tau"], spec["u"])
+        if hook:
+            s.thermal_hook(*hook)
+        sums.append(s.force_sums())
+    out = dict(mask=mask, f=s.f.copy(), fx=s.fx.copy(), fy=s.fy.copy(), sums=np.array(sums))
+    if th:
+        out["g"] = s.g.copy()
+    if spec.get("les"):
+        out["wall_dist"] = s.wall_dist.copy()
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(CS.CASES))
+def test_oracle_matches_reference_bit_exact(oracle_lib, name):
+    gold = np.load(os.path.join(GOLD, f"{name}.npz"))
+    got = run_oracle(oracle_lib, CS.CASES[name])
+    for key in gold.files:
+        a, b = got[key], gold[key]
+        assert a.shape == b.shape, key
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"{name}:{key} differs"
+
+
+def test_geometry_known_answers(oracle_lib):
+    O = oracle_lib
+    kat = np.load(os.path.join(GOLD, "kat.npz"))
+    for series, n in ((12, 50), (2412, 60), (4415, 33)):
+        assert np.array_equal(O.naca_coords(series, n), kat[f"naca_{series}_{n}"])
+    p = O.transform_points(O.naca_coords(2412, 40), 30.0, 20.0, 36.0, 8.0)
+    assert np.array_equal(p, kat["transform_2412"])
+    pip = [O.point_in_polygon(x, y, p) for x, y in kat["pip_pts"]]
+    assert np.array_equal(np.array(pip, np.uint8), kat["pip"])
+    eq = [[O.equilibrium(i, rho, u, v) for i in range(9)]
+          for rho, u, v in ((1.0, 0.0, 0.0), (1.2, 0.1, 0.05), (1.5, 0.12, -0.08), (0.9, -0.07, 0.11))]
+    assert np.array_equal(np.array(eq), kat["equilibrium"])
+    s = O.Solver(48, 40)
+    s.place_cylinder(20, 21, 7)
+    qs = [s.compute_q(x, y, i) for x in range(10, 31) for y in range(11, 32) for i in range(9)]
+    assert np.array_equal(np.array(qs), kat["q_cylinder"])
+    s.close()
+    s = O.Solver(96, 40)
+    s.place_polygon(p)
+    qs = [s.compute_q(x, y, i) for x in range(26, 70, 2) for y in range(14, 28) for i in range(9)]
+    assert np.array_equal(np.array(qs), kat["q_polygon"])
+    s.close()
+
+
+# Restatements of the reference's own unit tests (src/lbm_test.cpp) on the oracle.
+def test_equilibrium_sums_and_momentum(oracle_lib):
+    O = oracle_lib
+    assert abs(sum(O.equilibrium(i, 1.2, 0.1, 0.05) for i in range(9)) - 1.2) < 1e-12
+    cx = [0, 1, 0, -1, 0, 1, -1, -1, 1]
+    cy = [0, 0, 1, 0, -1, 1, 1, -1, -1]
+    mx = sum(O.equilibrium(i, 1.0, 0.15, 0.0) * cx[i] for i in range(9))
+    my = sum(O.equilibrium(i, 1.0, 0.15, 0.0) * cy[i] for i in range(9))
+    assert abs(mx - 0.15) < 1e-12 and abs(my) < 1e-12
+    w = [4 / 9] + [1 / 9] * 4 + [1 / 36] * 4
+    for i in range(9):
+        assert abs(O.equilibrium(i, 1.0, 0.0, 0.0) - w[i]) < 1e-15
+        assert O.equilibrium(i, 1.0, 0.1, 0.05) > 0.0
+
+
+def test_mass_conservation_10_steps(oracle_lib):
+    """src/lbm_test.cpp:158-199 at the reference's default 800x300 grid."""
+    O = oracle_lib
+    s = O.Solver(800, 300)
+    s.set_case(O.CYLINDER)
+    s.place_cylinder(200, 150, 30)
+    s.init_uniform(1.0, 0.1, 0.0)
+    fluid = s.obstacle == 0
+    m0 = s.f.reshape(-1, 9)[fluid].sum()
+    s.step(0.56, 0.1, n=10)
+    m1 = s.f.reshape(-1, 9)[fluid].sum()
+    s.close()
+    assert abs(m1 - m0) < 0.01 * m0
