@@ -1,0 +1,244 @@
+/*
+ * lbm2d.h -- C-ABI of the GB300 (sm_103a) D2Q9 lattice-Boltzmann step.
+ *
+ * This is the drop-in boundary.  The lbm-2d reference exposes its solver as a
+ * header-only C++ API: process-global knobs (src/lbm_types.hpp:15-32), a state
+ * struct LBMCapabilities (src/lbm_types.hpp:187-224) and free functions in
+ * src/lbm.hpp.  Each entry point below replaces one piece of that interface;
+ * the comment names the reference declaration it stands in for.  The C++
+ * headers in lbm-2d_gb300/dropin/ (lbm.hpp, lbm_types.hpp, thermal.hpp,
+ * geometry.hpp) re-create the reference's names on top of these calls, so the
+ * reference's case drivers compile unchanged against them.
+ *
+ * Conventions
+ *   - Every call returns an int status (LBM2D_OK = 0).  lbm2d_last_error()
+ *     gives a message for the last failing call on a handle, and
+ *     lbm2d_global_error() for a failed lbm2d_create().
+ *   - Host arrays are plain pointers with the reference's layouts:
+ *     populations FP64 array-of-structures f[node*9 + i], node = y*nx + x,
+ *     direction order of src/lbm_types.hpp:41-42; per-node fields FP64 or u8.
+ *   - A handle owns its device buffers and one CUDA stream; it is not
+ *     thread-safe.  Work is asynchronous on that stream; calls that return
+ *     host data synchronize it.
+ *   - State semantics follow execute_time_step (src/lbm.hpp:293-582): the
+ *     state a caller uploads and downloads is the post-stream, post-boundary
+ *     state the reference keeps in LBMCapabilities::f between steps.
+ */
+#ifndef LBM2D_H
+#define LBM2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes */
+#define LBM2D_OK 0
+#define LBM2D_ERR_INVALID 1   /* bad argument or configuration */
+#define LBM2D_ERR_OOM 2       /* device allocation failed */
+#define LBM2D_ERR_CUDA 3      /* CUDA runtime error */
+#define LBM2D_ERR_NAN 4       /* a non-finite density was produced */
+#define LBM2D_ERR_STATE 5     /* call out of order (e.g. no state uploaded) */
+#define LBM2D_ERR_NO_DEVICE 6 /* no usable CUDA device */
+#define LBM2D_ERR_TIMEOUT 7   /* a bounded device wait ran out */
+
+/* ---- case types: numbering of CaseType, src/lbm_types.hpp:20-23 */
+#define LBM2D_CASE_CYLINDER 0
+#define LBM2D_CASE_CAVITY 1
+#define LBM2D_CASE_STEP 2
+#define LBM2D_CASE_RIBS 3
+#define LBM2D_CASE_URBAN_CANYON 4
+#define LBM2D_CASE_DOWNWASH 5
+#define LBM2D_CASE_SQUARE_CYLINDER 6
+#define LBM2D_CASE_FLAT_PLATE 7
+#define LBM2D_CASE_SPORTS_BALL 8
+#define LBM2D_CASE_PERIODIC_HILLS 9
+#define LBM2D_CASE_CYLINDER_NEAR_WALL 10
+#define LBM2D_CASE_SIDE_BY_SIDE 11
+#define LBM2D_CASE_ROTATING_CYLINDER 12
+#define LBM2D_CASE_ORIFICE_PLATE 13
+
+/* ---- collision operators: CollisionType, src/lbm_types.hpp:26 */
+#define LBM2D_MRT 0
+#define LBM2D_BGK 1
+
+/* ---- population storage on the device (the collision always runs in FP32,
+ *      or in FP64 for LBM2D_STORE_FP64).  FP16/BF16 store the shifted
+ *      deviation f_i - w_i*rho0 (rho0 = 1), and g_i - w_i*T_ref for thermal. */
+#define LBM2D_STORE_FP32 0
+#define LBM2D_STORE_FP16 1
+#define LBM2D_STORE_BF16 2
+#define LBM2D_STORE_FP64 3
+
+/* ---- device-side thermal boundary passes (the drivers' post-step loops) */
+#define LBM2D_HOOK_NONE 0
+#define LBM2D_HOOK_HEATED_CAVITY 1   /* src/thermal_cavity.cpp:168-204 */
+#define LBM2D_HOOK_HEATED_SOLIDS 2   /* src/heated_cylinder.cpp:156-164 */
+
+typedef struct lbm2d_config {
+    int nx, ny;      /* NX, NY globals (src/lbm_types.hpp:15-16) */
+    int case_type;   /* g_case (src/lbm_types.hpp:28) */
+    int collision;   /* g_collision (src/lbm_types.hpp:27) */
+    int use_les;     /* g_use_les (src/lbm_types.hpp:31) */
+    double cs;       /* g_cs (src/lbm_types.hpp:32) */
+    int storage;     /* LBM2D_STORE_* */
+    int device;      /* CUDA device ordinal */
+} lbm2d_config;
+
+typedef struct lbm2d_info {
+    int nx, ny, storage;
+    double bytes_per_update;   /* algorithmic population bytes per lattice update */
+    size_t device_bytes;       /* device memory held by the handle */
+    int n_boundary_nodes;      /* nodes with a boundary record */
+    int n_force_nodes;         /* nodes with momentum-exchange links */
+    long long steps_done;      /* steps executed since the last upload */
+    int block_x, block_y;      /* launch shape of the step kernel */
+} lbm2d_info;
+
+typedef struct lbm2d_solver lbm2d_solver;
+
+/* Construct a solver: replaces `LBMCapabilities()` (src/lbm_types.hpp:209-218)
+ * together with the globals it reads (src/lbm_types.hpp:15-32).  The initial
+ * state matches the constructor: f = 0, g = 1, no obstacles. */
+int lbm2d_create(const lbm2d_config *cfg, lbm2d_solver **out);
+/* Release the handle and its device memory (LBMCapabilities destructor). */
+int lbm2d_destroy(lbm2d_solver *h);
+const char *lbm2d_last_error(const lbm2d_solver *h);
+const char *lbm2d_global_error(void);
+
+/* Re-select case/collision/LES: the globals g_case, g_collision, g_use_les,
+ * g_cs read by execute_time_step (src/lbm.hpp:300-302, :408, :531-543). */
+int lbm2d_set_case(lbm2d_solver *h, int case_type, int collision, int use_les, double cs);
+
+/* Solid mask, one byte per node: LBMCapabilities::obstacle
+ * (src/lbm_types.hpp:190), as written by place_walls / place_cylinder /
+ * place_polygon (src/lbm.hpp:79-87, :931-964) or by drivers directly. */
+int lbm2d_set_mask(lbm2d_solver *h, const uint8_t *obstacle);
+
+/* Interpolated bounce-back geometry: LBMCapabilities::bb_geom
+ * (BounceBackGeometry, src/lbm_types.hpp:90-182).  A cylinder with radius > 0
+ * or a polygon with >= 1 vertex makes bb_geom "valid" (:102); radius 0 and
+ * n = 0 clear it.  The polygon replaces any circle, as in the reference. */
+int lbm2d_set_bb_cylinder(lbm2d_solver *h, double cx, double cy, double radius);
+int lbm2d_set_bb_polygon(lbm2d_solver *h, const double *xy, int n_vertices);
+/* BounceBackGeometry::has_moving_wall/omega/rot_cx/rot_cy (src/lbm_types.hpp:98-100). */
+int lbm2d_set_moving_wall(lbm2d_solver *h, int on, double omega, double rot_cx, double rot_cy);
+/* BounceBackGeometry::use_mei_bb (src/lbm_types.hpp:181): 1 = Mei/Filippova-
+ * Hanel (default), 0 = classic Bouzidi with the Ladd wall term (src/lbm.hpp:257-285). */
+int lbm2d_set_mei(lbm2d_solver *h, int on);
+
+/* LBMCapabilities::body_force_x (src/lbm_types.hpp:207). */
+int lbm2d_set_body_force(lbm2d_solver *h, double fx);
+/* Thermal DDF knobs: LBMCapabilities::use_thermal, T_ref, alpha, omega_k,
+ * beta, g_buoyancy (src/lbm_types.hpp:196-201). */
+int lbm2d_set_thermal(lbm2d_solver *h, int use, double T_ref, double alpha, double omega_k,
+                      double beta, double g_buoyancy);
+/* Device-side version of a driver's post-step thermal loop (LBM2D_HOOK_*):
+ * HEATED_CAVITY(Ta = hot, Tb = cold) as src/thermal_cavity.cpp:168-204,
+ * HEATED_SOLIDS(Ta = wall temperature) as src/heated_cylinder.cpp:156-164.
+ * Applied to the state after every step, exactly where the drivers apply it. */
+int lbm2d_set_thermal_hook(lbm2d_solver *h, int kind, double Ta, double Tb);
+
+/* Populations, FP64 AoS [nx*ny*9]: writes LBMCapabilities::f / g_thermal
+ * (src/lbm_types.hpp:188, :194) as the drivers do before their loop. */
+int lbm2d_upload_f(lbm2d_solver *h, const double *f);
+int lbm2d_upload_g(lbm2d_solver *h, const double *g);
+
+/* One or more calls of execute_time_step(sys, tau, u_inflow)
+ * (src/lbm.hpp:293-582).  Asynchronous. */
+int lbm2d_step(lbm2d_solver *h, double tau, double u_inflow, int nsteps);
+
+/* Sum over nodes of fx_body / fy_body after the last step -- the driver's
+ * per-step reduction (src/main.cpp:106-110) of the momentum-exchange force
+ * (src/lbm.hpp:543-581).  FP64, synchronizes. */
+int lbm2d_force_sums(lbm2d_solver *h, double *fx_total, double *fy_total);
+/* Per-step force sums recorded on the device since the last upload or
+ * lbm2d_force_history_reset(): copies min(n, recorded) pairs, returns the
+ * number of recorded steps in *n_recorded. */
+int lbm2d_force_history(lbm2d_solver *h, double *fx, double *fy, int n, int *n_recorded);
+int lbm2d_force_history_reset(lbm2d_solver *h);
+
+/* Read back LBMCapabilities::f / g_thermal (FP64 AoS), fx_body / fy_body
+ * (FP64, per node), wall_dist (src/lbm_types.hpp:191) and the macroscopic
+ * fields of compute_macros / compute_temperature (src/lbm_types.hpp:278-288,
+ * src/thermal.hpp:55-60).  Any output pointer of download_macros may be NULL. */
+int lbm2d_download_f(lbm2d_solver *h, double *f);
+int lbm2d_download_g(lbm2d_solver *h, double *g);
+int lbm2d_download_force_field(lbm2d_solver *h, double *fx_body, double *fy_body);
+int lbm2d_download_macros(lbm2d_solver *h, double *rho, double *u, double *v, double *T);
+int lbm2d_download_wall_dist(lbm2d_solver *h, double *wall_dist);
+
+/* Wait for the handle's stream; reports LBM2D_ERR_NAN if any step since the
+ * last check produced a non-finite density. */
+int lbm2d_synchronize(lbm2d_solver *h);
+int lbm2d_get_info(lbm2d_solver *h, lbm2d_info *info);
+/* Launch shape of the step kernel (threads per block = bx*by, a multiple of
+ * 32, at most 1024).  0,0 restores the tuned default. */
+int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
+/* The CUDA stream the handle launches on (cudaStream_t as void*). */
+void *lbm2d_stream(lbm2d_solver *h);
+/* Count of kernel launches made by this handle since creation. */
+long long lbm2d_launch_count(lbm2d_solver *h);
+
+/* Kernel timing: while on, the handle records a CUDA event pair around every
+ * step-kernel launch on its stream; lbm2d_profile synchronizes, returns the
+ * summed step-kernel time in milliseconds and the number of timed launches,
+ * and clears the record. */
+int lbm2d_set_profiling(lbm2d_solver *h, int on);
+int lbm2d_profile(lbm2d_solver *h, double *step_kernel_ms, long long *n_launches);
+
+/* Device-resident variants for callers that keep populations on the GPU:
+ * pointers to device memory, same FP64 AoS layout, stream-ordered on the
+ * handle's stream (no host synchronization). */
+int lbm2d_upload_f_device(lbm2d_solver *h, const double *d_f);
+int lbm2d_download_f_device(lbm2d_solver *h, double *d_f);
+
+
+/* ---- host services (no device needed): the reference's set-up arithmetic,
+ *      shared by the C++ drop-in headers and the Python binding so masks and
+ *      link lists are bit-exact with the reference. */
+
+/* compute_equilibrium, src/lbm_types.hpp:269-273 */
+double lbm2d_equilibrium(int i, double rho, double u, double v);
+/* place_walls on a mask [nx*ny], src/lbm.hpp:79-87 */
+int lbm2d_mask_walls(int nx, int ny, uint8_t *mask);
+/* place_cylinder's mask rule sqrt(dx^2+dy^2) < r, src/lbm.hpp:931-944 */
+int lbm2d_mask_cylinder(int nx, int ny, uint8_t *mask, int cx, int cy, int radius);
+/* place_polygon's mask rule (point_in_polygon per node), src/lbm.hpp:951-964 */
+int lbm2d_mask_polygon(int nx, int ny, uint8_t *mask, const double *xy, int n_vertices);
+/* point_in_polygon, src/geometry.hpp:120-134 */
+int lbm2d_point_in_polygon(double px, double py, const double *xy, int n_vertices);
+/* naca_coords, src/geometry.hpp:17-90: writes 2n-1 points (x,y pairs) into
+ * out (capacity 2*(2n-1) doubles), returns the point count. */
+int lbm2d_naca_coords(int series, int n, double *out);
+/* transform_points, src/geometry.hpp:95-114 (in place) */
+int lbm2d_transform_points(double *xy, int n, double cx, double cy, double scale, double angle_deg);
+/* compute_wall_distance's result, src/lbm_types.hpp:231-264 */
+int lbm2d_wall_distance(int nx, int ny, const uint8_t *mask, double *wall_dist);
+
+/* Geometry of the interpolated bounce-back (BounceBackGeometry,
+ * src/lbm_types.hpp:90-182) for the host link query below. */
+typedef struct lbm2d_bb_geometry {
+    double cx, cy, radius;
+    const double *poly; /* x,y pairs, may be NULL */
+    int n_poly;
+    int has_moving_wall;
+    double omega, rot_cx, rot_cy;
+} lbm2d_bb_geometry;
+
+/* Every bounce-back link of a mask as the reference's streaming treats it
+ * (src/lbm.hpp:408-484): node index, link direction i (node -> solid or
+ * outside), kind (1 = simple bounce-back, 2 = interpolated, 3 = no source),
+ * q and wall velocity of interpolated links (src/lbm_types.hpp:106-176) and
+ * whether the force pass counts the link (src/lbm.hpp:543-581).  Returns the
+ * total link count in *count; arrays receive at most `capacity` entries. */
+int lbm2d_boundary_links(int nx, int ny, int case_type, const uint8_t *mask, const lbm2d_bb_geometry *geom,
+                         int capacity, int32_t *node, int8_t *dir, int8_t *kind, double *q, double *uwx,
+                         double *uwy, int8_t *counts_force, int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM2D_H */

@@ -1,0 +1,898 @@
+// lbm2d_capi.cpp -- the C-ABI (include/lbm2d.h) over the CUDA kernels.
+//
+// The handle keeps the device state in one of two forms:
+//   STAGED    the reference's state S (post-stream, post-boundary) as FP64
+//             AoS in device staging buffers -- right after an upload;
+//   COLLIDED  the post-collision populations of S in the storage precision,
+//             SoA -- what the step kernel consumes and produces.
+// A step call collides a STAGED state first (prologue kernel) with the
+// call's own collision parameters, so results match execute_time_step
+// (src/lbm.hpp:293-582) even when tau, the body force or the thermal
+// parameters change between calls: a change of those parameters, of the
+// geometry or of the case first rebuilds S from the stored populations
+// (readback kernel) and re-collides it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm2d.h"
+#include "lbm2d_geometry.h"
+#include "lbm2d_internal.h"
+
+using namespace lbm2d;
+
+namespace {
+thread_local std::string g_global_err;
+
+constexpr double W[9] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0,
+                         1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
+constexpr int CASE_CAVITY = 1, CASE_STEP = 2, CASE_RIBS = 3, CASE_HILLS = 9;
+
+size_t elem_size(int storage) {
+    switch (storage) {
+        case ST_FP32: return 4;
+        case ST_FP16:
+        case ST_BF16: return 2;
+        case ST_FP64: return 8;
+    }
+    return 0;
+}
+
+struct CollideParams {
+    int collision = 0, les = 0, thermal = 0;
+    double s_shear = 0, s_bulk = 0, s_normal = 0, tau = 0, cs_sq = 0, nu = 0, Fscale = 0;
+    double omega_k = 0, beta = 0, g_buoy = 0, T_ref = 0;
+    bool operator==(const CollideParams& o) const {
+        return collision == o.collision && les == o.les && thermal == o.thermal && s_shear == o.s_shear &&
+               s_bulk == o.s_bulk && s_normal == o.s_normal && tau == o.tau && cs_sq == o.cs_sq && nu == o.nu &&
+               Fscale == o.Fscale && omega_k == o.omega_k && beta == o.beta && g_buoy == o.g_buoy &&
+               T_ref == o.T_ref;
+    }
+};
+}  // namespace
+
+struct lbm2d_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nx = 0, ny = 0;
+    size_t N = 0;
+    int case_type = 0, collision = 0, use_les = 0, storage = 0;
+    double cs = 0.12;
+    std::vector<uint8_t> mask;
+    BBGeometry bb;
+    double body_force = 0.0;
+    bool thermal = false;
+    double T_ref = 1.0, alpha = 0.1666666667, omega_k = 1.0, beta = 0.0, g_buoy = 0.0;
+    int hook = 0;
+    double hook_a = 0.0, hook_b = 0.0;
+
+    // device buffers
+    void* P[2] = {nullptr, nullptr};
+    void* G[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint32_t* d_flags = nullptr;
+    uint32_t* d_rec_info = nullptr;
+    uint32_t* d_rec_force = nullptr;
+    double* d_rec_wd = nullptr;
+    double* d_rec_q = nullptr;
+    double* d_rec_uw = nullptr;
+    double* d_partials = nullptr;
+    int* d_block_slot = nullptr;
+    int nslots = 0, slot_bx = 0, slot_by = 0;
+    double* d_hist = nullptr;
+    int hist_cap = 1 << 18;
+    unsigned long long* d_counter = nullptr;
+    double* d_last = nullptr;
+    unsigned int* d_nan = nullptr;
+    double* d_stage_f = nullptr;
+    double* d_stage_g = nullptr;
+    double* d_fx = nullptr;
+    double* d_fy = nullptr;
+    size_t device_bytes = 0;
+
+    GeometryTables geo;
+    bool geom_dirty = true;
+    bool staged = true;  // STAGED (true) or COLLIDED (false)
+    bool stage_f_valid = false, stage_g_valid = false;  // staging holds S (else defaults)
+    CollideParams cp_of_P;
+    double u_last = 0.0;
+    long long steps_since_collide = 0;
+    long long steps_done = 0;
+    long long launches = 0;
+    int bx = 128, by = 2;
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;  // even/odd = start/stop
+    size_t ev_used = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(lbm2d_solver* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_fail(lbm2d_solver* h, cudaError_t e, const char* what) {
+    return fail(h, e == cudaErrorMemoryAllocation ? LBM2D_ERR_OOM : LBM2D_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                  \
+    do {                                                \
+        cudaError_t e_ = (expr);                        \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+    } while (0)
+
+template <class T>
+int dalloc(lbm2d_solver* h, T** p, size_t bytes) {
+    if (*p) return LBM2D_OK;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+    *p = static_cast<T*>(q);
+    h->device_bytes += bytes;
+    return LBM2D_OK;
+}
+
+template <class T>
+void dfree(lbm2d_solver* h, T** p) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    (void)h;
+}
+
+int bc_kind(int case_type) {
+    if (case_type == CASE_CAVITY) return BC_LID;
+    if (case_type == CASE_STEP) return BC_STEP;
+    if (case_type == CASE_RIBS || case_type == CASE_HILLS) return BC_NONE;
+    return BC_INFLOW;
+}
+
+CollideParams collide_params(const lbm2d_solver* h, double tau) {
+    CollideParams c;
+    c.collision = h->collision;
+    c.tau = tau;
+    const double s = 1.0 / tau;  // MRTParams::from_tau, src/lbm_types.hpp:72-76
+    c.s_shear = (s < 0.5) ? 0.5 : ((s > 1.99) ? 1.99 : s);
+    c.s_bulk = 1.2;
+    c.s_normal = 1.0;
+    c.cs_sq = h->use_les ? h->cs * h->cs : 0.0;
+    c.les = (h->collision == 0 && c.cs_sq > 0.0 && tau > 0.0) ? 1 : 0;
+    c.nu = (tau - 0.5) / 3.0;
+    c.Fscale = (h->body_force != 0.0) ? (1.0 - 1.0 / (2.0 * tau)) * 3.0 * h->body_force : 0.0;
+    c.thermal = h->thermal ? 1 : 0;
+    if (h->thermal) {
+        c.omega_k = h->omega_k;
+        c.beta = h->beta;
+        c.g_buoy = h->g_buoy;
+        c.T_ref = h->T_ref;
+    }
+    return c;
+}
+
+KParams base_params(const lbm2d_solver* h) {
+    KParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.nx = h->nx;
+    p.ny = h->ny;
+    p.N = (long long)h->N;
+    p.flags = h->d_flags;
+    p.rec_info = h->d_rec_info;
+    p.rec_force = h->d_rec_force;
+    p.rec_wd = h->d_rec_wd;
+    p.rec_q = h->d_rec_q;
+    p.rec_uw = h->d_rec_uw;
+    p.interp_classic = h->bb.use_mei ? 0 : 1;
+    p.moving_wall = h->bb.has_moving_wall ? 1 : 0;
+    p.bc_kind = bc_kind(h->case_type);
+    p.thermal = h->thermal ? 1 : 0;
+    p.hook_kind = h->thermal ? h->hook : 0;
+    p.hook_a = h->hook_a;
+    p.hook_b = h->hook_b;
+    p.nan_flag = h->d_nan;
+    const bool shifted = h->storage == ST_FP16 || h->storage == ST_BF16;
+    for (int j = 0; j < 9; ++j) {
+        p.shf[j] = shifted ? float(W[j]) : 0.0f;
+        p.shg[j] = shifted ? float(W[j] * h->T_ref) : 0.0f;
+    }
+    return p;
+}
+
+void apply_collide(KParams& p, const CollideParams& c) {
+    p.collide = 1;
+    p.collision = c.collision;
+    p.s_shear = c.s_shear;
+    p.s_bulk = c.s_bulk;
+    p.s_normal = c.s_normal;
+    p.tau = c.tau;
+    p.cs_sq = c.cs_sq;
+    p.nu = c.nu;
+    p.Fscale = c.Fscale;
+    p.les = c.les;
+    p.omega_k = c.omega_k;
+    p.beta = c.beta;
+    p.g_buoy = c.g_buoy;
+    p.T_ref = c.T_ref;
+}
+
+int ensure_populations(lbm2d_solver* h) {
+    const size_t bytes = h->N * 9 * elem_size(h->storage);
+    int rc;
+    if ((rc = dalloc(h, &h->P[0], bytes))) return rc;
+    if ((rc = dalloc(h, &h->P[1], bytes))) return rc;
+    if (h->thermal) {
+        if ((rc = dalloc(h, &h->G[0], bytes))) return rc;
+        if ((rc = dalloc(h, &h->G[1], bytes))) return rc;
+    }
+    return LBM2D_OK;
+}
+
+// Fill staging with the constructor defaults (f = 0, g = 1; src/lbm_types.hpp:211-216).
+int ensure_stage(lbm2d_solver* h, bool want_g) {
+    int rc;
+    const size_t bytes = h->N * 9 * sizeof(double);
+    if (!h->d_stage_f) {
+        if ((rc = dalloc(h, &h->d_stage_f, bytes))) return rc;
+        CK(cudaMemsetAsync(h->d_stage_f, 0, bytes, h->stream), "memset");
+    }
+    if (want_g && !h->d_stage_g) {
+        if ((rc = dalloc(h, &h->d_stage_g, bytes))) return rc;
+        std::vector<double> ones(std::min<size_t>(h->N * 9, size_t(1) << 20), 1.0);
+        for (size_t off = 0; off < h->N * 9; off += ones.size()) {
+            const size_t cnt = std::min(ones.size(), h->N * 9 - off);
+            CK(cudaMemcpyAsync(h->d_stage_g + off, ones.data(), cnt * sizeof(double), cudaMemcpyHostToDevice,
+                               h->stream),
+               "fill g");
+            CK(cudaStreamSynchronize(h->stream), "sync");
+        }
+    }
+    return LBM2D_OK;
+}
+
+int upload_geometry(lbm2d_solver* h) {
+    if (!h->geom_dirty) return LBM2D_OK;
+    GeometryInput in;
+    in.nx = h->nx;
+    in.ny = h->ny;
+    in.case_type = h->case_type;
+    in.thermal = h->thermal;
+    in.les = h->use_les && h->collision == 0 && h->cs * h->cs > 0.0;
+    in.mask = h->mask.data();
+    in.bb = &h->bb;
+    std::string err;
+    if (!build_geometry(in, h->geo, err)) return fail(h, LBM2D_ERR_INVALID, err);
+    dfree(h, &h->d_rec_info);
+    dfree(h, &h->d_rec_force);
+    dfree(h, &h->d_rec_wd);
+    dfree(h, &h->d_rec_q);
+    dfree(h, &h->d_rec_uw);
+    dfree(h, &h->d_block_slot);
+    dfree(h, &h->d_partials);
+    h->nslots = 0;
+    h->slot_bx = h->slot_by = 0;
+    int rc;
+    if ((rc = dalloc(h, &h->d_flags, h->N * sizeof(uint32_t)))) return rc;
+    CK(cudaMemcpyAsync(h->d_flags, h->geo.flags.data(), h->N * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream),
+       "flags H2D");
+    const size_t nr = h->geo.rec_info.size();
+    if ((rc = dalloc(h, &h->d_rec_info, nr * 4 + 16))) return rc;
+    if ((rc = dalloc(h, &h->d_rec_force, nr * 4 + 16))) return rc;
+    if ((rc = dalloc(h, &h->d_rec_wd, nr * 8 + 16))) return rc;
+    if ((rc = dalloc(h, &h->d_rec_q, nr * 72 + 16))) return rc;
+    if ((rc = dalloc(h, &h->d_rec_uw, nr * 144 + 16))) return rc;
+    if (nr) {
+        CK(cudaMemcpyAsync(h->d_rec_info, h->geo.rec_info.data(), nr * 4, cudaMemcpyHostToDevice, h->stream), "H2D");
+        CK(cudaMemcpyAsync(h->d_rec_force, h->geo.rec_force.data(), nr * 4, cudaMemcpyHostToDevice, h->stream), "H2D");
+        CK(cudaMemcpyAsync(h->d_rec_wd, h->geo.rec_wd.data(), nr * 8, cudaMemcpyHostToDevice, h->stream), "H2D");
+        CK(cudaMemcpyAsync(h->d_rec_q, h->geo.rec_q.data(), nr * 72, cudaMemcpyHostToDevice, h->stream), "H2D");
+        CK(cudaMemcpyAsync(h->d_rec_uw, h->geo.rec_uw.data(), nr * 144, cudaMemcpyHostToDevice, h->stream), "H2D");
+    }
+    CK(cudaStreamSynchronize(h->stream), "geometry upload");
+    h->geom_dirty = false;
+    return LBM2D_OK;
+}
+
+int ensure_slots(lbm2d_solver* h) {
+    if (h->slot_bx == h->bx && h->slot_by == h->by && h->d_block_slot) return LBM2D_OK;
+    std::vector<int> slots;
+    h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx, h->by, slots);
+    dfree(h, &h->d_block_slot);
+    dfree(h, &h->d_partials);
+    int rc;
+    if ((rc = dalloc(h, &h->d_block_slot, slots.size() * sizeof(int)))) return rc;
+    if ((rc = dalloc(h, &h->d_partials, (size_t)std::max(h->nslots, 1) * 2 * sizeof(double)))) return rc;
+    CK(cudaMemcpyAsync(h->d_block_slot, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream),
+       "slots H2D");
+    CK(cudaStreamSynchronize(h->stream), "slots");
+    h->slot_bx = h->bx;
+    h->slot_by = h->by;
+    return LBM2D_OK;
+}
+
+// Parameters of a kernel that rebuilds the reference state S_n of the last
+// step: S_n is pulled from the post-collision populations of the step BEFORE
+// it (the other ping-pong buffer), with the boundary velocity of step n.
+KParams rebuild_params(const lbm2d_solver* h) {
+    KParams p = base_params(h);
+    p.fin = h->P[h->cur ^ 1];
+    p.gin = h->G[h->cur ^ 1];
+    p.u_bc = h->u_last;
+    return p;
+}
+
+// COLLIDED -> STAGED: rebuild the reference state S from the stored populations.
+int materialize(lbm2d_solver* h) {
+    if (h->staged) return LBM2D_OK;
+    int rc;
+    if ((rc = ensure_stage(h, h->thermal))) return rc;
+    if (h->steps_since_collide > 0) {
+        KParams p = rebuild_params(h);
+        ROut o;
+        std::memset(&o, 0, sizeof(o));
+        o.f_aos = h->d_stage_f;
+        o.g_aos = h->thermal ? h->d_stage_g : nullptr;
+        int e = launch_readback(h->storage, p, o, h->stream);
+        ++h->launches;
+        if (e) return cuda_fail(h, (cudaError_t)e, "readback");
+    }  // else: no step since the prologue, staging still holds S
+    h->staged = true;
+    h->stage_f_valid = true;
+    if (h->thermal) h->stage_g_valid = true;
+    return LBM2D_OK;
+}
+
+// Any change of geometry / case / thermal switch while COLLIDED must first
+// rebuild S with the settings that produced the stored populations.
+int before_setting_change(lbm2d_solver* h) {
+    if (h->staged) return LBM2D_OK;
+    if (h->geom_dirty) {
+        // geometry already changed under a collided state cannot happen: every
+        // setter calls this function first.
+        return fail(h, LBM2D_ERR_STATE, "internal: dirty geometry under collided state");
+    }
+    return materialize(h);
+}
+
+int prologue(lbm2d_solver* h, const CollideParams& c) {
+    int rc;
+    if ((rc = ensure_populations(h))) return rc;
+    if ((rc = ensure_stage(h, h->thermal))) return rc;
+    KParams p = base_params(h);
+    apply_collide(p, c);
+    p.fout = h->P[h->cur];
+    p.gout = h->G[h->cur];
+    int e = launch_prologue(h->storage, p, h->d_stage_f, h->thermal ? h->d_stage_g : nullptr, h->stream);
+    ++h->launches;
+    if (e) return cuda_fail(h, (cudaError_t)e, "prologue");
+    h->staged = false;
+    h->cp_of_P = c;
+    h->steps_since_collide = 0;
+    return LBM2D_OK;
+}
+
+int check_handle(lbm2d_solver* h) {
+    if (!h) return LBM2D_ERR_INVALID;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    return LBM2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm2d_last_error(const lbm2d_solver* h) { return h ? h->err.c_str() : g_global_err.c_str(); }
+const char* lbm2d_global_error(void) { return g_global_err.c_str(); }
+
+int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
+    if (!cfg || !out) {
+        g_global_err = "null argument";
+        return LBM2D_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (cfg->nx < 3 || cfg->ny < 3 || (long long)cfg->nx * cfg->ny * 9 > (1LL << 40)) {
+        g_global_err = "grid must be at least 3x3";
+        return LBM2D_ERR_INVALID;
+    }
+    if (cfg->storage < 0 || cfg->storage > 3 || cfg->collision < 0 || cfg->collision > 1 || cfg->case_type < 0 ||
+        cfg->case_type > 13) {
+        g_global_err = "invalid storage, collision or case";
+        return LBM2D_ERR_INVALID;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        g_global_err = "no CUDA device";
+        return LBM2D_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) {
+        g_global_err = "device ordinal out of range";
+        return LBM2D_ERR_INVALID;
+    }
+    auto* h = new (std::nothrow) lbm2d_solver();
+    if (!h) {
+        g_global_err = "host allocation failed";
+        return LBM2D_ERR_OOM;
+    }
+    h->device = cfg->device;
+    h->nx = cfg->nx;
+    h->ny = cfg->ny;
+    h->N = (size_t)cfg->nx * cfg->ny;
+    h->case_type = cfg->case_type;
+    h->collision = cfg->collision;
+    h->use_les = cfg->use_les;
+    h->cs = cfg->cs;
+    h->storage = cfg->storage;
+    h->mask.assign(h->N, 0);
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    int rc = LBM2D_OK;
+    if (e != cudaSuccess) {
+        g_global_err = std::string("stream: ") + cudaGetErrorString(e);
+        delete h;
+        return LBM2D_ERR_CUDA;
+    }
+    if (!rc) rc = dalloc(h, &h->d_nan, 16);
+    if (!rc) rc = dalloc(h, &h->d_counter, 16);
+    if (!rc) rc = dalloc(h, &h->d_last, 16);
+    if (!rc) rc = dalloc(h, &h->d_hist, (size_t)h->hist_cap * 2 * sizeof(double));
+    if (!rc) rc = ensure_stage(h, false);
+    if (!rc) rc = ensure_populations(h);
+    if (!rc) {
+        cudaMemsetAsync(h->d_nan, 0, 16, h->stream);
+        cudaMemsetAsync(h->d_counter, 0, 16, h->stream);
+        cudaMemsetAsync(h->d_last, 0, 16, h->stream);
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = LBM2D_ERR_CUDA;
+    }
+    if (rc) {
+        g_global_err = h->err;
+        lbm2d_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return LBM2D_OK;
+}
+
+int lbm2d_destroy(lbm2d_solver* h) {
+    if (!h) return LBM2D_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
+                    h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
+                    h->d_counter, h->d_last, h->d_nan, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_case(lbm2d_solver* h, int case_type, int collision, int use_les, double cs) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (case_type < 0 || case_type > 13 || collision < 0 || collision > 1)
+        return fail(h, LBM2D_ERR_INVALID, "invalid case or collision");
+    if (case_type == h->case_type && collision == h->collision && use_les == h->use_les && cs == h->cs)
+        return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    h->case_type = case_type;
+    h->collision = collision;
+    h->use_les = use_les;
+    h->cs = cs;
+    h->geom_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_mask(lbm2d_solver* h, const uint8_t* obstacle) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!obstacle) return fail(h, LBM2D_ERR_INVALID, "null mask");
+    bool same = true;
+    for (size_t k = 0; k < h->N && same; ++k) same = (obstacle[k] != 0) == (h->mask[k] != 0);
+    if (same && !h->geom_dirty) return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    for (size_t k = 0; k < h->N; ++k) h->mask[k] = obstacle[k] ? 1 : 0;
+    h->geom_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_bb_cylinder(lbm2d_solver* h, double cx, double cy, double radius) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (h->bb.cx == cx && h->bb.cy == cy && h->bb.radius == radius) return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    h->bb.cx = cx;
+    h->bb.cy = cy;
+    h->bb.radius = radius;
+    h->geom_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_bb_polygon(lbm2d_solver* h, const double* xy, int n) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (n < 0 || (n > 0 && !xy)) return fail(h, LBM2D_ERR_INVALID, "bad polygon");
+    std::vector<double> poly(xy, xy + 2 * (size_t)n);
+    if (h->bb.is_polygon == (n > 0) && h->bb.poly == poly) return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    h->bb.poly = poly;
+    h->bb.is_polygon = n > 0;
+    h->geom_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_moving_wall(lbm2d_solver* h, int on, double omega, double rcx, double rcy) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (h->bb.has_moving_wall == (on != 0) && h->bb.omega == omega && h->bb.rot_cx == rcx && h->bb.rot_cy == rcy)
+        return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    h->bb.has_moving_wall = on != 0;
+    h->bb.omega = omega;
+    h->bb.rot_cx = rcx;
+    h->bb.rot_cy = rcy;
+    h->geom_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_mei(lbm2d_solver* h, int on) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (h->bb.use_mei == (on != 0)) return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    h->bb.use_mei = on != 0;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_body_force(lbm2d_solver* h, double fx) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    h->body_force = fx;  // takes effect through the collision parameters of the next step
+    return LBM2D_OK;
+}
+
+int lbm2d_set_thermal(lbm2d_solver* h, int use, double T_ref, double alpha, double omega_k, double beta,
+                      double g_buoyancy) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    const bool on = use != 0;
+    if (on != h->thermal || (on && T_ref != h->T_ref)) {
+        if ((rc = before_setting_change(h))) return rc;
+        if (on && (rc = ensure_stage(h, true))) return rc;
+        h->geom_dirty = true;
+    }
+    h->thermal = on;
+    h->T_ref = T_ref;
+    h->alpha = alpha;
+    h->omega_k = omega_k;
+    h->beta = beta;
+    h->g_buoy = g_buoyancy;
+    if (on && (rc = ensure_populations(h))) return rc;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_thermal_hook(lbm2d_solver* h, int kind, double Ta, double Tb) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (kind < 0 || kind > 2) return fail(h, LBM2D_ERR_INVALID, "unknown thermal hook");
+    if (kind == h->hook && Ta == h->hook_a && Tb == h->hook_b) return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;
+    h->hook = kind;
+    h->hook_a = Ta;
+    h->hook_b = Tb;
+    return LBM2D_OK;
+}
+
+static int upload_common(lbm2d_solver* h, const double* src, bool is_g, cudaMemcpyKind kind) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!src) return fail(h, LBM2D_ERR_INVALID, "null populations");
+    if ((rc = materialize(h))) return rc;
+    if ((rc = ensure_stage(h, true))) return rc;
+    double* dst = is_g ? h->d_stage_g : h->d_stage_f;
+    CK(cudaMemcpyAsync(dst, src, h->N * 9 * sizeof(double), kind, h->stream), "upload");
+    if (kind == cudaMemcpyHostToDevice) CK(cudaStreamSynchronize(h->stream), "upload");
+    (is_g ? h->stage_g_valid : h->stage_f_valid) = true;
+    h->staged = true;
+    CK(cudaMemsetAsync(h->d_counter, 0, 8, h->stream), "reset history");
+    h->steps_done = 0;
+    return LBM2D_OK;
+}
+
+int lbm2d_upload_f(lbm2d_solver* h, const double* f) { return upload_common(h, f, false, cudaMemcpyHostToDevice); }
+int lbm2d_upload_g(lbm2d_solver* h, const double* g) { return upload_common(h, g, true, cudaMemcpyHostToDevice); }
+int lbm2d_upload_f_device(lbm2d_solver* h, const double* d_f) {
+    return upload_common(h, d_f, false, cudaMemcpyDeviceToDevice);
+}
+
+int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (nsteps < 0) return fail(h, LBM2D_ERR_INVALID, "negative step count");
+    if (nsteps == 0) return LBM2D_OK;
+    if (!(tau > 0.0)) return fail(h, LBM2D_ERR_INVALID, "tau must be positive");
+    const CollideParams c = collide_params(h, tau);
+    if (!h->staged && !(c == h->cp_of_P)) {
+        if ((rc = materialize(h))) return rc;
+    }
+    if ((rc = upload_geometry(h))) return rc;
+    if ((rc = ensure_slots(h))) return rc;
+    if (h->staged) {
+        if ((rc = prologue(h, c))) return rc;
+    }
+    KParams p = base_params(h);
+    apply_collide(p, c);
+    p.u_bc = u_inflow;
+    p.block_slot = h->nslots > 0 ? h->d_block_slot : nullptr;
+    p.partials = h->d_partials;
+    for (int k = 0; k < nsteps; ++k) {
+        p.fin = h->P[h->cur];
+        p.fout = h->P[h->cur ^ 1];
+        p.gin = h->G[h->cur];
+        p.gout = h->G[h->cur ^ 1];
+        p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (h->profiling) {
+            if (h->ev_used + 2 > h->ev_pool.size()) {
+                for (int k2 = 0; k2 < 64; ++k2) {
+                    cudaEvent_t ev;
+                    CK(cudaEventCreate(&ev), "event");
+                    h->ev_pool.push_back(ev);
+                }
+            }
+            e0 = h->ev_pool[h->ev_used++];
+            e1 = h->ev_pool[h->ev_used++];
+            CK(cudaEventRecord(e0, h->stream), "event");
+        }
+        int e = launch_step(h->storage, p, h->bx, h->by, h->stream);
+        if (e1) CK(cudaEventRecord(e1, h->stream), "event");
+        ++h->launches;
+        if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
+        if (h->nslots > 0) {
+            e = launch_force_reduce(h->d_partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last,
+                                    h->stream);
+            ++h->launches;
+            if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");
+        }
+        h->cur ^= 1;
+        ++h->steps_since_collide;
+        ++h->steps_done;
+    }
+    h->u_last = u_inflow;
+    return LBM2D_OK;
+}
+
+int lbm2d_synchronize(lbm2d_solver* h) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    CK(cudaStreamSynchronize(h->stream), "synchronize");
+    unsigned int flag = 0;
+    CK(cudaMemcpy(&flag, h->d_nan, sizeof(flag), cudaMemcpyDeviceToHost), "nan flag");
+    if (flag) {
+        cudaMemset(h->d_nan, 0, sizeof(flag));
+        return fail(h, LBM2D_ERR_NAN, "a non-finite or zero density was produced");
+    }
+    return LBM2D_OK;
+}
+
+int lbm2d_force_sums(lbm2d_solver* h, double* fx, double* fy) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    double v[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(v, h->d_last, sizeof(v), cudaMemcpyDeviceToHost, h->stream), "force D2H");
+    CK(cudaStreamSynchronize(h->stream), "force sync");
+    if (fx) *fx = v[0];
+    if (fy) *fy = v[1];
+    return LBM2D_OK;
+}
+
+int lbm2d_force_history(lbm2d_solver* h, double* fx, double* fy, int n, int* n_recorded) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, h->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream), "counter");
+    CK(cudaStreamSynchronize(h->stream), "sync");
+    const long long rec = std::min<long long>((long long)cnt, h->hist_cap);
+    if (n_recorded) *n_recorded = (int)cnt;
+    const long long m = std::min<long long>(rec, n);
+    if (m > 0) {
+        std::vector<double> buf((size_t)m * 2);
+        CK(cudaMemcpy(buf.data(), h->d_hist, buf.size() * sizeof(double), cudaMemcpyDeviceToHost), "hist");
+        for (long long k = 0; k < m; ++k) {
+            if (fx) fx[k] = buf[2 * k];
+            if (fy) fy[k] = buf[2 * k + 1];
+        }
+    }
+    return LBM2D_OK;
+}
+
+int lbm2d_force_history_reset(lbm2d_solver* h) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    CK(cudaMemsetAsync(h->d_counter, 0, 8, h->stream), "reset");
+    return LBM2D_OK;
+}
+
+int lbm2d_download_f(lbm2d_solver* h, double* f) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!f) return fail(h, LBM2D_ERR_INVALID, "null output");
+    if ((rc = ensure_stage(h, h->thermal))) return rc;
+    if (!h->staged) {
+        // rebuild S into staging, keep the collided populations as the live state
+        if ((rc = materialize(h))) return rc;
+        h->staged = false;
+    }
+    CK(cudaMemcpyAsync(f, h->d_stage_f, h->N * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H f");
+    CK(cudaStreamSynchronize(h->stream), "D2H f");
+    return LBM2D_OK;
+}
+
+int lbm2d_download_f_device(lbm2d_solver* h, double* d_f) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!d_f) return fail(h, LBM2D_ERR_INVALID, "null output");
+    if ((rc = ensure_stage(h, h->thermal))) return rc;
+    if (!h->staged) {
+        if ((rc = materialize(h))) return rc;
+        h->staged = false;
+    }
+    CK(cudaMemcpyAsync(d_f, h->d_stage_f, h->N * 9 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream), "D2D");
+    return LBM2D_OK;
+}
+
+int lbm2d_download_g(lbm2d_solver* h, double* g) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!g) return fail(h, LBM2D_ERR_INVALID, "null output");
+    if ((rc = ensure_stage(h, true))) return rc;
+    if (!h->staged && h->thermal) {
+        if ((rc = materialize(h))) return rc;
+        h->staged = false;
+    }
+    CK(cudaMemcpyAsync(g, h->d_stage_g, h->N * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H g");
+    CK(cudaStreamSynchronize(h->stream), "D2H g");
+    return LBM2D_OK;
+}
+
+int lbm2d_download_force_field(lbm2d_solver* h, double* fx, double* fy) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!fx || !fy) return fail(h, LBM2D_ERR_INVALID, "null output");
+    if (h->staged || h->steps_since_collide == 0) {
+        // no step since the upload: the reference's fields are still the zeros
+        // of LBMCapabilities::reset_forces (or the previous step's values,
+        // which this handle does not keep across uploads)
+        std::fill(fx, fx + h->N, 0.0);
+        std::fill(fy, fy + h->N, 0.0);
+        return LBM2D_OK;
+    }
+    if ((rc = dalloc(h, &h->d_fx, h->N * sizeof(double)))) return rc;
+    if ((rc = dalloc(h, &h->d_fy, h->N * sizeof(double)))) return rc;
+    KParams p = rebuild_params(h);
+    ROut o;
+    std::memset(&o, 0, sizeof(o));
+    o.fx = h->d_fx;
+    o.fy = h->d_fy;
+    int e = launch_readback(h->storage, p, o, h->stream);
+    ++h->launches;
+    if (e) return cuda_fail(h, (cudaError_t)e, "force field");
+    CK(cudaMemcpyAsync(fx, h->d_fx, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H fx");
+    CK(cudaMemcpyAsync(fy, h->d_fy, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H fy");
+    CK(cudaStreamSynchronize(h->stream), "D2H force");
+    return LBM2D_OK;
+}
+
+int lbm2d_download_macros(lbm2d_solver* h, double* rho, double* u, double* v, double* T) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (h->staged || h->steps_since_collide == 0) return fail(h, LBM2D_ERR_STATE, "no step since the last upload");
+    double* bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    double* outs[4] = {rho, u, v, (h->thermal ? T : nullptr)};
+    for (int k = 0; k < 4; ++k) {
+        if (!outs[k]) continue;
+        if (cudaMalloc(&bufs[k], h->N * sizeof(double)) != cudaSuccess) {
+            for (int j = 0; j < k; ++j)
+                if (bufs[j]) cudaFree(bufs[j]);
+            return fail(h, LBM2D_ERR_OOM, "macros buffer");
+        }
+    }
+    KParams p = rebuild_params(h);
+    ROut o;
+    std::memset(&o, 0, sizeof(o));
+    o.rho = bufs[0];
+    o.u = bufs[1];
+    o.v = bufs[2];
+    o.T = bufs[3];
+    int e = launch_readback(h->storage, p, o, h->stream);
+    ++h->launches;
+    int ret = LBM2D_OK;
+    if (e) ret = cuda_fail(h, (cudaError_t)e, "macros");
+    for (int k = 0; k < 4 && !ret; ++k)
+        if (bufs[k]) {
+            cudaError_t ce = cudaMemcpyAsync(outs[k], bufs[k], h->N * sizeof(double), cudaMemcpyDeviceToHost,
+                                             h->stream);
+            if (ce != cudaSuccess) ret = cuda_fail(h, ce, "D2H macros");
+        }
+    cudaStreamSynchronize(h->stream);
+    for (int k = 0; k < 4; ++k)
+        if (bufs[k]) cudaFree(bufs[k]);
+    return ret;
+}
+
+int lbm2d_download_wall_dist(lbm2d_solver* h, double* wd) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!wd) return fail(h, LBM2D_ERR_INVALID, "null output");
+    std::vector<double> d;
+    wall_distance(h->nx, h->ny, h->mask.data(), d);
+    std::copy(d.begin(), d.end(), wd);
+    return LBM2D_OK;
+}
+
+int lbm2d_get_info(lbm2d_solver* h, lbm2d_info* info) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (!info) return fail(h, LBM2D_ERR_INVALID, "null output");
+    if ((rc = upload_geometry(h))) return rc;
+    info->nx = h->nx;
+    info->ny = h->ny;
+    info->storage = h->storage;
+    info->bytes_per_update = 2.0 * 9.0 * (double)elem_size(h->storage) * (h->thermal ? 2.0 : 1.0);
+    info->device_bytes = h->device_bytes;
+    info->n_boundary_nodes = (int)h->geo.rec_info.size();
+    info->n_force_nodes = h->geo.n_force_nodes;
+    info->steps_done = h->steps_done;
+    info->block_x = h->bx;
+    info->block_y = h->by;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_block(lbm2d_solver* h, int bx, int by) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (bx == 0 && by == 0) {
+        bx = 128;
+        by = 2;
+    }
+    if (bx <= 0 || by <= 0 || bx * by > 512 || (bx * by) % 32 != 0)
+        return fail(h, LBM2D_ERR_INVALID, "block must have a multiple of 32 threads, at most 512");
+    h->bx = bx;
+    h->by = by;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_profiling(lbm2d_solver* h, int on) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    h->profiling = on != 0;
+    return LBM2D_OK;
+}
+
+int lbm2d_profile(lbm2d_solver* h, double* ms, long long* n) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    CK(cudaStreamSynchronize(h->stream), "profile sync");
+    double total = 0.0;
+    for (size_t k = 0; k + 1 < h->ev_used; k += 2) {
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, h->ev_pool[k], h->ev_pool[k + 1]), "elapsed");
+        total += t;
+    }
+    if (ms) *ms = total;
+    if (n) *n = (long long)(h->ev_used / 2);
+    h->ev_used = 0;
+    return LBM2D_OK;
+}
+
+void* lbm2d_stream(lbm2d_solver* h) { return h ? (void*)h->stream : nullptr; }
+long long lbm2d_launch_count(lbm2d_solver* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

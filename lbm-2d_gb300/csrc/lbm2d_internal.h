@@ -1,0 +1,97 @@
+// lbm2d_internal.h -- types shared by the CUDA kernels and the host runtime.
+//
+// Device data layout (one solver instance)
+//   populations : structure-of-arrays, 9 planes of nx*ny elements each,
+//                 plane j holds direction j for node y*nx + x.  Two buffers
+//                 (ping-pong).  What is stored is the POST-COLLISION state of
+//                 the last step: the step kernel pulls from it, rebuilds the
+//                 reference's post-stream/post-boundary state in registers,
+//                 collides, and writes the next post-collision state.
+//   flags       : one uint32 per node
+//                   bit 0      solid
+//                   bit 1      boundary node (has a boundary record)
+//                   bits 2..31 record index (boundary) or LES wall distance
+//                              (fluid; WD_UNREACHED means "no obstacle")
+//   records     : per boundary node: slot types, thermal bounce mask, force
+//                 mask, wall distance, and per-slot q / wall velocity for
+//                 interpolated links.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace lbm2d {
+
+constexpr uint32_t FLAG_SOLID = 1u;
+constexpr uint32_t FLAG_BOUNDARY = 2u;
+constexpr uint32_t WD_UNREACHED = 0x3FFFFFFFu;  // stands for the reference's 1e9
+constexpr uint32_t MAX_RECORDS = 0x3FFFFFFFu;
+
+// Slot types (2 bits per pull slot j) in rec_info bits 0..17.
+constexpr uint32_t SLOT_REGULAR = 0;  // pull from the neighbour (wrapped)
+constexpr uint32_t SLOT_SIMPLE_BB = 1;  // own post-collision value of bb(j)
+constexpr uint32_t SLOT_INTERP = 2;  // interpolated bounce-back (Mei or Bouzidi)
+constexpr uint32_t SLOT_ZERO = 3;  // no source (x outside the domain)
+// rec_info bits 18..26: thermal slot j bounces (adiabatic) instead of pulling.
+constexpr int REC_GBB_SHIFT = 18;
+
+// Boundary-condition families of execute_time_step (src/lbm.hpp:531-540).
+enum BcKind : int { BC_NONE = 0, BC_LID = 1, BC_INFLOW = 2, BC_STEP = 3 };
+
+enum Storage : int { ST_FP32 = 0, ST_FP16 = 1, ST_BF16 = 2, ST_FP64 = 3 };
+
+struct KParams {
+    int nx, ny;
+    long long N;  // nx*ny
+    // populations
+    const void* fin;
+    void* fout;
+    const void* gin;
+    void* gout;
+    // geometry
+    const uint32_t* flags;
+    const uint32_t* rec_info;
+    const uint32_t* rec_force;  // force slot mask per record (bits 0..8)
+    const double* rec_wd;
+    const double* rec_q;   // [rec*9 + j]
+    const double* rec_uw;  // [(rec*9 + j)*2 + {0,1}]
+    int interp_classic;    // 1: classic Bouzidi (+Ladd), 0: Mei
+    int moving_wall;
+    // boundary conditions of THIS step
+    int bc_kind;
+    double u_bc;
+    // collision parameters (for the collision that ends the step)
+    int collide;  // 0: rebuild state only (readback)
+    int collision;  // 0 MRT, 1 BGK
+    double s_shear, s_bulk, s_normal, tau, cs_sq, nu, Fscale;
+    int les;
+    int thermal;
+    double omega_k, beta, g_buoy, T_ref;
+    int hook_kind;
+    double hook_a, hook_b;
+    // storage shifts (FP16/BF16 store f - w*rho0, g - w*T_ref)
+    float shf[9], shg[9];
+    // force reduction
+    const int* block_slot;  // per block: slot index or -1
+    double* partials;       // [slot*2 + {0,1}]
+    unsigned int* nan_flag;
+    // solid nodes whose state can no longer change may skip their stores
+    int skip_settled_solids;
+};
+
+// Readback outputs (any may be null).
+struct ROut {
+    double* f_aos;
+    double* g_aos;
+    double *rho, *u, *v, *T;
+    double *fx, *fy;
+};
+
+// Launchers (lbm2d_kernels.cu).  All return a cudaError_t as int.
+int launch_step(int storage, const KParams& p, int bx, int by, void* stream);
+int launch_readback(int storage, const KParams& p, const ROut& o, void* stream);
+// Collide an FP64 AoS state S (device) into the stored post-collision state.
+int launch_prologue(int storage, const KParams& p, const double* f_aos, const double* g_aos, void* stream);
+int launch_force_reduce(const double* partials, int nslots, double* hist, int hist_cap,
+                        unsigned long long* counter, double* last, void* stream);
+
+}  // namespace lbm2d

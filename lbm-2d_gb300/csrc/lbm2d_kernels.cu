@@ -1,0 +1,615 @@
+// lbm2d_kernels.cu -- sm_103a kernels of the D2Q9 lattice-Boltzmann step.
+//
+// One fused, bandwidth-bound pull kernel per time step.  For node m it
+//   1. pulls the post-collision populations of the previous step from the
+//      9 neighbour positions (SoA planes, coalesced 32-bit/16-bit loads),
+//   2. rebuilds the reference's post-stream state: bounce-back, interpolated
+//      bounce-back (Mei / Filippova-Hanel or classic Bouzidi with the Ladd
+//      wall term) and the "no source" slots, from a per-node boundary record,
+//   3. applies the boundary conditions of execute_time_step (lid, Zou/He
+//      inlet, parabolic step inlet, zero-gradient outlet) and, if enabled,
+//      a driver's post-step thermal pass,
+//   4. accumulates the momentum-exchange force of its links (FP64),
+//   5. collides (MRT d'Humieres or BGK, Smagorinsky/Van Driest LES, body
+//      force, thermal DDF with Boussinesq/Guo buoyancy) in FP32 (FP64 for the
+//      FP64 storage variant) and writes the next post-collision state.
+// Items 1-3 are the reference's steps streaming -> swap -> boundary
+// conditions (src/lbm.hpp:400-540); item 4 is its force pass (:543-581) and
+// item 5 is the collision that opens the next call (:300-397).  Storing the
+// post-collision state makes the writes aligned and lets the force come from
+// registers; the readback kernel rebuilds the reference's state on demand
+// with the same device functions.
+//
+// No tensor cores: the step is a stencil with ~2-3 flop per byte.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lbm2d_internal.h"
+
+namespace lbm2d {
+namespace {
+
+// D2Q9 lattice, direction order of src/lbm_types.hpp:41-55.
+__host__ __device__ constexpr int CXf(int i) { return (i == 1 || i == 5 || i == 8) ? 1 : ((i == 3 || i == 6 || i == 7) ? -1 : 0); }
+__host__ __device__ constexpr int CYf(int i) { return (i == 2 || i == 5 || i == 6) ? 1 : ((i == 4 || i == 7 || i == 8) ? -1 : 0); }
+__host__ __device__ constexpr int BBf(int i) { return i == 0 ? 0 : (i < 5 ? ((i + 1) % 4 + 1) : ((i - 5 + 2) % 4 + 5)); }
+static_assert(BBf(1) == 3 && BBf(2) == 4 && BBf(3) == 1 && BBf(4) == 2, "bounce-back map");
+static_assert(BBf(5) == 7 && BBf(6) == 8 && BBf(7) == 5 && BBf(8) == 6, "bounce-back map");
+__host__ __device__ constexpr double wgt(int i) { return i == 0 ? 4.0 / 9.0 : (i < 5 ? 1.0 / 9.0 : 1.0 / 36.0); }
+
+// ----------------------------------------------------------------- storage formats
+template <class T>
+struct Pop;
+template <>
+struct Pop<float> {
+    using R = float;
+    static __device__ __forceinline__ R ld(const float* __restrict__ p, size_t i, float) { return __ldg(p + i); }
+    static __device__ __forceinline__ void st(float* __restrict__ p, size_t i, R v, float) { p[i] = v; }
+};
+template <>
+struct Pop<double> {
+    using R = double;
+    static __device__ __forceinline__ R ld(const double* __restrict__ p, size_t i, float) { return __ldg(p + i); }
+    static __device__ __forceinline__ void st(double* __restrict__ p, size_t i, R v, float) { p[i] = v; }
+};
+template <>
+struct Pop<__half> {
+    using R = float;
+    static __device__ __forceinline__ R ld(const __half* __restrict__ p, size_t i, float sh) {
+        return __half2float(__ldg(p + i)) + sh;
+    }
+    static __device__ __forceinline__ void st(__half* __restrict__ p, size_t i, R v, float sh) {
+        p[i] = __float2half_rn(v - sh);
+    }
+};
+template <>
+struct Pop<__nv_bfloat16> {
+    using R = float;
+    static __device__ __forceinline__ R ld(const __nv_bfloat16* __restrict__ p, size_t i, float sh) {
+        return __bfloat162float(__ldg(p + i)) + sh;
+    }
+    static __device__ __forceinline__ void st(__nv_bfloat16* __restrict__ p, size_t i, R v, float sh) {
+        p[i] = __float2bfloat16_rn(v - sh);
+    }
+};
+
+// ----------------------------------------------------------------- lattice math
+// compute_equilibrium, src/lbm_types.hpp:269-273
+template <class R>
+__device__ __forceinline__ R feq(int i, R rho, R u, R v) {
+    R ed = R(CXf(i)) * u + R(CYf(i)) * v;
+    R usq = u * u + v * v;
+    return R(wgt(i)) * rho * (R(1) + R(3) * ed + R(4.5) * ed * ed - R(1.5) * usq);
+}
+
+// compute_macros, src/lbm_types.hpp:278-288
+template <class R>
+__device__ __forceinline__ void macros(const R f[9], R& rho, R& u, R& v) {
+    rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
+    R mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    R my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    u = mx / rho;
+    v = my / rho;
+}
+
+template <class R>
+__device__ __forceinline__ R clamp_rate(R s) { return s < R(0.5) ? R(0.5) : (s > R(1.99) ? R(1.99) : s); }
+
+// ----------------------------------------------------------------- pull + rebuild
+template <class T>
+__device__ __forceinline__ void pull(const KParams& p, const T* __restrict__ P, const float* sh, int x, int y,
+                                     typename Pop<T>::R f[9]) {
+    const int nx = p.nx, ny = p.ny;
+    const size_t N = (size_t)p.N;
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
+    // slot j pulls from (x - cx_j, y - cy_j), wrapped; records override the
+    // slots whose source is solid or outside the domain.
+    f[0] = Pop<T>::ld(P, r0 + x, sh[0]);
+    f[1] = Pop<T>::ld(P + N, r0 + xm, sh[1]);
+    f[2] = Pop<T>::ld(P + 2 * N, rm + x, sh[2]);
+    f[3] = Pop<T>::ld(P + 3 * N, r0 + xp, sh[3]);
+    f[4] = Pop<T>::ld(P + 4 * N, rp + x, sh[4]);
+    f[5] = Pop<T>::ld(P + 5 * N, rm + xm, sh[5]);
+    f[6] = Pop<T>::ld(P + 6 * N, rm + xp, sh[6]);
+    f[7] = Pop<T>::ld(P + 7 * N, rp + xp, sh[7]);
+    f[8] = Pop<T>::ld(P + 8 * N, rp + xm, sh[8]);
+}
+
+// Rebuild the non-regular f slots of a boundary node from its record
+// (streaming bounce-back src/lbm.hpp:418-428, :449-452, :470-480 and
+// apply_bouzidi_bb :226-288).
+template <class T>
+__device__ __forceinline__ void fix_f(const KParams& p, const T* __restrict__ P, int x, int y, uint32_t rec,
+                                   typename Pop<T>::R f[9]) {
+    using R = typename Pop<T>::R;
+    const uint32_t types = p.rec_info[rec] & 0x3FFFFu;
+    if (types == 0) return;
+    const size_t N = (size_t)p.N;
+    const size_t n = (size_t)y * p.nx + x;
+    R own[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) own[j] = Pop<T>::ld(P + j * N, n, p.shf[j]);
+    R rho, u, v;
+    macros(own, rho, u, v);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const uint32_t t = (types >> (2 * j)) & 3u;
+        if (t == SLOT_SIMPLE_BB) {
+            f[j] = own[BBf(j)];
+        } else if (t == SLOT_ZERO) {
+            f[j] = R(0);
+        } else if (t == SLOT_INTERP) {
+            const int i = BBf(j);  // the reference's link direction (node -> solid)
+            const R q = R(p.rec_q[(size_t)rec * 9 + j]);
+            R uwx = R(0), uwy = R(0);
+            if (p.moving_wall) {
+                uwx = R(p.rec_uw[((size_t)rec * 9 + j) * 2]);
+                uwy = R(p.rec_uw[((size_t)rec * 9 + j) * 2 + 1]);
+            }
+            const R ed = R(CXf(i)) * uwx + R(CYf(i)) * uwy;
+            R fbb;
+            if (!p.interp_classic) {
+                // Mei (1999) / Filippova-Hanel (1998), src/lbm.hpp:234-256
+                fbb = q * feq<R>(i, rho, uwx, uwy) + (R(1) - q) * own[i] +
+                      (R(2) * q - R(1)) * R(wgt(i)) * rho * ed * R(3);
+            } else {
+                // classic Bouzidi (2001), src/lbm.hpp:257-273, + Ladd :276-285
+                if (q < R(0.5)) {
+                    const int sx = x - CXf(i), sy = y - CYf(i);
+                    R fsrc = own[i];
+                    if (sx >= 0 && sx < p.nx && sy >= 0 && sy < p.ny)
+                        fsrc = Pop<T>::ld(P + i * N, (size_t)sy * p.nx + sx, p.shf[i]);
+                    fbb = R(2) * q * own[i] + (R(1) - R(2) * q) * fsrc;
+                } else {
+                    const R inv2q = R(1) / (R(2) * q);
+                    fbb = inv2q * own[i] + (R(1) - inv2q) * own[j];
+                }
+                if (p.moving_wall) fbb -= R(2) * R(wgt(i)) * rho * ed * R(3);
+            }
+            f[j] = fbb;
+        }
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void fix_g(const KParams& p, const T* __restrict__ G, int x, int y, uint32_t rec,
+                                   typename Pop<T>::R g[9]) {
+    using R = typename Pop<T>::R;
+    const uint32_t m = (p.rec_info[rec] >> REC_GBB_SHIFT) & 0x1FFu;
+    if (m == 0) return;
+    const size_t N = (size_t)p.N;
+    const size_t n = (size_t)y * p.nx + x;
+    R own[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) own[j] = Pop<T>::ld(G + j * N, n, p.shg[j]);
+#pragma unroll
+    for (int j = 0; j < 9; ++j)
+        if (m & (1u << j)) g[j] = own[BBf(j)];  // adiabatic bounce-back, src/lbm.hpp:512-520
+}
+
+// Zou/He velocity inlet on one node, src/lbm.hpp:21-34 / :40-58
+template <class R>
+__device__ __forceinline__ void zou_he(R f[9], R uin) {
+    R rho = (f[0] + f[2] + f[4] + R(2) * (f[3] + f[6] + f[7])) / (R(1) - uin);
+    f[1] = f[3] + R(2.0 / 3.0) * rho * uin;
+    f[5] = f[7] + R(1.0 / 6.0) * rho * uin;
+    f[8] = f[6] + R(1.0 / 6.0) * rho * uin;
+}
+
+// The reference's state after streaming, boundary conditions and (optionally)
+// a driver thermal pass, for node (x, y).  f/g hold it on return.
+template <class T, bool TH>
+__device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint32_t fl, typename Pop<T>::R f[9],
+                                            typename Pop<T>::R g[9]) {
+    using R = typename Pop<T>::R;
+    const T* __restrict__ Pf = static_cast<const T*>(p.fin);
+    const bool outflow_col = (p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x == p.nx - 1;
+    // zero-gradient outlet: column NX-1 takes NX-2's post-stream state (src/lbm.hpp:63-73)
+    const int sx = outflow_col ? x - 1 : x;
+    const uint32_t sfl = outflow_col ? __ldg(p.flags + (size_t)y * p.nx + sx) : fl;
+    if (sfl & FLAG_SOLID) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) f[j] = R(0);
+    } else {
+        pull<T>(p, Pf, p.shf, sx, y, f);
+        if (sfl & FLAG_BOUNDARY) fix_f<T>(p, Pf, sx, y, sfl >> 2, f);
+    }
+    if (TH) {
+        const T* __restrict__ Pg = static_cast<const T*>(p.gin);
+        if (fl & FLAG_SOLID) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) g[j] = R(0);
+        } else {
+            pull<T>(p, Pg, p.shg, x, y, g);
+            if (fl & FLAG_BOUNDARY) fix_g<T>(p, Pg, x, y, fl >> 2, g);
+        }
+    }
+    // boundary conditions, src/lbm.hpp:531-540
+    if (p.bc_kind == BC_LID) {
+        if (y == p.ny - 1) {  // enforce_lid :110-120 (corner nodes included)
+            R rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
+            const R ul = R(p.u_bc);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) f[i] = feq<R>(i, rho, ul, R(0));
+        }
+    } else if (p.bc_kind == BC_INFLOW) {
+        if (x == 0) zou_he<R>(f, R(p.u_bc));
+    } else if (p.bc_kind == BC_STEP) {
+        const int hs = p.ny / 3;
+        if (x == 0 && y >= hs && !(fl & FLAG_SOLID)) {
+            const R yy = R(y - hs), h = R(p.ny - 1 - hs);
+            zou_he<R>(f, R(p.u_bc) * R(4) * yy * (h - yy) / (h * h));
+        }
+    }
+    if (TH && p.hook_kind == 1) {
+        // src/thermal_cavity.cpp:168-204: Dirichlet columns, then adiabatic rows
+        if ((x == 1 || x == p.nx - 2) && y >= 1 && y <= p.ny - 2) {
+            const R Tw = R(x == p.nx - 2 ? p.hook_b : p.hook_a);
+            R rho, u, v;
+            macros(f, rho, u, v);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = feq<R>(i, Tw, u, v);
+        }
+        if ((y == 1 || y == p.ny - 2) && x >= 1 && x <= p.nx - 2) {
+            g[1] = g[3];
+            g[2] = g[4];
+            g[5] = g[7];
+            g[6] = g[8];
+        }
+    } else if (TH && p.hook_kind == 2) {
+        if (fl & FLAG_SOLID) {  // src/heated_cylinder.cpp:156-164
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = R(wgt(i)) * R(p.hook_a);
+        }
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R wall_distance(const KParams& p, uint32_t fl) {
+    if (fl & FLAG_BOUNDARY) return R(p.rec_wd[fl >> 2]);
+    const uint32_t d = fl >> 2;
+    return d == WD_UNREACHED ? R(1e9) : R(d);
+}
+
+// Collision of one fluid node: src/lbm.hpp:300-354 (mrt_collide :128-218,
+// LES :158-182 with y+ :317-325, body force :327-331) and the thermal
+// collision with Boussinesq/Guo forcing :357-397 (src/thermal.hpp:25-52).
+template <class R, bool TH>
+__device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R g[9]) {
+    R rho, u, v;
+    macros(f, rho, u, v);
+    if (!(rho == rho) || rho == R(0)) atomicOr(p.nan_flag, 1u);
+    if (p.collision == 0) {
+        const R f0 = f[0], f1 = f[1], f2 = f[2], f3 = f[3], f4 = f[4];
+        const R f5 = f[5], f6 = f[6], f7 = f[7], f8 = f[8];
+        R me = R(-4) * f0 - f1 - f2 - f3 - f4 + R(2) * (f5 + f6 + f7 + f8);
+        R meps = R(4) * f0 - R(2) * (f1 + f2 + f3 + f4) + (f5 + f6 + f7 + f8);
+        R mqx = R(-2) * f1 + R(2) * f3 + f5 - f6 - f7 + f8;
+        R mqy = R(-2) * f2 + R(2) * f4 + f5 + f6 - f7 - f8;
+        R mpxx = f1 - f2 + f3 - f4;
+        R mpxy = f5 - f6 + f7 - f8;
+        const R jx = rho * u, jy = rho * v;
+        const R usq = u * u + v * v;
+        const R e_eq = R(-2) * rho + R(3) * rho * usq;
+        const R eps_eq = rho - R(3) * rho * usq;
+        const R pxx_eq = rho * (u * u - v * v);
+        const R pxy_eq = rho * u * v;
+        R s_eff = R(p.s_shear);
+        if (p.les) {
+            const R tau = R(p.tau), cs_sq = R(p.cs_sq), nu = R(p.nu);
+            R csq = cs_sq;
+            if (nu > R(0)) {
+                const R wd = wall_distance<R>(p, fl);
+                const R speed = sqrt(u * u + v * v);
+                const R yp = wd * sqrt(speed * speed + R(1e-12)) / nu;
+                if (yp > R(0)) {  // Van Driest damping always wins when y+ > 0 (:171-182)
+                    const R damp = R(1) - exp(-yp / R(26));
+                    const R cd = sqrt(cs_sq) * damp;
+                    csq = cd * cd;
+                }
+            }
+            const R a = mpxx - pxx_eq, b = mpxy - pxy_eq;
+            const R Q = sqrt(R(2) * (a * a + b * b));
+            const R A = R(9) * csq * Q / (R(2) * rho);
+            const R te = (tau + sqrt(tau * tau + R(4) * A)) / R(2);
+            s_eff = clamp_rate<R>(R(1) / te);
+        }
+        const R sb = R(p.s_bulk), sn = R(p.s_normal);
+        me -= sb * (me - e_eq);
+        meps -= sb * (meps - eps_eq);
+        mqx -= sn * (mqx + jx);
+        mqy -= sn * (mqy + jy);
+        mpxx -= s_eff * (mpxx - pxx_eq);
+        mpxy -= s_eff * (mpxy - pxy_eq);
+        // closed-form inverse transform (src/lbm.hpp:193-217), common terms shared
+        const R a0 = R(1.0 / 9.0) * rho;
+        const R ax = a0 - R(1.0 / 36.0) * me - R(1.0 / 18.0) * meps;  // axial base
+        const R ad = a0 + R(1.0 / 18.0) * me + R(1.0 / 36.0) * meps;  // diagonal base
+        const R hx = R(1.0 / 6.0) * jx - R(1.0 / 6.0) * mqx;
+        const R hy = R(1.0 / 6.0) * jy - R(1.0 / 6.0) * mqy;
+        const R dx = R(1.0 / 6.0) * jx + R(1.0 / 12.0) * mqx;
+        const R dy = R(1.0 / 6.0) * jy + R(1.0 / 12.0) * mqy;
+        const R px = R(0.25) * mpxx, py = R(0.25) * mpxy;
+        f[0] = a0 - R(1.0 / 9.0) * me + R(1.0 / 9.0) * meps;
+        f[1] = ax + hx + px;
+        f[2] = ax + hy - px;
+        f[3] = ax - hx + px;
+        f[4] = ax - hy - px;
+        f[5] = ad + dx + dy + py;
+        f[6] = ad - dx + dy - py;
+        f[7] = ad - dx - dy + py;
+        f[8] = ad + dx - dy - py;
+    } else {
+        const R it = R(1) / R(p.tau);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f[i] -= it * (f[i] - feq<R>(i, rho, u, v));
+    }
+    if (p.Fscale != 0.0) {
+        const R F = R(p.Fscale);
+        const R fa = R(1.0 / 9.0) * F, fd = R(1.0 / 36.0) * F;
+        f[1] += fa;
+        f[3] -= fa;
+        f[5] += fd;
+        f[6] -= fd;
+        f[7] -= fd;
+        f[8] += fd;
+    }
+    if (TH) {
+        R rho2, u2, v2;
+        macros(f, rho2, u2, v2);
+        const R T = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8];
+        const R om = R(p.omega_k);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) g[i] -= om * (g[i] - feq<R>(i, T, u2, v2));
+        if (p.beta > 0.0 && p.g_buoy != 0.0) {
+            const R fyb = -R(p.beta) * (T - R(p.T_ref)) * R(p.g_buoy);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const R eu = R(CXf(i)) * u2 + R(CYf(i)) * v2;
+                const R Fd = R(CYf(i)) * fyb;
+                f[i] += R(wgt(i)) * (R(3) * Fd + R(9) * eu * Fd);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void block_reduce2(double& a, double& b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    __shared__ double sa[32], sb[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    if ((tid & 31) == 0) {
+        sa[tid >> 5] = a;
+        sb[tid >> 5] = b;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        a = tid < nw ? sa[tid] : 0.0;
+        b = tid < nw ? sb[tid] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+    }
+}
+
+// ----------------------------------------------------------------- kernels
+template <class T, bool TH>
+__global__ void __launch_bounds__(512) step_kernel(const KParams p) {
+    using R = typename Pop<T>::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    double fxs = 0.0, fys = 0.0;
+    if (x < p.nx && y < p.ny) {
+        const size_t n = (size_t)y * p.nx + x;
+        const uint32_t fl = __ldg(p.flags + n);
+        R f[9], g[9];
+        build_state<T, TH>(p, x, y, fl, f, g);
+        if (!(fl & FLAG_SOLID)) {
+            if (fl & FLAG_BOUNDARY) {
+                const uint32_t fm = p.rec_force[fl >> 2];
+                if (fm) {
+#pragma unroll
+                    for (int j = 0; j < 9; ++j)
+                        if (fm & (1u << j)) {
+                            fxs += double(-CXf(j)) * 2.0 * double(f[j]);
+                            fys += double(-CYf(j)) * 2.0 * double(f[j]);
+                        }
+                }
+            }
+            collide<R, TH>(p, fl, f, g);
+        }
+        T* __restrict__ Fo = static_cast<T*>(p.fout);
+        const size_t N = (size_t)p.N;
+        if (!((fl & FLAG_SOLID) && p.skip_settled_solids && x > 0 && x < p.nx - 1 && y < p.ny - 1)) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) Pop<T>::st(Fo + j * N, n, f[j], p.shf[j]);
+            if (TH) {
+                T* __restrict__ Go = static_cast<T*>(p.gout);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) Pop<T>::st(Go + j * N, n, g[j], p.shg[j]);
+            }
+        }
+    }
+    if (p.block_slot) {
+        const int slot = p.block_slot[blockIdx.y * gridDim.x + blockIdx.x];
+        if (slot >= 0) {  // uniform per block
+            block_reduce2(fxs, fys);
+            if (threadIdx.x == 0 && threadIdx.y == 0) {
+                p.partials[2 * slot] = fxs;
+                p.partials[2 * slot + 1] = fys;
+            }
+        }
+    }
+}
+
+template <class T, bool TH>
+__global__ void readback_kernel(const KParams p, const ROut o) {
+    using R = typename Pop<T>::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.nx || y >= p.ny) return;
+    const size_t n = (size_t)y * p.nx + x;
+    const uint32_t fl = p.flags[n];
+    R f[9], g[9];
+    build_state<T, TH>(p, x, y, fl, f, g);
+    if (o.f_aos)
+        for (int j = 0; j < 9; ++j) o.f_aos[n * 9 + j] = double(f[j]);
+    if (TH && o.g_aos)
+        for (int j = 0; j < 9; ++j) o.g_aos[n * 9 + j] = double(g[j]);
+    if (o.rho || o.u || o.v) {
+        double fd[9];
+        for (int j = 0; j < 9; ++j) fd[j] = double(f[j]);
+        double rho, u, v;
+        macros(fd, rho, u, v);
+        if (o.rho) o.rho[n] = rho;
+        if (o.u) o.u[n] = u;
+        if (o.v) o.v[n] = v;
+    }
+    if (TH && o.T) {
+        double T = 0.0;
+        for (int j = 0; j < 9; ++j) T += double(g[j]);
+        o.T[n] = T;
+    }
+    if (o.fx) {
+        double fx = 0.0, fy = 0.0;
+        if (!(fl & FLAG_SOLID) && (fl & FLAG_BOUNDARY)) {
+            const uint32_t fm = p.rec_force[fl >> 2];
+            for (int i = 0; i < 9; ++i) {  // reference accumulation order (src/lbm.hpp:550-577)
+                const int j = BBf(i);
+                if (fm & (1u << j)) {
+                    fx += double(CXf(i)) * 2.0 * double(f[j]);
+                    fy += double(CYf(i)) * 2.0 * double(f[j]);
+                }
+            }
+        }
+        o.fx[n] = fx;
+        o.fy[n] = fy;
+    }
+}
+
+template <class T, bool TH>
+__global__ void prologue_kernel(const KParams p, const double* __restrict__ fa, const double* __restrict__ ga) {
+    using R = typename Pop<T>::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.nx || y >= p.ny) return;
+    const size_t n = (size_t)y * p.nx + x;
+    const uint32_t fl = p.flags[n];
+    R f[9], g[9];
+    for (int j = 0; j < 9; ++j) f[j] = R(fa[n * 9 + j]);
+    if (TH)
+        for (int j = 0; j < 9; ++j) g[j] = R(ga[n * 9 + j]);
+    if (!(fl & FLAG_SOLID)) collide<R, TH>(p, fl, f, g);
+    T* Fo = static_cast<T*>(p.fout);
+    const size_t N = (size_t)p.N;
+    for (int j = 0; j < 9; ++j) Pop<T>::st(Fo + j * N, n, f[j], p.shf[j]);
+    if (TH) {
+        T* Go = static_cast<T*>(p.gout);
+        for (int j = 0; j < 9; ++j) Pop<T>::st(Go + j * N, n, g[j], p.shg[j]);
+    }
+}
+
+// Deterministic second stage of the force reduction: one block sums the
+// per-block partials in a fixed order and appends (fx, fy) to the history.
+__global__ void force_reduce_kernel(const double* __restrict__ part, int nslots, double* hist, int cap,
+                                    unsigned long long* counter, double* last) {
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < nslots; k += blockDim.x) {
+        a += part[2 * k];
+        b += part[2 * k + 1];
+    }
+    block_reduce2(a, b);
+    if (threadIdx.x == 0) {
+        const unsigned long long k = *counter;
+        if (k < (unsigned long long)cap) {
+            hist[2 * k] = a;
+            hist[2 * k + 1] = b;
+        }
+        last[0] = a;
+        last[1] = b;
+        *counter = k + 1;
+    }
+}
+
+template <class T>
+int launch_step_t(const KParams& p, int bx, int by, cudaStream_t s) {
+    dim3 blk(bx, by), grd((p.nx + bx - 1) / bx, (p.ny + by - 1) / by);
+    if (p.thermal)
+        step_kernel<T, true><<<grd, blk, 0, s>>>(p);
+    else
+        step_kernel<T, false><<<grd, blk, 0, s>>>(p);
+    return (int)cudaGetLastError();
+}
+
+template <class T>
+int launch_readback_t(const KParams& p, const ROut& o, cudaStream_t s) {
+    dim3 blk(128, 2), grd((p.nx + 127) / 128, (p.ny + 1) / 2);
+    if (p.thermal)
+        readback_kernel<T, true><<<grd, blk, 0, s>>>(p, o);
+    else
+        readback_kernel<T, false><<<grd, blk, 0, s>>>(p, o);
+    return (int)cudaGetLastError();
+}
+
+template <class T>
+int launch_prologue_t(const KParams& p, const double* fa, const double* ga, cudaStream_t s) {
+    dim3 blk(128, 2), grd((p.nx + 127) / 128, (p.ny + 1) / 2);
+    if (p.thermal)
+        prologue_kernel<T, true><<<grd, blk, 0, s>>>(p, fa, ga);
+    else
+        prologue_kernel<T, false><<<grd, blk, 0, s>>>(p, fa, ga);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+int launch_step(int storage, const KParams& p, int bx, int by, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_step_t<float>(p, bx, by, s);
+        case ST_FP16: return launch_step_t<__half>(p, bx, by, s);
+        case ST_BF16: return launch_step_t<__nv_bfloat16>(p, bx, by, s);
+        case ST_FP64: return launch_step_t<double>(p, bx, by, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_readback(int storage, const KParams& p, const ROut& o, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_readback_t<float>(p, o, s);
+        case ST_FP16: return launch_readback_t<__half>(p, o, s);
+        case ST_BF16: return launch_readback_t<__nv_bfloat16>(p, o, s);
+        case ST_FP64: return launch_readback_t<double>(p, o, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_prologue(int storage, const KParams& p, const double* fa, const double* ga, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_prologue_t<float>(p, fa, ga, s);
+        case ST_FP16: return launch_prologue_t<__half>(p, fa, ga, s);
+        case ST_BF16: return launch_prologue_t<__nv_bfloat16>(p, fa, ga, s);
+        case ST_FP64: return launch_prologue_t<double>(p, fa, ga, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_force_reduce(const double* partials, int nslots, double* hist, int cap, unsigned long long* counter,
+                        double* last, void* stream) {
+    force_reduce_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(partials, nslots, hist, cap, counter,
+                                                                           last);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace lbm2d

@@ -1,0 +1,360 @@
+// lbm.hpp -- drop-in replacement of the reference's src/lbm.hpp.
+//
+// execute_time_step runs on the GPU (one fused sm_103a kernel per step, see
+// lbm-2d_gb300/csrc/lbm2d_kernels.cu).  Everything else keeps the reference's
+// names and host semantics: the boundary-condition helpers, the node-level
+// MRT collision and interpolated bounce-back, the obstacle placement and the
+// frame/force/metadata writers, which read the LBMCapabilities mirrors (so
+// they download the device state on first use after a step).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <filesystem>
+#include <fstream>
+#include <iostream>
+#include <string>
+
+#include "geometry.hpp"
+#include "lbm_types.hpp"
+#include "thermal.hpp"
+#if __has_include("ibm.hpp")
+#include "ibm.hpp"  // immersed-boundary helpers of the reference (host side, optional)
+#endif
+#if __has_include("wall_functions.hpp")
+#include "wall_functions.hpp"
+#endif
+
+// ---------------------------------------------------------------- boundary conditions (host)
+// Zou/He velocity inlet at x = 0, src/lbm.hpp:21-34
+inline void enforce_inflow(LBMCapabilities& sys, double u_inflow) {
+    for (int y = 0; y < NY; ++y) {
+        double* fn = &sys.f[static_cast<size_t>(node_index(0, y)) * 9];
+        const double rho = (fn[0] + fn[2] + fn[4] + 2.0 * (fn[3] + fn[6] + fn[7])) / (1.0 - u_inflow);
+        fn[1] = fn[3] + (2.0 / 3.0) * rho * u_inflow;
+        fn[5] = fn[7] + (1.0 / 6.0) * rho * u_inflow;
+        fn[8] = fn[6] + (1.0 / 6.0) * rho * u_inflow;
+    }
+}
+
+// parabolic inlet, src/lbm.hpp:40-58
+inline void enforce_step_inflow(LBMCapabilities& sys, int h_step, int h_inlet, double u_max) {
+    for (int y = h_step; y < NY; ++y) {
+        if (sys.obstacle[node_index(0, y)]) continue;
+        double* fn = &sys.f[static_cast<size_t>(node_index(0, y)) * 9];
+        const double yy = static_cast<double>(y - h_step), h = static_cast<double>(h_inlet);
+        const double ul = u_max * 4.0 * yy * (h - yy) / (h * h);
+        const double rho = (fn[0] + fn[2] + fn[4] + 2.0 * (fn[3] + fn[6] + fn[7])) / (1.0 - ul);
+        fn[1] = fn[3] + (2.0 / 3.0) * rho * ul;
+        fn[5] = fn[7] + (1.0 / 6.0) * rho * ul;
+        fn[8] = fn[6] + (1.0 / 6.0) * rho * ul;
+    }
+}
+
+// zero-gradient outlet, src/lbm.hpp:63-73
+inline void enforce_outflow(LBMCapabilities& sys) {
+    for (int y = 0; y < NY; ++y) {
+        double* dst = &sys.f[static_cast<size_t>(node_index(NX - 1, y)) * 9];
+        const double* src = &sys.f[static_cast<size_t>(node_index(NX - 2, y)) * 9];
+        for (int i = 0; i < 9; ++i) dst[i] = src[i];
+    }
+}
+
+// src/lbm.hpp:79-87
+inline void place_walls(LBMCapabilities& sys) { lbm2d_mask_walls(NX, NY, sys.obstacle.data()); }
+
+// src/lbm.hpp:93-104
+inline bool check_convergence(const std::vector<double>& values, int window = 1000, double threshold = 1e-4) {
+    const int n = static_cast<int>(values.size());
+    if (n < 2 * window) return false;
+    double recent = 0.0, earlier = 0.0;
+    for (int i = n - window; i < n; ++i) recent += values[i];
+    recent /= static_cast<double>(window);
+    for (int i = n - 2 * window; i < n - window; ++i) earlier += values[i];
+    earlier /= static_cast<double>(window);
+    return std::abs(recent - earlier) < threshold;
+}
+
+// equilibrium lid at y = NY-1, src/lbm.hpp:110-120
+inline void enforce_lid(LBMCapabilities& sys, double u_lid) {
+    for (int x = 0; x < NX; ++x) {
+        double* fn = &sys.f[static_cast<size_t>(node_index(x, NY - 1)) * 9];
+        double rho, u, v;
+        compute_macros(fn, rho, u, v);
+        for (int i = 0; i < 9; ++i) fn[i] = compute_equilibrium(i, rho, u_lid, 0.0);
+    }
+}
+
+// ---------------------------------------------------------------- node-level operators (host)
+// d'Humieres MRT of one node with optional Smagorinsky / Van Driest,
+// src/lbm.hpp:128-218.  The GPU kernel applies the same operator to every node.
+inline void mrt_collide(double* f_node, double rho, double u, double v, const MRTParams& mrt, double cs_sq = 0.0,
+                        double tau_base = 0.0, double y_plus = 0.0) {
+    const double f0 = f_node[0], f1 = f_node[1], f2 = f_node[2], f3 = f_node[3], f4 = f_node[4];
+    const double f5 = f_node[5], f6 = f_node[6], f7 = f_node[7], f8 = f_node[8];
+    double e = -4 * f0 - f1 - f2 - f3 - f4 + 2 * (f5 + f6 + f7 + f8);
+    double eps = 4 * f0 - 2 * (f1 + f2 + f3 + f4) + (f5 + f6 + f7 + f8);
+    double qx = -2 * f1 + 2 * f3 + f5 - f6 - f7 + f8;
+    double qy = -2 * f2 + 2 * f4 + f5 + f6 - f7 - f8;
+    double pxx = f1 - f2 + f3 - f4;
+    double pxy = f5 - f6 + f7 - f8;
+    const double jx = rho * u, jy = rho * v, usq = u * u + v * v;
+    const double e_eq = -2 * rho + 3 * rho * usq, eps_eq = rho - 3 * rho * usq;
+    const double pxx_eq = rho * (u * u - v * v), pxy_eq = rho * u * v;
+    auto clamp = [](double s) { return (s < 0.5) ? 0.5 : ((s > 1.99) ? 1.99 : s); };
+    double s_eff = mrt.s_shear;
+    if (cs_sq > 0.0 && tau_base > 0.0) {
+        double csq = cs_sq;
+        if (y_plus > 0.0) {
+            const double cd = std::sqrt(cs_sq) * (1.0 - std::exp(-y_plus / 26.0));
+            csq = cd * cd;
+        }
+        const double a = pxx - pxx_eq, b = pxy - pxy_eq;
+        const double Q = std::sqrt(2.0 * (a * a + b * b));
+        const double A = 9.0 * csq * Q / (2.0 * rho);
+        s_eff = clamp(1.0 / ((tau_base + std::sqrt(tau_base * tau_base + 4.0 * A)) / 2.0));
+    }
+    e -= mrt.s_bulk * (e - e_eq);
+    eps -= mrt.s_bulk * (eps - eps_eq);
+    qx -= mrt.s_normal * (qx + jx);
+    qy -= mrt.s_normal * (qy + jy);
+    pxx -= s_eff * (pxx - pxx_eq);
+    pxy -= s_eff * (pxy - pxy_eq);
+    const double a0 = rho / 9.0;
+    const double ax = a0 - e / 36.0 - eps / 18.0, ad = a0 + e / 18.0 + eps / 36.0;
+    const double hx = (jx - qx) / 6.0, hy = (jy - qy) / 6.0;
+    const double dx = jx / 6.0 + qx / 12.0, dy = jy / 6.0 + qy / 12.0;
+    f_node[0] = a0 - e / 9.0 + eps / 9.0;
+    f_node[1] = ax + hx + pxx / 4.0;
+    f_node[2] = ax + hy - pxx / 4.0;
+    f_node[3] = ax - hx + pxx / 4.0;
+    f_node[4] = ax - hy - pxx / 4.0;
+    f_node[5] = ad + dx + dy + pxy / 4.0;
+    f_node[6] = ad - dx + dy - pxy / 4.0;
+    f_node[7] = ad - dx - dy + pxy / 4.0;
+    f_node[8] = ad + dx - dy - pxy / 4.0;
+}
+
+// Interpolated bounce-back of one link into sys.f_next (host), src/lbm.hpp:226-288.
+inline void apply_bouzidi_bb(LBMCapabilities& sys, int x, int y, int i, const double* f_node, int node_idx) {
+    if (sys.f_next.size() != sys.f.size()) sys.f_next.assign(sys.f.size(), 0.0);
+    const BounceBackGeometry& g = sys.bb_geom;
+    const double q = g.compute_q(static_cast<double>(x), static_cast<double>(y), i);
+    const int bb = bounce_back[i];
+    double rho, u, v;
+    compute_macros(f_node, rho, u, v);
+    double uwx = 0.0, uwy = 0.0;
+    if (g.has_moving_wall) g.compute_wall_velocity(x + cx[i], y + cy[i], uwx, uwy);
+    const double ed = cx[i] * uwx + cy[i] * uwy;
+    double fbb;
+    if (g.use_mei_bb) {
+        fbb = q * compute_equilibrium(i, rho, uwx, uwy) + (1.0 - q) * f_node[i] +
+              (2.0 * q - 1.0) * weights[i] * rho * ed * 3.0;
+    } else {
+        if (q < 0.5) {
+            const int sx = x - cx[i], sy = y - cy[i];
+            const double fs = (sx >= 0 && sx < NX && sy >= 0 && sy < NY)
+                                  ? sys.f[static_cast<size_t>(node_index(sx, sy)) * 9 + i]
+                                  : f_node[i];
+            fbb = 2.0 * q * f_node[i] + (1.0 - 2.0 * q) * fs;
+        } else {
+            const double inv2q = 1.0 / (2.0 * q);
+            fbb = inv2q * f_node[i] + (1.0 - inv2q) * sys.f[static_cast<size_t>(node_idx) * 9 + bb];
+        }
+        if (g.has_moving_wall) fbb -= 2.0 * weights[i] * rho * ed * 3.0;
+    }
+    sys.f_next[static_cast<size_t>(node_idx) * 9 + bb] = fbb;
+}
+
+// ---------------------------------------------------------------- the time step (GPU)
+// src/lbm.hpp:293-582: collision, streaming with (interpolated) bounce-back,
+// boundary conditions and the momentum-exchange force, fused on the device.
+inline void execute_time_step(LBMCapabilities& sys, double tau, double u_inflow) { sys.device_step(tau, u_inflow); }
+
+// ---------------------------------------------------------------- obstacle placement
+// src/lbm.hpp:931-944
+inline void place_cylinder(LBMCapabilities& sys, int cx_cyl, int cy_cyl, int radius) {
+    sys.bb_geom.cx = static_cast<double>(cx_cyl);
+    sys.bb_geom.cy = static_cast<double>(cy_cyl);
+    sys.bb_geom.radius = static_cast<double>(radius);
+    lbm2d_mask_cylinder(NX, NY, sys.obstacle.data(), cx_cyl, cy_cyl, radius);
+}
+
+// src/lbm.hpp:951-964
+inline void place_polygon(LBMCapabilities& sys, const std::vector<std::pair<double, double>>& poly) {
+    sys.bb_geom.poly_vertices = poly;
+    sys.bb_geom.is_polygon = true;
+    std::vector<double> xy;
+    xy.reserve(poly.size() * 2);
+    for (auto& p : poly) {
+        xy.push_back(p.first);
+        xy.push_back(p.second);
+    }
+    lbm2d_mask_polygon(NX, NY, sys.obstacle.data(), xy.data(), static_cast<int>(poly.size()));
+}
+
+// ---------------------------------------------------------------- output writers (host)
+namespace lbm2d_dropin {
+// Downsampled macroscopic fields + vorticity, the frame format of
+// src/lbm.hpp:588-701 (and :707-817 with a temperature channel).
+inline void write_frame(const LBMCapabilities& sys, int step, const std::string& output_dir, bool thermal,
+                        double T_wall) {
+    const int ds = std::max(1, NX / 100);
+    const int nxd = (NX + ds - 1) / ds, nyd = (NY + ds - 1) / ds, nd = nxd * nyd;
+    const std::string dir = output_dir + "/frames";
+    std::filesystem::create_directories(dir);
+    std::ofstream out(dir + "/frame_" + std::to_string(step) + ".json");
+    out.precision(6);
+    out << std::fixed;
+    std::vector<double> vel(nd, 0.0), ua(nd, 0.0), va(nd, 0.0), ra(nd, 0.0), om(nd, 0.0), ta(nd, 0.0);
+    std::vector<int> ob(nd, 0);
+    const double* f = sys.f.data();
+    const double* g = thermal ? sys.g_thermal.data() : nullptr;
+    int k = 0;
+    for (int y = 0; y < NY; y += ds) {
+        for (int x = 0; x < NX; x += ds, ++k) {
+            const int idx = node_index(x, y);
+            if (sys.obstacle[idx]) {
+                ob[k] = 1;
+                if (thermal) ta[k] = T_wall;
+                continue;
+            }
+            double rho, u, v;
+            compute_macros(f + static_cast<size_t>(idx) * 9, rho, u, v);
+            double T = 0.0;
+            if (thermal) compute_temperature(g + static_cast<size_t>(idx) * 9, T);
+            if (rho < 1e-12 || std::isnan(rho)) {
+                rho = 1.0;
+                u = 0.0;
+                v = 0.0;
+            }
+            if (std::isnan(u)) u = 0.0;
+            if (std::isnan(v)) v = 0.0;
+            if (thermal && std::isnan(T)) T = 1.0;
+            double s = std::sqrt(u * u + v * v);
+            if (std::isnan(s)) s = 0.0;
+            vel[k] = s;
+            ua[k] = u;
+            va[k] = v;
+            ra[k] = rho;
+            ta[k] = T;
+        }
+    }
+    for (int j = 0; j < nyd; ++j)
+        for (int i = 0; i < nxd; ++i) {
+            const int idx = j * nxd + i;
+            if (ob[idx]) continue;
+            const int il = std::max(0, i - 1), ir = std::min(nxd - 1, i + 1);
+            const int jd = std::max(0, j - 1), ju = std::min(nyd - 1, j + 1);
+            const double dvdx = (va[j * nxd + ir] - va[j * nxd + il]) / (2.0 * static_cast<double>((ir - il) * ds));
+            const double dudy = (ua[ju * nxd + i] - ua[jd * nxd + i]) / (2.0 * static_cast<double>((ju - jd) * ds));
+            om[idx] = dvdx - dudy;
+        }
+    auto arr = [&](const char* name, auto&& get, bool first) {
+        out << (first ? "" : "],") << "\"" << name << "\":[";
+        for (int i = 0; i < nd; ++i) {
+            if (i > 0) out << ",";
+            out << get(i);
+        }
+    };
+    out << "{\"nx\":" << nxd << ",\"ny\":" << nyd << ",";
+    arr("velocity", [&](int i) { return vel[i]; }, true);
+    arr("u", [&](int i) { return ua[i]; }, false);
+    arr("v", [&](int i) { return va[i]; }, false);
+    arr("rho", [&](int i) { return ra[i]; }, false);
+    arr("p", [&](int i) { return ra[i] / 3.0; }, false);
+    arr("omega", [&](int i) { return om[i]; }, false);
+    if (thermal) arr("temperature", [&](int i) { return ta[i]; }, false);
+    arr("obstacle", [&](int i) { return ob[i]; }, false);
+    out << "]}";
+}
+}  // namespace lbm2d_dropin
+
+inline void save_json_frame(const LBMCapabilities& sys, int step, const std::string& output_dir) {
+    lbm2d_dropin::write_frame(sys, step, output_dir, false, 0.0);
+}
+
+inline void save_json_frame_thermal(LBMCapabilities& sys, int step, const std::string& output_dir, double T_wall) {
+    lbm2d_dropin::write_frame(sys, step, output_dir, true, T_wall);
+}
+
+// src/lbm.hpp:822-834 (one cached file handle per output directory)
+inline void save_forces_jsonl(const std::string& output_dir, int step, double cd, double cl) {
+    static std::string cached_dir;
+    static std::ofstream out;
+    if (cached_dir != output_dir) {
+        if (out.is_open()) out.close();
+        out.open(output_dir + "/forces.jsonl", std::ios::trunc);
+        out.precision(6);
+        out << std::fixed;
+        cached_dir = output_dir;
+    }
+    out << "{\"step\":" << step << ",\"cd\":" << cd << ",\"cl\":" << cl << "}\n";
+}
+
+// src/lbm.hpp:839-855
+inline void save_meta_json(const std::string& output_dir, double re, double tau, double u_inflow,
+                           double length_scale, const std::string& shape_type, int nx, int ny) {
+    std::ofstream out(output_dir + "/meta.json");
+    out.precision(6);
+    out << std::fixed << "{\n"
+        << "  \"nx\": " << nx << ",\n"
+        << "  \"ny\": " << ny << ",\n"
+        << "  \"re\": " << re << ",\n"
+        << "  \"tau\": " << tau << ",\n"
+        << "  \"u_inflow\": " << u_inflow << ",\n"
+        << "  \"length_scale\": " << length_scale << ",\n"
+        << "  \"shape_type\": \"" << shape_type << "\"\n"
+        << "}\n";
+}
+
+// legacy VTK structured points, src/lbm.hpp:860-926
+inline void save_vtk_frame(const LBMCapabilities& sys, int frame, const std::string& output_dir = "output") {
+    std::ofstream out(output_dir + "/frame_" + std::to_string(frame) + ".vtk");
+    out << "# vtk DataFile Version 3.0\nLBM Fluid Grid\nASCII\nDATASET STRUCTURED_POINTS\n";
+    out << "DIMENSIONS " << NX << " " << NY << " 1\n";
+    out << "ORIGIN 0 0 0\nSPACING 1 1 1\n";
+    out << "POINT_DATA " << NX * NY << "\n";
+    const double* f = sys.f.data();
+    auto macros_at = [&](int idx, double& rho, double& u, double& v) {
+        compute_macros(f + static_cast<size_t>(idx) * 9, rho, u, v);
+    };
+    out << "SCALARS VelocityMagnitude double 1\nLOOKUP_TABLE default\n";
+    for (int idx = 0; idx < NX * NY; ++idx) {
+        if (sys.obstacle[idx]) {
+            out << "0.0\n";
+            continue;
+        }
+        double rho, u, v;
+        macros_at(idx, rho, u, v);
+        out << std::sqrt(u * u + v * v) << "\n";
+    }
+    out << "VECTORS Velocity double\n";
+    for (int idx = 0; idx < NX * NY; ++idx) {
+        if (sys.obstacle[idx]) {
+            out << "0 0 0\n";
+            continue;
+        }
+        double rho, u, v;
+        macros_at(idx, rho, u, v);
+        out << u << " " << v << " 0\n";
+    }
+    out << "SCALARS Density double 1\nLOOKUP_TABLE default\n";
+    for (int idx = 0; idx < NX * NY; ++idx) {
+        if (sys.obstacle[idx]) {
+            out << "0.0\n";
+            continue;
+        }
+        double rho, u, v;
+        macros_at(idx, rho, u, v);
+        out << rho << "\n";
+    }
+    out << "SCALARS DragForce double 1\nLOOKUP_TABLE default\n";
+    for (int idx = 0; idx < NX * NY; ++idx) {
+        const double fx = sys.fx_body[idx], fy = sys.fy_body[idx];
+        if (fx != 0.0 || fy != 0.0)
+            out << fx << "\n";
+        else
+            out << "0.0\n";
+    }
+}

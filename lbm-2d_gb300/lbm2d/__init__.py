@@ -1,0 +1,411 @@
+"""Python binding of liblbm2d (the GB300 D2Q9 lattice-Boltzmann step).
+
+A thin ctypes layer over the C-ABI in include/lbm2d.h.  :class:`Solver`
+mirrors the reference's solver surface (LBMCapabilities + execute_time_step +
+place_* helpers of src/lbm.hpp / src/lbm_types.hpp) with host arrays in the
+reference's layouts, so tests and benchmarks read like the reference's own.
+
+There is no CPU fallback: every compute call goes to the CUDA library, and
+constructing a Solver without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._build import LIB, build as _build_lib, needs_build  # noqa: F401
+
+CYLINDER, CAVITY, STEP, RIBS, URBAN_CANYON, DOWNWASH, SQUARE_CYLINDER, FLAT_PLATE, \
+    SPORTS_BALL, PERIODIC_HILLS, CYLINDER_NEAR_WALL, SIDE_BY_SIDE, ROTATING_CYLINDER, \
+    ORIFICE_PLATE = range(14)
+MRT, BGK = 0, 1
+STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2, "fp64": 3}
+BYTES_PER_POP = {"fp32": 4, "fp16": 2, "bf16": 2, "fp64": 8}
+HOOK_NONE, HOOK_HEATED_CAVITY, HOOK_HEATED_SOLIDS = 0, 1, 2
+
+ERRORS = {1: "invalid argument", 2: "out of device memory", 3: "CUDA error", 4: "non-finite density",
+          5: "call out of order", 6: "no CUDA device", 7: "device wait timed out"}
+
+
+class LBMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lbm2d error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("case_type", C.c_int), ("collision", C.c_int),
+                ("use_les", C.c_int), ("cs", C.c_double), ("storage", C.c_int), ("device", C.c_int)]
+
+
+class Info(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("storage", C.c_int), ("bytes_per_update", C.c_double),
+                ("device_bytes", C.c_size_t), ("n_boundary_nodes", C.c_int), ("n_force_nodes", C.c_int),
+                ("steps_done", C.c_longlong), ("block_x", C.c_int), ("block_y", C.c_int)]
+
+
+class BBGeometry(C.Structure):
+    _fields_ = [("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double),
+                ("poly", C.POINTER(C.c_double)), ("n_poly", C.c_int), ("has_moving_wall", C.c_int),
+                ("omega", C.c_double), ("rot_cx", C.c_double), ("rot_cy", C.c_double)]
+
+
+_D, _I, _P = C.c_double, C.c_int, C.c_void_p
+_DP = C.POINTER(C.c_double)
+_U8P = C.POINTER(C.c_uint8)
+
+_SIGS = {
+    "lbm2d_create": ([C.POINTER(Config), C.POINTER(_P)], _I),
+    "lbm2d_destroy": ([_P], _I),
+    "lbm2d_last_error": ([_P], C.c_char_p),
+    "lbm2d_global_error": ([], C.c_char_p),
+    "lbm2d_set_case": ([_P, _I, _I, _I, _D], _I),
+    "lbm2d_set_mask": ([_P, _U8P], _I),
+    "lbm2d_set_bb_cylinder": ([_P, _D, _D, _D], _I),
+    "lbm2d_set_bb_polygon": ([_P, _DP, _I], _I),
+    "lbm2d_set_moving_wall": ([_P, _I, _D, _D, _D], _I),
+    "lbm2d_set_mei": ([_P, _I], _I),
+    "lbm2d_set_body_force": ([_P, _D], _I),
+    "lbm2d_set_thermal": ([_P, _I, _D, _D, _D, _D, _D], _I),
+    "lbm2d_set_thermal_hook": ([_P, _I, _D, _D], _I),
+    "lbm2d_upload_f": ([_P, _DP], _I),
+    "lbm2d_upload_g": ([_P, _DP], _I),
+    "lbm2d_upload_f_device": ([_P, _P], _I),
+    "lbm2d_download_f_device": ([_P, _P], _I),
+    "lbm2d_step": ([_P, _D, _D, _I], _I),
+    "lbm2d_force_sums": ([_P, _DP, _DP], _I),
+    "lbm2d_force_history": ([_P, _DP, _DP, _I, C.POINTER(_I)], _I),
+    "lbm2d_force_history_reset": ([_P], _I),
+    "lbm2d_download_f": ([_P, _DP], _I),
+    "lbm2d_download_g": ([_P, _DP], _I),
+    "lbm2d_download_force_field": ([_P, _DP, _DP], _I),
+    "lbm2d_download_macros": ([_P, _DP, _DP, _DP, _DP], _I),
+    "lbm2d_download_wall_dist": ([_P, _DP], _I),
+    "lbm2d_synchronize": ([_P], _I),
+    "lbm2d_get_info": ([_P, C.POINTER(Info)], _I),
+    "lbm2d_set_block": ([_P, _I, _I], _I),
+    "lbm2d_stream": ([_P], _P),
+    "lbm2d_set_profiling": ([_P, _I], _I),
+    "lbm2d_profile": ([_P, _DP, C.POINTER(C.c_longlong)], _I),
+    "lbm2d_launch_count": ([_P], C.c_longlong),
+    # host services
+    "lbm2d_equilibrium": ([_I, _D, _D, _D], _D),
+    "lbm2d_mask_walls": ([_I, _I, _U8P], _I),
+    "lbm2d_mask_cylinder": ([_I, _I, _U8P, _I, _I, _I], _I),
+    "lbm2d_mask_polygon": ([_I, _I, _U8P, _DP, _I], _I),
+    "lbm2d_point_in_polygon": ([_D, _D, _DP, _I], _I),
+    "lbm2d_naca_coords": ([_I, _I, _DP], _I),
+    "lbm2d_transform_points": ([_DP, _I, _D, _D, _D, _D], _I),
+    "lbm2d_wall_distance": ([_I, _I, _U8P, _DP], _I),
+    "lbm2d_boundary_links": ([_I, _I, _I, _U8P, C.POINTER(BBGeometry), _I, C.POINTER(C.c_int32),
+                              C.POINTER(C.c_int8), C.POINTER(C.c_int8), _DP, _DP, _DP,
+                              C.POINTER(C.c_int8), C.POINTER(_I)], _I),
+}
+
+_lib: C.CDLL | None = None
+
+
+def build(force: bool = False, quiet: bool = False) -> str:
+    return _build_lib(force=force, quiet=quiet)
+
+
+def lib() -> C.CDLL:
+    """Load liblbm2d.so (in-tree).  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"{LIB} is not built; call lbm2d.build() first")
+        L = C.CDLL(LIB)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def _d(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def _u8(a: np.ndarray):
+    return a.ctypes.data_as(_U8P)
+
+
+# ---------------------------------------------------------------- host services
+def equilibrium(i, rho, u, v) -> float:
+    return lib().lbm2d_equilibrium(int(i), float(rho), float(u), float(v))
+
+
+def equilibrium_field(nx, ny, rho, u, v) -> np.ndarray:
+    """Uniform equilibrium populations [nx*ny*9] (FP64 AoS), as the drivers' init loops."""
+    one = np.array([equilibrium(i, rho, u, v) for i in range(9)])
+    return np.tile(one, nx * ny)
+
+
+def naca_coords(series: int, n: int = 200) -> np.ndarray:
+    out = np.zeros(2 * (2 * n), np.float64)
+    k = lib().lbm2d_naca_coords(int(series), int(n), _d(out))
+    return out[: 2 * k].reshape(-1, 2).copy()
+
+
+def transform_points(xy, cx, cy, scale, angle_deg) -> np.ndarray:
+    a = np.ascontiguousarray(xy, np.float64).reshape(-1).copy()
+    lib().lbm2d_transform_points(_d(a), len(a) // 2, float(cx), float(cy), float(scale), float(angle_deg))
+    return a.reshape(-1, 2)
+
+
+def point_in_polygon(px, py, xy) -> bool:
+    a = np.ascontiguousarray(xy, np.float64).reshape(-1)
+    return bool(lib().lbm2d_point_in_polygon(float(px), float(py), _d(a), len(a) // 2))
+
+
+def wall_distance(nx, ny, mask) -> np.ndarray:
+    m = np.ascontiguousarray(mask, np.uint8).reshape(-1)
+    out = np.zeros(nx * ny, np.float64)
+    lib().lbm2d_wall_distance(nx, ny, _u8(m), _d(out))
+    return out
+
+
+def boundary_links(nx, ny, case_type, mask, cylinder=None, polygon=None, moving_wall=None) -> dict:
+    """The reference's bounce-back link list for a mask (see include/lbm2d.h)."""
+    m = np.ascontiguousarray(mask, np.uint8).reshape(-1)
+    g = BBGeometry()
+    keep = None
+    if cylinder is not None:
+        g.cx, g.cy, g.radius = map(float, cylinder)
+    if polygon is not None:
+        keep = np.ascontiguousarray(polygon, np.float64).reshape(-1)
+        g.poly = _d(keep)
+        g.n_poly = len(keep) // 2
+    if moving_wall is not None:
+        g.has_moving_wall = 1
+        g.omega, g.rot_cx, g.rot_cy = map(float, moving_wall)
+    cnt = C.c_int(0)
+    L = lib()
+    rc = L.lbm2d_boundary_links(nx, ny, case_type, _u8(m), C.byref(g), 0, None, None, None, None, None, None,
+                                None, C.byref(cnt))
+    if rc:
+        raise LBMError(rc, "boundary_links")
+    n = cnt.value
+    out = dict(node=np.zeros(n, np.int32), dir=np.zeros(n, np.int8), kind=np.zeros(n, np.int8),
+               q=np.zeros(n), uwx=np.zeros(n), uwy=np.zeros(n), force=np.zeros(n, np.int8))
+    L.lbm2d_boundary_links(nx, ny, case_type, _u8(m), C.byref(g), n,
+                           out["node"].ctypes.data_as(C.POINTER(C.c_int32)),
+                           out["dir"].ctypes.data_as(C.POINTER(C.c_int8)),
+                           out["kind"].ctypes.data_as(C.POINTER(C.c_int8)),
+                           _d(out["q"]), _d(out["uwx"]), _d(out["uwy"]),
+                           out["force"].ctypes.data_as(C.POINTER(C.c_int8)), C.byref(cnt))
+    del keep
+    return out
+
+
+# ---------------------------------------------------------------- solver
+class Solver:
+    """One GPU solver instance (the reference's LBMCapabilities + globals)."""
+
+    def __init__(self, nx: int, ny: int, case_type: int = CYLINDER, collision: int = MRT, use_les: bool = False,
+                 cs: float = 0.12, storage: str = "fp32", device: int = 0):
+        L = lib()
+        cfg = Config(nx, ny, case_type, collision, int(bool(use_les)), cs, STORAGE[storage], device)
+        h = _P()
+        rc = L.lbm2d_create(C.byref(cfg), C.byref(h))
+        if rc:
+            raise LBMError(rc, L.lbm2d_global_error().decode())
+        self.h = h
+        self.L = L
+        self.nx, self.ny = nx, ny
+        self.storage = storage
+        self.obstacle = np.zeros(nx * ny, np.uint8)
+        self._mask_sent = None
+
+    # -- plumbing
+    def _ck(self, rc):
+        if rc:
+            raise LBMError(rc, self.L.lbm2d_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lbm2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _sync_mask(self):
+        if self._mask_sent is None or not np.array_equal(self._mask_sent, self.obstacle):
+            m = np.ascontiguousarray(self.obstacle, np.uint8)
+            self._ck(self.L.lbm2d_set_mask(self.h, _u8(m)))
+            self._mask_sent = m.copy()
+
+    # -- configuration (reference names)
+    def set_case(self, case_type, collision=MRT, use_les=False, cs=0.12):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_set_case(self.h, int(case_type), int(collision), int(bool(use_les)), float(cs)))
+
+    def place_walls(self):
+        self._ck(self.L.lbm2d_mask_walls(self.nx, self.ny, _u8(self.obstacle)))
+
+    def place_cylinder(self, cx, cy, r):
+        self._ck(self.L.lbm2d_mask_cylinder(self.nx, self.ny, _u8(self.obstacle), int(cx), int(cy), int(r)))
+        self.set_bb_cylinder(cx, cy, r)
+
+    def place_polygon(self, xy):
+        a = np.ascontiguousarray(xy, np.float64).reshape(-1)
+        self._ck(self.L.lbm2d_mask_polygon(self.nx, self.ny, _u8(self.obstacle), _d(a), len(a) // 2))
+        self.set_bb_polygon(a)
+
+    def set_bb_cylinder(self, cx, cy, r):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_set_bb_cylinder(self.h, float(cx), float(cy), float(r)))
+
+    def set_bb_polygon(self, xy):
+        self._sync_mask()
+        a = np.ascontiguousarray(xy, np.float64).reshape(-1)
+        self._ck(self.L.lbm2d_set_bb_polygon(self.h, _d(a), len(a) // 2))
+
+    def set_moving_wall(self, on, omega=0.0, rcx=0.0, rcy=0.0):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_set_moving_wall(self.h, int(bool(on)), float(omega), float(rcx), float(rcy)))
+
+    def set_mei(self, on):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_set_mei(self.h, int(bool(on))))
+
+    def set_body_force(self, fx):
+        self._ck(self.L.lbm2d_set_body_force(self.h, float(fx)))
+
+    def set_thermal(self, use, T_ref=1.0, alpha=0.1666666667, omega_k=1.0, beta=0.0, g_buoyancy=0.0):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_set_thermal(self.h, int(bool(use)), T_ref, alpha, omega_k, beta, g_buoyancy))
+
+    def set_thermal_hook(self, kind, Ta=0.0, Tb=0.0):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_set_thermal_hook(self.h, int(kind), float(Ta), float(Tb)))
+
+    def set_block(self, bx, by):
+        self._ck(self.L.lbm2d_set_block(self.h, int(bx), int(by)))
+
+    # -- state
+    def upload_f(self, f):
+        self._sync_mask()
+        a = np.ascontiguousarray(f, np.float64).reshape(-1)
+        assert a.size == self.nx * self.ny * 9
+        self._ck(self.L.lbm2d_upload_f(self.h, _d(a)))
+
+    def upload_g(self, g):
+        self._sync_mask()
+        a = np.ascontiguousarray(g, np.float64).reshape(-1)
+        assert a.size == self.nx * self.ny * 9
+        self._ck(self.L.lbm2d_upload_g(self.h, _d(a)))
+
+    def init_uniform(self, rho, u, v):
+        self.upload_f(equilibrium_field(self.nx, self.ny, rho, u, v))
+
+    def step(self, tau, u_in, n=1):
+        self._sync_mask()
+        self._ck(self.L.lbm2d_step(self.h, float(tau), float(u_in), int(n)))
+
+    def synchronize(self):
+        self._ck(self.L.lbm2d_synchronize(self.h))
+
+    def force_sums(self):
+        a, b = _D(), _D()
+        self._ck(self.L.lbm2d_force_sums(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def force_history(self, n=None):
+        cnt = _I(0)
+        self._ck(self.L.lbm2d_force_history(self.h, None, None, 0, C.byref(cnt)))
+        m = cnt.value if n is None else min(n, cnt.value)
+        fx, fy = np.zeros(m), np.zeros(m)
+        self._ck(self.L.lbm2d_force_history(self.h, _d(fx), _d(fy), m, C.byref(cnt)))
+        return fx, fy
+
+    def force_history_reset(self):
+        self._ck(self.L.lbm2d_force_history_reset(self.h))
+
+    @property
+    def f(self) -> np.ndarray:
+        out = np.empty(self.nx * self.ny * 9, np.float64)
+        self._ck(self.L.lbm2d_download_f(self.h, _d(out)))
+        return out
+
+    @property
+    def g(self) -> np.ndarray:
+        out = np.empty(self.nx * self.ny * 9, np.float64)
+        self._ck(self.L.lbm2d_download_g(self.h, _d(out)))
+        return out
+
+    def force_field(self):
+        fx = np.empty(self.nx * self.ny, np.float64)
+        fy = np.empty(self.nx * self.ny, np.float64)
+        self._ck(self.L.lbm2d_download_force_field(self.h, _d(fx), _d(fy)))
+        return fx, fy
+
+    @property
+    def fx(self):
+        return self.force_field()[0]
+
+    @property
+    def fy(self):
+        return self.force_field()[1]
+
+    def macros(self, thermal=False):
+        n = self.nx * self.ny
+        rho, u, v = np.empty(n), np.empty(n), np.empty(n)
+        T = np.empty(n) if thermal else None
+        self._ck(self.L.lbm2d_download_macros(self.h, _d(rho), _d(u), _d(v), _d(T) if thermal else None))
+        return (rho, u, v, T) if thermal else (rho, u, v)
+
+    @property
+    def wall_dist(self):
+        out = np.empty(self.nx * self.ny, np.float64)
+        self._ck(self.L.lbm2d_download_wall_dist(self.h, _d(out)))
+        return out
+
+    def info(self) -> Info:
+        i = Info()
+        self._sync_mask()
+        self._ck(self.L.lbm2d_get_info(self.h, C.byref(i)))
+        return i
+
+    def set_profiling(self, on: bool):
+        self._ck(self.L.lbm2d_set_profiling(self.h, int(bool(on))))
+
+    def profile(self):
+        """(summed step-kernel milliseconds, timed launches) since the last call."""
+        ms, n = _D(), C.c_longlong()
+        self._ck(self.L.lbm2d_profile(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def upload_f_ptr(self, host_ptr: int):
+        """Upload populations from a host pointer (e.g. pinned memory)."""
+        self._sync_mask()
+        self._ck(self.L.lbm2d_upload_f(self.h, C.cast(host_ptr, _DP)))
+
+    def download_f_ptr(self, host_ptr: int):
+        self._ck(self.L.lbm2d_download_f(self.h, C.cast(host_ptr, _DP)))
+
+    @property
+    def stream(self) -> int:
+        return int(self.L.lbm2d_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.lbm2d_launch_count(self.h))
