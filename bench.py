@@ -133,9 +133,9 @@ def make_geometry(nx=NX, ny=NY, n_circles=N_CIRCLES):
     return mask, circles
 
 
-def configure(lbm2d, storage, mask, circles, device=0, nx=NX, ny=NY):
-    s = lbm2d.Solver(nx, ny, lbm2d.RIBS, lbm2d.MRT, True, CS_LES, storage, device)
-    s.obstacle[:] = mask
+def configure(lbm2d, storage, mask, circles, device=0, nx=NX, ny=NY, les=True):
+    s = lbm2d.Solver(nx, ny, lbm2d.RIBS, lbm2d.MRT, les, CS_LES, storage, device)
+    s.set_mask(mask)
     cx, cy, r = circles[-1]
     s.set_bb_cylinder(cx, cy, r)  # bb_geom keeps the last placed circle (unused by the periodic case)
     s.set_body_force(BODY_FORCE)
@@ -180,56 +180,67 @@ def time_e2e(lbm2d, s, torch, steps, f0_pinned, fout_pinned):
     return (t1 - t0) * 1e3, s.launches - l0
 
 
-def cpu_sample(threads: int | None = None, size: int = 1024, steps: int = 2):
-    """The oracle (OpenMP restatement of the reference step, including its
-    per-step wall-distance sweep under LES) on a bounded sample of the
-    workload: the same generator at size x size with circles scaled by area."""
+def _oracle_channel(size):
     from oracle import oracle as O
     if not os.path.exists(O.LIB_ORACLE):
         O.build()
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
     nc = max(1, int(round(N_CIRCLES * (size * size) / (NX * NY))))
-    mask, circles = CS.channel_circles_mask(size, size, nc, RMIN, RMAX, SEED)
+    mask, _ = CS.channel_circles_mask(size, size, nc, RMIN, RMAX, SEED)
     s = O.Solver(size, size)
     s.set_case(O.RIBS, O.MRT, True, CS_LES)
     s.obstacle[:] = mask
-    s.set_body_force(12.0 * NU * U0 / ((size - 2) ** 2))
+    s.set_body_force(BODY_FORCE)
     s.init_uniform(1.0, U0, 0.0)
+    return s, nc
+
+
+def cpu_sample(size: int = 1024, budget_s: float = 12.0, max_steps: int = 50):
+    """The oracle (OpenMP restatement of the reference step, including its
+    per-step wall-distance sweep under LES) on a bounded sample of the
+    workload: the same generator and physics at size x size, circles scaled
+    by area; steps are timed until about `budget_s` of CPU work."""
+    s, nc = _oracle_channel(size)
     s.step(TAU, U0)  # warm-up
-    t0 = time.perf_counter()
-    s.step(TAU, U0, steps)
+    n, t0 = 0, time.perf_counter()
+    while n < max_steps and (time.perf_counter() - t0) < budget_s:
+        s.step(TAU, U0)
+        n += 1
     dt = time.perf_counter() - t0
     s.close()
-    mlups = size * size * steps / dt / 1e6
-    return mlups, dt, nc
+    return size * size * n / dt / 1e6, dt, nc, n
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    from oracle import oracle as O
-    if not os.path.exists(O.LIB_ORACLE):
-        O.build()
     cores = os.cpu_count() or 1
     size = args.cpu_size
+    s, nc = _oracle_channel(size)
+    for _ in range(min(args.warmup, 1)):
+        s.step(TAU, U0)
     per = []
-    for _ in range(max(1, args.warmup and 1)):
-        cpu_sample(cores, size, 1)
-    for _ in range(args.steps):
-        mlups, dt, nc = cpu_sample(cores, size, 1)
-        per.append(dt)
+    t_all = time.perf_counter()
+    for _ in range(args.steps):  # each step is one oracle step over the size x size sample
+        t0 = time.perf_counter()
+        s.step(TAU, U0)
+        per.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > args.ref_budget:
+            break
+    s.close()
     dt = float(np.sum(per))
     value = size * size * len(per) / dt / 1e9
     line = {
-        "impl": "reference", "metric": "GLUPS (D2Q9 step, lattice updates/s)", "value": value, "unit": "GLUPS",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / len(per) * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": f"{size}x{size}, {nc} circles, 1 step per timed step"},
+        "impl": "reference", "metric": "GLUPS (D2Q9 step, lattice updates/s) & %HBM roofline, FP32 vs FP16/BF16 storage",
+        "value": value, "unit": "GLUPS", "n_gpus": args.gpus, "steps": len(per), "warmup": args.warmup,
+        "ms_per_step": dt / len(per) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args.nx, args.ny),
+                   "sample": f"{size}x{size} with {nc} circles (same generator and physics), "
+                             f"{len(per)} of {args.steps} requested steps within {args.ref_budget:.0f} s"},
         "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": "port",
-                         "sample": f"oracle (OpenMP restatement of the reference step incl. per-step wall-distance "
-                                   f"sweep) on {size}x{size} with {nc} circles, {len(per)} steps"},
+                         "sample": f"oracle/lbm_oracle.c (OpenMP restatement of the reference step incl. its "
+                                   f"per-step wall-distance sweep), {cores} threads, {size}x{size}, {len(per)} steps"},
         "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -245,7 +256,9 @@ def main():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--storages", default="fp32,fp16,bf16")
-    ap.add_argument("--cpu-size", type=int, default=512)
+    ap.add_argument("--plain", default="fp32,fp16", help="storages also timed without LES (plain MRT)")
+    ap.add_argument("--cpu-size", type=int, default=1024)
+    ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (default: --steps)")
@@ -269,13 +282,14 @@ def main():
 
     nx, ny = args.nx, args.ny
     storages = [x for x in args.storages.split(",") if x]
+    runs = [(st, st, True) for st in storages] + [(st + "_plain", st, False) for st in args.plain.split(",") if st]
     mask, circles = make_geometry(nx, ny)
     f0 = lbm2d.equilibrium_field(nx, ny, 1.0, U0, 0.0)
     clocks = ClockSampler(local)
     clocks.start()
     results = {}
-    for storage in storages:
-        s = configure(lbm2d, storage, mask, circles, local, nx, ny)
+    for label, storage, les in runs:
+        s = configure(lbm2d, storage, mask, circles, local, nx, ny, les)
         s.upload_f(f0)
         if dist:
             dist.barrier()
@@ -292,12 +306,12 @@ def main():
         if dist:
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
         info = s.info()
-        results[storage] = dict(ms=float(t[0]), kernel_ms=kms, launches=launches, nan=nan,
+        results[label] = dict(ms=float(t[0]), kernel_ms=kms, launches=launches, nan=nan,
                                 bytes_per_update=info.bytes_per_update, boundary=info.n_boundary_nodes,
                                 force_nodes=info.n_force_nodes, block=(info.block_x, info.block_y))
-        if storage == storages[0] and not nan:
-            results[storage]["force"] = s.force_sums()
-        if storage == storages[0] and not args.no_e2e:
+        if label == storages[0] and not nan:
+            results[label]["force"] = s.force_sums()
+        if label == storages[0] and not args.no_e2e:
             # end-to-end through the public API with host buffers
             e2e_steps = args.e2e_steps or args.steps
             pin = torch.empty(nx * ny * 9, dtype=torch.float64, pin_memory=True)
@@ -334,13 +348,13 @@ def main():
     if tr and tr.get("storage") == main_st and tr.get("nodes"):
         traffic = float(tr["dram_bytes_per_launch"]) * nodes / float(tr["nodes"])
     prec = {}
-    for st in storages[1:]:
-        r = results[st]
+    for label, st, les in runs[1:]:
+        r = results[label]
         g = world * nodes * args.steps / (r["ms"] * 1e-3) / 1e9
         b = 2 * 9 * lbm2d.BYTES_PER_POP[st]
         kach = nodes * b / (r["kernel_ms"] * 1e-3) / 1e9
-        prec[st] = {"glups": g, "vs_" + main_st: g / value, "kernel_ms": r["kernel_ms"],
-                    "roofline_frac": kach / peak, "bytes_per_update": b, "diverged": r["nan"]}
+        prec[label] = {"glups": g, "vs_" + main_st: g / value, "kernel_ms": r["kernel_ms"], "les": les,
+                       "roofline_frac": kach / peak, "bytes_per_update": b, "diverged": r["nan"]}
     e2e = None
     if "e2e" in results:
         e = results["e2e"]
@@ -352,11 +366,11 @@ def main():
     if not args.no_cpu:
         try:
             cores = os.cpu_count() or 1
-            mlups, dt, nc = cpu_sample(cores, args.cpu_size, 2)
+            mlups, dt, nc, n = cpu_sample(args.cpu_size)
             cpu = {"value": mlups / 1e3, "unit": "GLUPS", "cores": cores, "kind": "port",
-                   "sample": f"oracle (OpenMP restatement of the reference step, per-step wall-distance sweep "
-                             f"included) on the same generator at {args.cpu_size}x{args.cpu_size}, {nc} circles, "
-                             f"2 steps, {dt:.1f} s"}
+                   "sample": f"oracle/lbm_oracle.c (OpenMP restatement of the reference step, per-step "
+                             f"wall-distance sweep included), {cores} threads, same generator and physics at "
+                             f"{args.cpu_size}x{args.cpu_size} with {nc} circles, {n} steps in {dt:.1f} s"}
         except Exception as ex:  # the CPU leg never blocks the GPU line
             cpu = {"value": None, "unit": "GLUPS", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {ex}"}

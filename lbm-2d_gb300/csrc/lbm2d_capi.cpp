@@ -195,6 +195,12 @@ KParams base_params(const lbm2d_solver* h) {
     p.hook_kind = h->thermal ? h->hook : 0;
     p.hook_a = h->hook_a;
     p.hook_b = h->hook_b;
+    p.pd.hook_a = h->hook_a;
+    p.pd.hook_b = h->hook_b;
+    p.pf.hook_a = float(h->hook_a);
+    p.pf.hook_b = float(h->hook_b);
+    p.pd.T_ref = h->T_ref;
+    p.pf.T_ref = float(h->T_ref);
     p.nan_flag = h->d_nan;
     const bool shifted = h->storage == ST_FP16 || h->storage == ST_BF16;
     for (int j = 0; j < 9; ++j) {
@@ -204,7 +210,33 @@ KParams base_params(const lbm2d_solver* h) {
     return p;
 }
 
+template <class R>
+void fill_phys(Phys<R>& q, const CollideParams& c) {
+    q.s_shear = R(c.s_shear);
+    q.s_bulk = R(c.s_bulk);
+    q.s_normal = R(c.s_normal);
+    q.tau = R(c.tau);
+    q.inv_tau = R(1.0 / c.tau);
+    q.cs_sq = R(c.cs_sq);
+    q.cs = R(std::sqrt(c.cs_sq));
+    q.nu = R(c.nu);
+    q.inv_nu = c.nu > 0.0 ? R(1.0 / c.nu) : R(0);
+    q.Fscale = R(c.Fscale);
+    q.omega_k = R(c.omega_k);
+    q.beta = R(c.beta);
+    q.g_buoy = R(c.g_buoy);
+    q.T_ref = R(c.T_ref);
+}
+
+void set_u_bc(KParams& p, double u) {
+    p.u_bc = u;
+    p.pd.u_bc = u;
+    p.pf.u_bc = float(u);
+}
+
 void apply_collide(KParams& p, const CollideParams& c) {
+    fill_phys(p.pd, c);
+    fill_phys(p.pf, c);
     p.collide = 1;
     p.collision = c.collision;
     p.s_shear = c.s_shear;
@@ -301,7 +333,7 @@ int upload_geometry(lbm2d_solver* h) {
 int ensure_slots(lbm2d_solver* h) {
     if (h->slot_bx == h->bx && h->slot_by == h->by && h->d_block_slot) return LBM2D_OK;
     std::vector<int> slots;
-    h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx, h->by, slots);
+    h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx, h->by, slots);  // per-warp slots
     dfree(h, &h->d_block_slot);
     dfree(h, &h->d_partials);
     int rc;
@@ -322,7 +354,7 @@ KParams rebuild_params(const lbm2d_solver* h) {
     KParams p = base_params(h);
     p.fin = h->P[h->cur ^ 1];
     p.gin = h->G[h->cur ^ 1];
-    p.u_bc = h->u_last;
+    set_u_bc(p, h->u_last);
     return p;
 }
 
@@ -396,8 +428,8 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
         return LBM2D_ERR_INVALID;
     }
     *out = nullptr;
-    if (cfg->nx < 3 || cfg->ny < 3 || (long long)cfg->nx * cfg->ny * 9 > (1LL << 40)) {
-        g_global_err = "grid must be at least 3x3";
+    if (cfg->nx < 3 || cfg->ny < 3 || (long long)cfg->nx * cfg->ny >= (1LL << 32)) {
+        g_global_err = "grid must be at least 3x3 and hold fewer than 2^32 nodes";
         return LBM2D_ERR_INVALID;
     }
     if (cfg->storage < 0 || cfg->storage > 3 || cfg->collision < 0 || cfg->collision > 1 || cfg->case_type < 0 ||
@@ -629,7 +661,7 @@ int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
     }
     KParams p = base_params(h);
     apply_collide(p, c);
-    p.u_bc = u_inflow;
+    set_u_bc(p, u_inflow);
     p.block_slot = h->nslots > 0 ? h->d_block_slot : nullptr;
     p.partials = h->d_partials;
     for (int k = 0; k < nsteps; ++k) {

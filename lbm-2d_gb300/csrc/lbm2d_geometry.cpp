@@ -209,9 +209,13 @@ int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, s
         const int x = id % nx, y = id / nx;
         slots[static_cast<size_t>(y / by) * gx + x / bx] = 0;
     }
+    const int warps = (bx * by + 31) / 32;  // each force block owns one slot per warp
     int k = 0;
     for (auto& s : slots)
-        if (s == 0) s = k++;
+        if (s == 0) {
+            s = k;
+            k += warps;
+        }
     return k;
 }
 

@@ -56,7 +56,9 @@ void wall_distance(int nx, int ny, const uint8_t* mask, std::vector<double>& out
 
 bool build_geometry(const GeometryInput& in, GeometryTables& out, std::string& err);
 
-// Per-block force slots for a launch shape (bx, by); returns the slot count.
+// Force-reduction slots for a launch shape (bx, by): every block holding a
+// force node gets one slot per warp starting at slots[block] (-1 otherwise);
+// returns the total slot count.
 int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, std::vector<int>& slots);
 
 }  // namespace lbm2d

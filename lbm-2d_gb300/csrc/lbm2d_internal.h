@@ -39,6 +39,15 @@ enum BcKind : int { BC_NONE = 0, BC_LID = 1, BC_INFLOW = 2, BC_STEP = 3 };
 
 enum Storage : int { ST_FP32 = 0, ST_FP16 = 1, ST_BF16 = 2, ST_FP64 = 3 };
 
+// Physical parameters of one step, held in both compute precisions so the
+// FP32 kernels never convert from double at run time.
+template <class R>
+struct Phys {
+    R s_shear, s_bulk, s_normal, tau, inv_tau, cs_sq, cs, inv_nu, nu, Fscale;
+    R omega_k, beta, g_buoy, T_ref;
+    R u_bc, hook_a, hook_b;
+};
+
 struct KParams {
     int nx, ny;
     long long N;  // nx*ny
@@ -70,8 +79,11 @@ struct KParams {
     double hook_a, hook_b;
     // storage shifts (FP16/BF16 store f - w*rho0, g - w*T_ref)
     float shf[9], shg[9];
-    // force reduction
-    const int* block_slot;  // per block: slot index or -1
+    Phys<float> pf;
+    Phys<double> pd;
+    // force reduction: blocks holding force nodes own (threads/32) consecutive
+    // per-warp slots starting at block_slot[block] (-1: no force node)
+    const int* block_slot;
     double* partials;       // [slot*2 + {0,1}]
     unsigned int* nan_flag;
     // solid nodes whose state can no longer change may skip their stores

@@ -74,6 +74,31 @@ struct Pop<__nv_bfloat16> {
     }
 };
 
+// Parameters in the compute precision.
+template <class R>
+__device__ __forceinline__ const Phys<R>& phys(const KParams& p);
+template <>
+__device__ __forceinline__ const Phys<float>& phys<float>(const KParams& p) { return p.pf; }
+template <>
+__device__ __forceinline__ const Phys<double>& phys<double>(const KParams& p) { return p.pd; }
+
+// Reciprocal / square root / exponential: hardware approximations (a few
+// ulp) in the FP32 path, IEEE in the FP64 path.
+template <class R>
+struct Fm;
+template <>
+struct Fm<float> {
+    static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
+    static __device__ __forceinline__ float sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+    static __device__ __forceinline__ float exp(float x) { return __expf(x); }
+};
+template <>
+struct Fm<double> {
+    static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+};
+
 // ----------------------------------------------------------------- lattice math
 // compute_equilibrium, src/lbm_types.hpp:269-273
 template <class R>
@@ -89,8 +114,9 @@ __device__ __forceinline__ void macros(const R f[9], R& rho, R& u, R& v) {
     rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
     R mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
     R my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
-    u = mx / rho;
-    v = my / rho;
+    const R inv = Fm<R>::rcp(rho);
+    u = mx * inv;
+    v = my * inv;
 }
 
 template <class R>
@@ -100,18 +126,19 @@ __device__ __forceinline__ R clamp_rate(R s) { return s < R(0.5) ? R(0.5) : (s >
 template <class T>
 __device__ __forceinline__ void pull(const KParams& p, const T* __restrict__ P, const float* sh, int x, int y,
                                      typename Pop<T>::R f[9]) {
-    const int nx = p.nx, ny = p.ny;
+    const unsigned nx = (unsigned)p.nx, ny = (unsigned)p.ny;
     const size_t N = (size_t)p.N;
-    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
-    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
+    const unsigned ux = (unsigned)x, uy = (unsigned)y;
+    const unsigned xm = ux == 0 ? nx - 1 : ux - 1, xp = ux == nx - 1 ? 0 : ux + 1;
+    const unsigned ym = uy == 0 ? ny - 1 : uy - 1, yp = uy == ny - 1 ? 0 : uy + 1;
+    const unsigned r0 = uy * nx, rm = ym * nx, rp = yp * nx;  // nx*ny < 2^32 (checked at create)
     // slot j pulls from (x - cx_j, y - cy_j), wrapped; records override the
     // slots whose source is solid or outside the domain.
-    f[0] = Pop<T>::ld(P, r0 + x, sh[0]);
+    f[0] = Pop<T>::ld(P, r0 + ux, sh[0]);
     f[1] = Pop<T>::ld(P + N, r0 + xm, sh[1]);
-    f[2] = Pop<T>::ld(P + 2 * N, rm + x, sh[2]);
+    f[2] = Pop<T>::ld(P + 2 * N, rm + ux, sh[2]);
     f[3] = Pop<T>::ld(P + 3 * N, r0 + xp, sh[3]);
-    f[4] = Pop<T>::ld(P + 4 * N, rp + x, sh[4]);
+    f[4] = Pop<T>::ld(P + 4 * N, rp + ux, sh[4]);
     f[5] = Pop<T>::ld(P + 5 * N, rm + xm, sh[5]);
     f[6] = Pop<T>::ld(P + 6 * N, rm + xp, sh[6]);
     f[7] = Pop<T>::ld(P + 7 * N, rp + xp, sh[7]);
@@ -231,23 +258,23 @@ __device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint
     if (p.bc_kind == BC_LID) {
         if (y == p.ny - 1) {  // enforce_lid :110-120 (corner nodes included)
             R rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
-            const R ul = R(p.u_bc);
+            const R ul = phys<R>(p).u_bc;
 #pragma unroll
             for (int i = 0; i < 9; ++i) f[i] = feq<R>(i, rho, ul, R(0));
         }
     } else if (p.bc_kind == BC_INFLOW) {
-        if (x == 0) zou_he<R>(f, R(p.u_bc));
+        if (x == 0) zou_he<R>(f, phys<R>(p).u_bc);
     } else if (p.bc_kind == BC_STEP) {
         const int hs = p.ny / 3;
         if (x == 0 && y >= hs && !(fl & FLAG_SOLID)) {
             const R yy = R(y - hs), h = R(p.ny - 1 - hs);
-            zou_he<R>(f, R(p.u_bc) * R(4) * yy * (h - yy) / (h * h));
+            zou_he<R>(f, phys<R>(p).u_bc * R(4) * yy * (h - yy) / (h * h));
         }
     }
     if (TH && p.hook_kind == 1) {
         // src/thermal_cavity.cpp:168-204: Dirichlet columns, then adiabatic rows
         if ((x == 1 || x == p.nx - 2) && y >= 1 && y <= p.ny - 2) {
-            const R Tw = R(x == p.nx - 2 ? p.hook_b : p.hook_a);
+            const R Tw = x == p.nx - 2 ? phys<R>(p).hook_b : phys<R>(p).hook_a;
             R rho, u, v;
             macros(f, rho, u, v);
 #pragma unroll
@@ -262,7 +289,7 @@ __device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint
     } else if (TH && p.hook_kind == 2) {
         if (fl & FLAG_SOLID) {  // src/heated_cylinder.cpp:156-164
 #pragma unroll
-            for (int i = 0; i < 9; ++i) g[i] = R(wgt(i)) * R(p.hook_a);
+            for (int i = 0; i < 9; ++i) g[i] = R(wgt(i)) * phys<R>(p).hook_a;
         }
     }
 }
@@ -279,14 +306,16 @@ __device__ __forceinline__ R wall_distance(const KParams& p, uint32_t fl) {
 // collision with Boussinesq/Guo forcing :357-397 (src/thermal.hpp:25-52).
 template <class R, bool TH>
 __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R g[9]) {
+    const Phys<R>& q = phys<R>(p);
     R rho, u, v;
     macros(f, rho, u, v);
     if (!(rho == rho) || rho == R(0)) atomicOr(p.nan_flag, 1u);
     if (p.collision == 0) {
         const R f0 = f[0], f1 = f[1], f2 = f[2], f3 = f[3], f4 = f[4];
         const R f5 = f[5], f6 = f[6], f7 = f[7], f8 = f[8];
-        R me = R(-4) * f0 - f1 - f2 - f3 - f4 + R(2) * (f5 + f6 + f7 + f8);
-        R meps = R(4) * f0 - R(2) * (f1 + f2 + f3 + f4) + (f5 + f6 + f7 + f8);
+        const R sd = f5 + f6 + f7 + f8, sa = f1 + f2 + f3 + f4;
+        R me = R(-4) * f0 - sa + R(2) * sd;
+        R meps = R(4) * f0 - R(2) * sa + sd;
         R mqx = R(-2) * f1 + R(2) * f3 + f5 - f6 - f7 + f8;
         R mqy = R(-2) * f2 + R(2) * f4 + f5 + f6 - f7 - f8;
         R mpxx = f1 - f2 + f3 - f4;
@@ -297,39 +326,37 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
         const R eps_eq = rho - R(3) * rho * usq;
         const R pxx_eq = rho * (u * u - v * v);
         const R pxy_eq = rho * u * v;
-        R s_eff = R(p.s_shear);
+        R s_eff = q.s_shear;
         if (p.les) {
-            const R tau = R(p.tau), cs_sq = R(p.cs_sq), nu = R(p.nu);
-            R csq = cs_sq;
-            if (nu > R(0)) {
+            // Smagorinsky with Van Driest damping (src/lbm.hpp:158-182, y+ :317-325);
+            // the damped branch always applies when y+ > 0
+            R csq = q.cs_sq;
+            if (q.nu > R(0)) {
                 const R wd = wall_distance<R>(p, fl);
-                const R speed = sqrt(u * u + v * v);
-                const R yp = wd * sqrt(speed * speed + R(1e-12)) / nu;
-                if (yp > R(0)) {  // Van Driest damping always wins when y+ > 0 (:171-182)
-                    const R damp = R(1) - exp(-yp / R(26));
-                    const R cd = sqrt(cs_sq) * damp;
+                const R yp = wd * Fm<R>::sqrt(usq + R(1e-12)) * q.inv_nu;
+                if (yp > R(0)) {
+                    const R cd = q.cs * (R(1) - Fm<R>::exp(-yp * R(1.0 / 26.0)));
                     csq = cd * cd;
                 }
             }
             const R a = mpxx - pxx_eq, b = mpxy - pxy_eq;
-            const R Q = sqrt(R(2) * (a * a + b * b));
-            const R A = R(9) * csq * Q / (R(2) * rho);
-            const R te = (tau + sqrt(tau * tau + R(4) * A)) / R(2);
-            s_eff = clamp_rate<R>(R(1) / te);
+            const R Q = Fm<R>::sqrt(R(2) * (a * a + b * b));
+            const R A = R(4.5) * csq * Q * Fm<R>::rcp(rho);
+            const R te2 = q.tau + Fm<R>::sqrt(q.tau * q.tau + R(4) * A);  // 2 * tau_eff
+            s_eff = clamp_rate<R>(R(2) * Fm<R>::rcp(te2));
         }
-        const R sb = R(p.s_bulk), sn = R(p.s_normal);
-        me -= sb * (me - e_eq);
-        meps -= sb * (meps - eps_eq);
-        mqx -= sn * (mqx + jx);
-        mqy -= sn * (mqy + jy);
+        me -= q.s_bulk * (me - e_eq);
+        meps -= q.s_bulk * (meps - eps_eq);
+        mqx -= q.s_normal * (mqx + jx);
+        mqy -= q.s_normal * (mqy + jy);
         mpxx -= s_eff * (mpxx - pxx_eq);
         mpxy -= s_eff * (mpxy - pxy_eq);
         // closed-form inverse transform (src/lbm.hpp:193-217), common terms shared
         const R a0 = R(1.0 / 9.0) * rho;
         const R ax = a0 - R(1.0 / 36.0) * me - R(1.0 / 18.0) * meps;  // axial base
         const R ad = a0 + R(1.0 / 18.0) * me + R(1.0 / 36.0) * meps;  // diagonal base
-        const R hx = R(1.0 / 6.0) * jx - R(1.0 / 6.0) * mqx;
-        const R hy = R(1.0 / 6.0) * jy - R(1.0 / 6.0) * mqy;
+        const R hx = R(1.0 / 6.0) * (jx - mqx);
+        const R hy = R(1.0 / 6.0) * (jy - mqy);
         const R dx = R(1.0 / 6.0) * jx + R(1.0 / 12.0) * mqx;
         const R dy = R(1.0 / 6.0) * jy + R(1.0 / 12.0) * mqy;
         const R px = R(0.25) * mpxx, py = R(0.25) * mpxy;
@@ -343,12 +370,12 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
         f[7] = ad - dx - dy + py;
         f[8] = ad + dx - dy - py;
     } else {
-        const R it = R(1) / R(p.tau);
+        const R it = q.inv_tau;
 #pragma unroll
         for (int i = 0; i < 9; ++i) f[i] -= it * (f[i] - feq<R>(i, rho, u, v));
     }
     if (p.Fscale != 0.0) {
-        const R F = R(p.Fscale);
+        const R F = q.Fscale;
         const R fa = R(1.0 / 9.0) * F, fd = R(1.0 / 36.0) * F;
         f[1] += fa;
         f[3] -= fa;
@@ -361,11 +388,11 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
         R rho2, u2, v2;
         macros(f, rho2, u2, v2);
         const R T = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8];
-        const R om = R(p.omega_k);
+        const R om = q.omega_k;
 #pragma unroll
         for (int i = 0; i < 9; ++i) g[i] -= om * (g[i] - feq<R>(i, T, u2, v2));
-        if (p.beta > 0.0 && p.g_buoy != 0.0) {
-            const R fyb = -R(p.beta) * (T - R(p.T_ref)) * R(p.g_buoy);
+        if (p.pd.beta > 0.0 && p.pd.g_buoy != 0.0) {
+            const R fyb = -q.beta * (T - q.T_ref) * q.g_buoy;
 #pragma unroll
             for (int i = 0; i < 9; ++i) {
                 const R eu = R(CXf(i)) * u2 + R(CYf(i)) * v2;
@@ -407,23 +434,22 @@ __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
     using R = typename Pop<T>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    double fxs = 0.0, fys = 0.0;
+    R fxs = R(0), fys = R(0);
     if (x < p.nx && y < p.ny) {
-        const size_t n = (size_t)y * p.nx + x;
+        const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
         const uint32_t fl = __ldg(p.flags + n);
         R f[9], g[9];
         build_state<T, TH>(p, x, y, fl, f, g);
         if (!(fl & FLAG_SOLID)) {
             if (fl & FLAG_BOUNDARY) {
+                // momentum exchange of this node's links (src/lbm.hpp:565-577)
                 const uint32_t fm = p.rec_force[fl >> 2];
-                if (fm) {
 #pragma unroll
-                    for (int j = 0; j < 9; ++j)
-                        if (fm & (1u << j)) {
-                            fxs += double(-CXf(j)) * 2.0 * double(f[j]);
-                            fys += double(-CYf(j)) * 2.0 * double(f[j]);
-                        }
-                }
+                for (int j = 1; j < 9; ++j)
+                    if (fm & (1u << j)) {
+                        fxs -= R(CXf(j)) * R(2) * f[j];
+                        fys -= R(CYf(j)) * R(2) * f[j];
+                    }
             }
             collide<R, TH>(p, fl, f, g);
         }
@@ -440,12 +466,19 @@ __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
         }
     }
     if (p.block_slot) {
-        const int slot = p.block_slot[blockIdx.y * gridDim.x + blockIdx.x];
-        if (slot >= 0) {  // uniform per block
-            block_reduce2(fxs, fys);
-            if (threadIdx.x == 0 && threadIdx.y == 0) {
-                p.partials[2 * slot] = fxs;
-                p.partials[2 * slot + 1] = fys;
+        const int base = p.block_slot[blockIdx.y * gridDim.x + blockIdx.x];
+        if (base >= 0) {  // uniform per block; no barrier: one slot per warp
+            double a = double(fxs), b = double(fys);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_down_sync(0xffffffffu, a, o);
+                b += __shfl_down_sync(0xffffffffu, b, o);
+            }
+            const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+            if ((tid & 31) == 0) {
+                const int slot = base + (tid >> 5);
+                p.partials[2 * slot] = a;
+                p.partials[2 * slot + 1] = b;
             }
         }
     }

@@ -222,8 +222,7 @@ class Solver:
         self.L = L
         self.nx, self.ny = nx, ny
         self.storage = storage
-        self.obstacle = np.zeros(nx * ny, np.uint8)
-        self._mask_sent = None
+        self._mask = np.zeros(nx * ny, np.uint8)
 
     # -- plumbing
     def _ck(self, rc):
@@ -247,55 +246,62 @@ class Solver:
     def __exit__(self, *a):
         self.close()
 
-    def _sync_mask(self):
-        if self._mask_sent is None or not np.array_equal(self._mask_sent, self.obstacle):
-            m = np.ascontiguousarray(self.obstacle, np.uint8)
-            self._ck(self.L.lbm2d_set_mask(self.h, _u8(m)))
-            self._mask_sent = m.copy()
+    @property
+    def obstacle(self) -> np.ndarray:
+        """Solid mask (read-only view); change it with set_mask or place_*."""
+        v = self._mask.view()
+        v.flags.writeable = False
+        return v
+
+    def set_mask(self, mask):
+        """LBMCapabilities::obstacle: one byte per node, pushed to the solver."""
+        m = np.ascontiguousarray(mask, np.uint8).reshape(-1)
+        assert m.size == self.nx * self.ny
+        self._mask = (m != 0).astype(np.uint8)
+        self._ck(self.L.lbm2d_set_mask(self.h, _u8(self._mask)))
 
     # -- configuration (reference names)
     def set_case(self, case_type, collision=MRT, use_les=False, cs=0.12):
-        self._sync_mask()
         self._ck(self.L.lbm2d_set_case(self.h, int(case_type), int(collision), int(bool(use_les)), float(cs)))
 
     def place_walls(self):
-        self._ck(self.L.lbm2d_mask_walls(self.nx, self.ny, _u8(self.obstacle)))
+        m = self._mask.copy()
+        self._ck(self.L.lbm2d_mask_walls(self.nx, self.ny, _u8(m)))
+        self.set_mask(m)
 
     def place_cylinder(self, cx, cy, r):
-        self._ck(self.L.lbm2d_mask_cylinder(self.nx, self.ny, _u8(self.obstacle), int(cx), int(cy), int(r)))
+        m = self._mask.copy()
+        self._ck(self.L.lbm2d_mask_cylinder(self.nx, self.ny, _u8(m), int(cx), int(cy), int(r)))
+        self.set_mask(m)
         self.set_bb_cylinder(cx, cy, r)
 
     def place_polygon(self, xy):
         a = np.ascontiguousarray(xy, np.float64).reshape(-1)
-        self._ck(self.L.lbm2d_mask_polygon(self.nx, self.ny, _u8(self.obstacle), _d(a), len(a) // 2))
+        m = self._mask.copy()
+        self._ck(self.L.lbm2d_mask_polygon(self.nx, self.ny, _u8(m), _d(a), len(a) // 2))
+        self.set_mask(m)
         self.set_bb_polygon(a)
 
     def set_bb_cylinder(self, cx, cy, r):
-        self._sync_mask()
         self._ck(self.L.lbm2d_set_bb_cylinder(self.h, float(cx), float(cy), float(r)))
 
     def set_bb_polygon(self, xy):
-        self._sync_mask()
         a = np.ascontiguousarray(xy, np.float64).reshape(-1)
         self._ck(self.L.lbm2d_set_bb_polygon(self.h, _d(a), len(a) // 2))
 
     def set_moving_wall(self, on, omega=0.0, rcx=0.0, rcy=0.0):
-        self._sync_mask()
         self._ck(self.L.lbm2d_set_moving_wall(self.h, int(bool(on)), float(omega), float(rcx), float(rcy)))
 
     def set_mei(self, on):
-        self._sync_mask()
         self._ck(self.L.lbm2d_set_mei(self.h, int(bool(on))))
 
     def set_body_force(self, fx):
         self._ck(self.L.lbm2d_set_body_force(self.h, float(fx)))
 
     def set_thermal(self, use, T_ref=1.0, alpha=0.1666666667, omega_k=1.0, beta=0.0, g_buoyancy=0.0):
-        self._sync_mask()
         self._ck(self.L.lbm2d_set_thermal(self.h, int(bool(use)), T_ref, alpha, omega_k, beta, g_buoyancy))
 
     def set_thermal_hook(self, kind, Ta=0.0, Tb=0.0):
-        self._sync_mask()
         self._ck(self.L.lbm2d_set_thermal_hook(self.h, int(kind), float(Ta), float(Tb)))
 
     def set_block(self, bx, by):
@@ -303,13 +309,11 @@ class Solver:
 
     # -- state
     def upload_f(self, f):
-        self._sync_mask()
         a = np.ascontiguousarray(f, np.float64).reshape(-1)
         assert a.size == self.nx * self.ny * 9
         self._ck(self.L.lbm2d_upload_f(self.h, _d(a)))
 
     def upload_g(self, g):
-        self._sync_mask()
         a = np.ascontiguousarray(g, np.float64).reshape(-1)
         assert a.size == self.nx * self.ny * 9
         self._ck(self.L.lbm2d_upload_g(self.h, _d(a)))
@@ -318,7 +322,6 @@ class Solver:
         self.upload_f(equilibrium_field(self.nx, self.ny, rho, u, v))
 
     def step(self, tau, u_in, n=1):
-        self._sync_mask()
         self._ck(self.L.lbm2d_step(self.h, float(tau), float(u_in), int(n)))
 
     def synchronize(self):
@@ -381,7 +384,6 @@ class Solver:
 
     def info(self) -> Info:
         i = Info()
-        self._sync_mask()
         self._ck(self.L.lbm2d_get_info(self.h, C.byref(i)))
         return i
 
@@ -396,7 +398,6 @@ class Solver:
 
     def upload_f_ptr(self, host_ptr: int):
         """Upload populations from a host pointer (e.g. pinned memory)."""
-        self._sync_mask()
         self._ck(self.L.lbm2d_upload_f(self.h, C.cast(host_ptr, _DP)))
 
     def download_f_ptr(self, host_ptr: int):

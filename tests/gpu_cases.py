@@ -23,7 +23,7 @@ def gpu_solver(lbm2d, O, spec, storage="fp32"):
     s.close()
     g = lbm2d.Solver(spec["nx"], spec["ny"], spec["case"], spec.get("collision", 0), spec.get("les", False),
                      spec.get("cs", 0.12), storage)
-    g.obstacle[:] = mask
+    g.set_mask(mask)
     for op in spec["geometry"]:  # bb_geom keeps the last circle / polygon
         if op[0] == "cylinder":
             g.set_bb_cylinder(*op[1:])
