@@ -247,6 +247,264 @@ def run_reference(args):
     return 0
 
 
+# --------------------------------------------------------------------------- batch / serving
+def _c4_instances(n=256, seed=7):
+    """256 uneven solves: sides log-uniform in [64, 1024], aspect 1-3, case in
+    {cavity, step, cylinder}, Re ~ U[50, 1000] with u = 0.1, 30% heated
+    cavities (Pr 0.71, Ra <= 1e5)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        side = int(np.exp(rng.uniform(np.log(64), np.log(1024))))
+        aspect = rng.uniform(1.0, 3.0)
+        if rng.random() < 0.3:
+            out.append(dict(nx=side, ny=side, geometry=4, re=0.0, param=float(10 ** rng.uniform(3, 5))))
+            continue
+        geom = int(rng.integers(0, 3))
+        nx, ny = (side, side) if geom == 0 else (int(side * aspect), side)
+        out.append(dict(nx=max(nx, 16), ny=max(ny, 16), geometry=geom, re=float(rng.uniform(50, 1000)), param=0.0))
+    return out
+
+
+def _c5_requests(n, seed=11):
+    """Serving stream: grids 128x64 .. 2048x768 (log-uniform), geometry in
+    {cavity, step h=H/3, cylinder D=H/5, side-by-side S/D in [2,5]},
+    Re ~ U[50, 2000], budgets log-uniform in [1k, 50k] steps."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        t = rng.uniform(0, 1)
+        nx = int(np.exp(np.log(128) + t * (np.log(2048) - np.log(128))))
+        ny = int(np.exp(np.log(64) + t * (np.log(768) - np.log(64))))
+        geom = int(rng.integers(0, 4))
+        if geom == 0:
+            ny = nx = max(64, int(np.sqrt(nx * ny)))
+        out.append(dict(nx=nx, ny=ny, geometry=geom, re=float(rng.uniform(50, 2000)),
+                        param=float(rng.uniform(2, 5)) if geom == 3 else 0.0,
+                        steps=int(np.exp(rng.uniform(np.log(1000), np.log(50000))))))
+    return out
+
+
+def run_serve(args):
+    """Poisson arrivals (rate --rate) of --requests solves through the serving
+    loop, against the same requests solved one at a time with the plain
+    per-solve API (lbm2d_step) on the same GPU."""
+    import lbm2d
+    lbm2d.build(quiet=True)
+    reqs = _c5_requests(args.requests)
+    scale = args.budget_scale  # scales every step budget (bounded run time)
+    for r in reqs:
+        r["steps"] = max(100, int(r["steps"] * scale))
+    rng = np.random.default_rng(5)
+    gaps = rng.exponential(1.0 / args.rate, len(reqs))
+    storage = args.serve_storage
+    # --- serving loop
+    srv = lbm2d.Server(0, budget_bytes=args.serve_budget_gb * (1 << 30), max_active=args.max_active,
+                       steps_per_tick=args.tick)
+    t0 = time.perf_counter()
+    next_t = t0
+    for r, gap in zip(reqs, gaps):
+        next_t += gap
+        while time.perf_counter() < next_t:
+            time.sleep(min(0.001, max(0.0, next_t - time.perf_counter())))
+        srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"])
+    srv.wait(len(reqs), timeout_s=3600)
+    t_end = time.perf_counter()
+    res = srv.results()
+    st = srv.stats()
+    srv.close()
+    lat = np.array([x["t_done"] - x["t_submit"] for x in res])
+    lu = sum(x["steps"] * x["nodes"] for x in res)
+    span = max(x["t_done"] for x in res) - min(x["t_submit"] for x in res)
+    serve = {"requests": len(res), "failed": int(sum(1 for x in res if x["status"] != 0)),
+             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+             "mean_s": float(lat.mean()), "makespan_s": span, "glups": lu / span / 1e9,
+             "busy_glups": st["lattice_updates"] / max(st["busy_s"], 1e-9) / 1e9, "lattice_updates": lu}
+    # --- sequential plain solves (one solve per launch sequence, FIFO, same arrivals)
+    seq = None
+    if not args.no_sequential:
+        import torch  # noqa: F401  (CUDA context for timing parity)
+        arrivals = np.cumsum(gaps)
+        clock = 0.0
+        lat_s = []
+        lu_s = 0
+        wall0 = time.perf_counter()
+        for r, at in zip(reqs, arrivals):
+            start = max(clock, at)
+            ts = time.perf_counter()
+            s = _plain_solver(lbm2d, r, storage)
+            s.step(s._tau, s._ubc, r["steps"])
+            s.synchronize()
+            s.close()
+            dt = time.perf_counter() - ts
+            clock = start + dt
+            lat_s.append(clock - at)
+            lu_s += r["steps"] * r["nx"] * r["ny"]
+        busy = time.perf_counter() - wall0
+        lat_s = np.array(lat_s)
+        seq = {"p50_s": float(np.percentile(lat_s, 50)), "p99_s": float(np.percentile(lat_s, 99)),
+               "makespan_s": clock, "glups": lu_s / clock / 1e9, "busy_glups": lu_s / busy / 1e9,
+               "note": "same requests and arrival times, solved one at a time with lbm2d_step (FIFO)"}
+    line = {"metric": "serving: p50/p99 time-to-solution and aggregate GLUPS", "unit": "GLUPS",
+            "value": serve["glups"], "serve": serve, "sequential": seq,
+            "speedup_vs_sequential": (serve["glups"] / seq["glups"]) if seq else None,
+            "config": {"workload": f"{len(reqs)} requests, Poisson {args.rate}/s, grids 128x64..2048x768, "
+                                   f"{{cavity, step, cylinder, side-by-side}}, Re 50-2000, budgets 1k-50k x {scale}",
+                       "storage": storage, "tick": args.tick, "budget_gb": args.serve_budget_gb}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _plain_solver(lbm2d, r, storage):
+    """One request set up through the plain per-solve API, as the serving loop
+    sets it up (same geometry rules)."""
+    nx, ny, geom = r["nx"], r["ny"], r["geometry"]
+    u = 0.1
+    mask = np.zeros(nx * ny, np.uint8)
+    L = lbm2d.lib()
+    bb = None
+    thermal = geom == 4
+    if geom == 0:
+        case, Lc = lbm2d.CAVITY, nx
+        L.lbm2d_mask_walls(nx, ny, lbm2d._u8(mask))
+    elif geom == 1:
+        case = lbm2d.STEP
+        hs = ny // 3
+        m = mask.reshape(ny, nx)
+        m[0, :] = 1
+        m[ny - 1, :] = 1
+        m[:hs, : nx // 4] = 1
+        Lc = 2.0 * (ny - 1 - hs)
+    elif geom == 2:
+        case, Lc = lbm2d.CYLINDER, ny / 5.0
+        bb = (nx // 4, ny // 2 + 1, ny // 10)
+        L.lbm2d_mask_cylinder(nx, ny, lbm2d._u8(mask), *bb)
+    elif geom == 3:
+        case = lbm2d.SIDE_BY_SIDE
+        rad = ny // 10
+        D = 2 * rad
+        sp = int((r["param"] or 3.0) * D)
+        cy1 = ny // 2 - sp // 2
+        L.lbm2d_mask_cylinder(nx, ny, lbm2d._u8(mask), nx // 4, cy1, rad)
+        L.lbm2d_mask_cylinder(nx, ny, lbm2d._u8(mask), nx // 4, cy1 + sp, rad)
+        bb = (nx // 4, cy1 + sp, rad)
+        Lc = D
+    else:
+        case = lbm2d.CYLINDER
+        m = mask.reshape(ny, nx)
+        m[:, 0] = m[:, -1] = 1
+        m[0, :] = m[-1, :] = 1
+        Lc = None
+    tau = 0.8 if thermal else 0.5 + 3.0 * (u * Lc / r["re"])
+    s = lbm2d.Solver(nx, ny, case, lbm2d.MRT, tau < 0.55, 0.12, storage)
+    s.set_mask(mask)
+    if bb:
+        s.set_bb_cylinder(*bb)
+    ubc = u
+    if thermal:
+        Pr, Th, Tc = 0.71, 1.5, 0.5
+        nu = (tau - 0.5) / 3.0
+        alpha = nu / Pr
+        gb = (r["param"] or 1e4) * nu * alpha / ((Th - Tc) * ny ** 3)
+        s.set_thermal(True, 1.0, alpha, 1.0 / (0.5 + 3.0 * alpha), 0.001, -gb / 0.001)
+        s.set_thermal_hook(lbm2d.HOOK_HEATED_CAVITY, Th, Tc)
+        ubc = 0.0
+    s.init_equilibrium(1.0, u if geom in (2, 3) else 0.0, 0.0, 1.0)
+    s._tau, s._ubc = tau, ubc
+    return s
+
+
+def run_batch(args):
+    """256 uneven solves stepped together (one packed launch per step per
+    storage group) against the same solves stepped one after another."""
+    import torch
+
+    import lbm2d
+    lbm2d.build(quiet=True)
+    inst = _c4_instances(args.instances)
+    steps = args.steps
+    storage = args.batch_storage
+    solvers = [_plain_solver(lbm2d, r, storage) for r in inst]
+    nodes = sum(r["nx"] * r["ny"] for r in inst)
+    # sequential: each solver alone, one after the other
+    for s in solvers:
+        s.step(s._tau, s._ubc, 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.step(s._tau, s._ubc, steps)
+    for s in solvers:
+        s.synchronize()
+    t_seq = time.perf_counter() - t0
+    # batched
+    b = lbm2d.Batch()
+    for s in solvers:
+        b.add(s, s._tau, s._ubc)
+    if args.autotune:
+        bx, by = b.autotune(5)
+    b.step(2)
+    b.synchronize()
+    t0 = time.perf_counter()
+    l0 = b.launches
+    b.step(steps)
+    b.synchronize()
+    t_bat = time.perf_counter() - t0
+    nan = 0
+    for s in solvers:
+        try:
+            s.synchronize()
+        except lbm2d.LBMError:
+            nan += 1
+    line = {"metric": "batched uneven solves: aggregate GLUPS", "unit": "GLUPS",
+            "value": nodes * steps / t_bat / 1e9, "sequential_glups": nodes * steps / t_seq / 1e9,
+            "speedup_vs_sequential": t_seq / t_bat, "steps": steps, "instances": len(inst), "nodes": nodes,
+            "batch_launches": b.launches - l0, "diverged": nan,
+            "thermal_instances": sum(1 for r in inst if r["geometry"] == 4),
+            "config": {"workload": "256 uneven cavity/step/cylinder solves, sides log-uniform 64-1024, aspect 1-3, "
+                                   "Re U[50,1000], u=0.1, 30% heated cavities (Pr 0.71, Ra<=1e5)",
+                       "storage": storage, "block": [b.L and 0, 0]}}
+    b.close()
+    for s in solvers:
+        s.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_precision(args):
+    """Error of FP32 / FP16 / BF16 storage against an FP64 run of the same
+    kernel on the channel workload: relative L2 of the velocity field over
+    fluid nodes and relative error of the mean drag over the run."""
+    import lbm2d
+    lbm2d.build(quiet=True)
+    nx, ny, steps = args.nx, args.ny, args.steps
+    mask, circles = make_geometry(nx, ny)
+    fluid = mask == 0
+    out = {}
+    ref = None
+    for st in ("fp64", "fp32", "fp16", "bf16"):
+        s = configure(lbm2d, st, mask, circles, 0, nx, ny, True)
+        s.init_equilibrium(1.0, U0, 0.0)
+        s.step(TAU, U0, steps)
+        s.synchronize()
+        rho, u, v = s.macros()
+        fx, fy = s.force_history()
+        s.close()
+        if ref is None:
+            ref = (u, v, fx, fy)
+            out[st] = {"steps": steps}
+            continue
+        du = np.sqrt(np.sum((u - ref[0])[fluid] ** 2 + (v - ref[1])[fluid] ** 2) /
+                     np.sum(ref[0][fluid] ** 2 + ref[1][fluid] ** 2))
+        drag_ref = float(np.mean(ref[2][steps // 2:]))
+        drag = float(np.mean(fx[steps // 2:]))
+        out[st] = {"velocity_rel_l2": float(du), "drag_rel_err": abs(drag - drag_ref) / abs(drag_ref),
+                   "drag": drag, "drag_fp64": drag_ref}
+    line = {"metric": "storage precision vs FP64 (same kernel)", "config": {"workload": workload_name(nx, ny),
+            "steps": steps}, "results": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -262,22 +520,36 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (default: --steps)")
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "precision"])
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--batch-storage", default="fp32")
+    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--budget-scale", type=float, default=0.1)
+    ap.add_argument("--serve-storage", default="fp16")
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--max-active", type=int, default=512)
+    ap.add_argument("--tick", type=int, default=200)
+    ap.add_argument("--no-sequential", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "batch":
+        return run_batch(args)
+    if args.mode == "serve":
+        return run_serve(args)
+    if args.mode == "precision":
+        return run_precision(args)
 
     import torch
 
     import lbm2d
     lbm2d.build(quiet=True)
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:  # independent replicas, one per GPU: no data-path collective
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+    from lbm2d.replicas import Replicas
+    reps = Replicas()  # independent replicas, one per GPU: no data-path collective
+    rank, world, local = reps.rank, reps.size, reps.local
     torch.cuda.set_device(local)
 
     nx, ny = args.nx, args.ny
@@ -291,8 +563,7 @@ def main():
     for label, storage, les in runs:
         s = configure(lbm2d, storage, mask, circles, local, nx, ny, les)
         s.upload_f(f0)
-        if dist:
-            dist.barrier()
+        reps.barrier()
         clocks.active = True
         try:
             ms, kms, launches = time_device(s, torch, args.steps, args.warmup)
@@ -302,11 +573,9 @@ def main():
                 raise
             ms, kms, launches, nan = float("nan"), float("nan"), 0, True
         clocks.active = False
-        t = torch.tensor([ms], dtype=torch.float64)
-        if dist:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = reps.max(ms)
         info = s.info()
-        results[label] = dict(ms=float(t[0]), kernel_ms=kms, launches=launches, nan=nan,
+        results[label] = dict(ms=ms, kernel_ms=kms, launches=launches, nan=nan,
                                 bytes_per_update=info.bytes_per_update, boundary=info.n_boundary_nodes,
                                 force_nodes=info.n_force_nodes, block=(info.block_x, info.block_y))
         if label == storages[0] and not nan:
@@ -320,20 +589,17 @@ def main():
             s.upload_f(f0)
             s.step(TAU, U0, args.warmup)
             s.synchronize()
-            if dist:
-                dist.barrier()
+            reps.barrier()
             clocks.active = True
             e2e_ms, e2e_launches = time_e2e(lbm2d, s, torch, e2e_steps, pin, pout)
             clocks.active = False
-            t = torch.tensor([e2e_ms], dtype=torch.float64)
-            if dist:
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            results["e2e"] = dict(ms=float(t[0]), steps=e2e_steps, launches=e2e_launches)
+            results["e2e"] = dict(ms=reps.max(e2e_ms), steps=e2e_steps, launches=e2e_launches)
             del pin, pout
         s.close()
     clocks.stop()
 
     if rank != 0:
+        reps.close()
         return 0
     nodes = nx * ny
     peak, peak_kind = peaks()
@@ -394,8 +660,7 @@ def main():
         "drag_lift": r0.get("force"),
     }
     print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    reps.close()
     return 0
 
 

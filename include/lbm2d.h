@@ -146,6 +146,13 @@ int lbm2d_set_thermal_hook(lbm2d_solver *h, int kind, double Ta, double Tb);
 int lbm2d_upload_f(lbm2d_solver *h, const double *f);
 int lbm2d_upload_g(lbm2d_solver *h, const double *g);
 
+/* Uniform equilibrium state on the device, without a host transfer: the
+ * drivers' initialisation loops, f_i = compute_equilibrium(i, rho, u, v)
+ * (src/lbm_types.hpp:269-273) and g_i = thermal_equilibrium(i, T, u, v)
+ * (src/thermal.hpp:25-30) at every node, e.g. src/cavity.cpp:79-84,
+ * src/thermal_cavity.cpp:118-129. */
+int lbm2d_init_equilibrium(lbm2d_solver *h, double rho, double u, double v, double T);
+
 /* One or more calls of execute_time_step(sys, tau, u_inflow)
  * (src/lbm.hpp:293-582).  Asynchronous. */
 int lbm2d_step(lbm2d_solver *h, double tau, double u_inflow, int nsteps);
@@ -195,6 +202,85 @@ int lbm2d_profile(lbm2d_solver *h, double *step_kernel_ms, long long *n_launches
 int lbm2d_upload_f_device(lbm2d_solver *h, const double *d_f);
 int lbm2d_download_f_device(lbm2d_solver *h, double *d_f);
 
+
+/* ---- batching: many independent solves in one launch.
+ * The reference steps one LBMCapabilities per process (its globals allow no
+ * more); these entry points have no counterpart there.  A batch steps every
+ * member with one packed launch per storage/thermal group: a
+ * tile-to-instance table maps each launch block to (member, block of that
+ * member's grid).  Repeated step pairs are replayed from a captured CUDA
+ * graph.  Members keep their own state, geometry, forces and history; their
+ * own streams are ordered after the batch's work, so lbm2d_download_* on a
+ * member sees the batched steps. */
+typedef struct lbm2d_batch lbm2d_batch;
+int lbm2d_batch_create(int device, lbm2d_batch **out);
+int lbm2d_batch_destroy(lbm2d_batch *b);
+const char *lbm2d_batch_last_error(const lbm2d_batch *b);
+/* Add / remove a member; (tau, u_inflow) are the arguments of its
+ * execute_time_step calls while in the batch. */
+int lbm2d_batch_add(lbm2d_batch *b, lbm2d_solver *h, double tau, double u_inflow);
+int lbm2d_batch_remove(lbm2d_batch *b, lbm2d_solver *h);
+int lbm2d_batch_set_params(lbm2d_batch *b, lbm2d_solver *h, double tau, double u_inflow);
+int lbm2d_batch_size(lbm2d_batch *b);
+/* Step every member nsteps times (asynchronous on the batch stream). */
+int lbm2d_batch_step(lbm2d_batch *b, int nsteps);
+int lbm2d_batch_synchronize(lbm2d_batch *b);
+/* Launch shape shared by the members (multiple of 32 threads, <= 512). */
+int lbm2d_batch_set_block(lbm2d_batch *b, int bx, int by);
+void *lbm2d_batch_stream(lbm2d_batch *b);
+long long lbm2d_batch_launch_count(lbm2d_batch *b);
+
+/* ---- serving loop: requests of different grid sizes, geometries, Reynolds
+ * numbers and step budgets arrive at any time; a worker thread admits them
+ * by device-memory footprint, steps all active solves together through a
+ * batch (one packed launch per step per storage group) and retires each one
+ * exactly at its budget.  No counterpart in the reference (one solve per
+ * process there). */
+#define LBM2D_GEOM_CAVITY 0        /* lid-driven cavity, src/cavity.cpp */
+#define LBM2D_GEOM_STEP 1          /* backward-facing step h = NY/3, src/step.cpp */
+#define LBM2D_GEOM_CYLINDER 2      /* cylinder D = NY/5, src/main.cpp */
+#define LBM2D_GEOM_SIDE_BY_SIDE 3  /* two cylinders D = NY/5, S/D = param */
+#define LBM2D_GEOM_HEATED_CAVITY 4 /* differentially heated cavity, Ra = param, src/thermal_cavity.cpp */
+
+typedef struct lbm2d_request {
+    int nx, ny;
+    int geometry;   /* LBM2D_GEOM_* */
+    double re;      /* Reynolds number (tau = 0.5 + 3 u L / Re; LES when tau < 0.55) */
+    double param;   /* S/D for side-by-side cylinders, Ra for the heated cavity */
+    double u;       /* lid / inlet velocity (default 0.1) */
+    int steps;      /* step budget */
+    int storage;    /* LBM2D_STORE_* */
+} lbm2d_request;
+
+typedef struct lbm2d_result {
+    long long id;
+    int status;                     /* LBM2D_OK, LBM2D_ERR_NAN, ... */
+    double t_submit, t_admit, t_done; /* seconds, steady clock */
+    long long steps, nodes;
+    double fx, fy;                  /* final drag / lift sums */
+} lbm2d_result;
+
+typedef struct lbm2d_server_stats_t {
+    long long submitted, finished, queued, active;
+    double busy_s;                  /* wall time the worker spent stepping */
+    long long lattice_updates;
+    double device_bytes_in_use;
+} lbm2d_server_stats_t;
+
+typedef struct lbm2d_server lbm2d_server;
+int lbm2d_server_create(int device, double budget_bytes, int max_active, int steps_per_tick, lbm2d_server **out);
+int lbm2d_server_submit(lbm2d_server *s, const lbm2d_request *r, long long *id);
+/* Block until at least n_finished requests are done (or timeout). */
+int lbm2d_server_wait(lbm2d_server *s, long long n_finished, double timeout_s);
+int lbm2d_server_results(lbm2d_server *s, lbm2d_result *out, int capacity, int *count);
+int lbm2d_server_stats(lbm2d_server *s, lbm2d_server_stats_t *stats);
+int lbm2d_server_destroy(lbm2d_server *s);
+
+/* ---- launch-shape autotuner: times `steps` steps for each candidate block
+ * shape (the state is saved before and restored after), keeps the fastest
+ * and returns it.  No counterpart in the reference. */
+int lbm2d_autotune(lbm2d_solver *h, int steps, double tau, double u_inflow, int *best_bx, int *best_by);
+int lbm2d_batch_autotune(lbm2d_batch *b, int steps, int *best_bx, int *best_by);
 
 /* ---- host services (no device needed): the reference's set-up arithmetic,
  *      shared by the C++ drop-in headers and the Python binding so masks and

@@ -1,0 +1,483 @@
+// lbm2d_batch.cpp -- many independent solves in one launch, CUDA-graph
+// replay, and the launch-shape autotuner.
+//
+// A batch owns a stream.  Each call of lbm2d_batch_step
+//   1. prepares every member on its own stream (re-collision after a
+//      parameter change, geometry and force-slot upload, prologue) and makes
+//      the batch stream wait for it,
+//   2. writes the kernel parameters of the next two steps of every member
+//      (ping-pong parity 0 and 1) and the tile-to-instance table (first
+//      launch block of every member) into device arrays,
+//   3. launches, per (storage, thermal) group, one batch_step_kernel that
+//      covers every member's blocks, followed by one batched force reduction,
+//      replaying step pairs from a captured CUDA graph,
+//   4. advances every member's state and orders the members' streams after
+//      the batch stream.
+#include <algorithm>
+#include <chrono>
+#include <map>
+
+#include "lbm2d_runtime.h"
+
+using namespace lbm2d;
+using namespace lbm2d::rt;
+
+namespace {
+struct Member {
+    lbm2d_solver* h;
+    double tau, u;
+};
+
+struct Group {
+    int storage = 0, thermal = 0;
+    std::vector<int> members;  // indices into lbm2d_batch::members
+    int nblocks = 0;
+    int njobs = 0;
+    KParams* d_params[2] = {nullptr, nullptr};
+    int* d_block_start = nullptr;
+    ReduceJob* d_jobs = nullptr;
+    size_t cap_members = 0;
+};
+}  // namespace
+
+struct lbm2d_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;
+    std::vector<Member> members;
+    std::vector<Group> groups;
+    bool layout_dirty = true;
+    int bx = 128, by = 2;
+    // host staging (pinned) for parameters
+    KParams* h_params = nullptr;
+    size_t h_params_cap = 0;
+    // captured step pair
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    long long launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int bfail(lbm2d_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+#define BCK(expr, what)                                                                          \
+    do {                                                                                         \
+        cudaError_t e_ = (expr);                                                                 \
+        if (e_ != cudaSuccess) return bfail(b, LBM2D_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+void free_groups(lbm2d_batch* b) {
+    for (auto& g : b->groups) {
+        cudaFree(g.d_params[0]);
+        cudaFree(g.d_params[1]);
+        cudaFree(g.d_block_start);
+        cudaFree(g.d_jobs);
+    }
+    b->groups.clear();
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_valid = false;
+}
+
+int member_index(lbm2d_batch* b, lbm2d_solver* h) {
+    for (size_t k = 0; k < b->members.size(); ++k)
+        if (b->members[k].h == h) return (int)k;
+    return -1;
+}
+
+// (Re)build the groups and their device arrays.
+int build_layout(lbm2d_batch* b) {
+    if (!b->layout_dirty) return LBM2D_OK;
+    free_groups(b);
+    std::map<std::pair<int, int>, int> gi;
+    for (size_t k = 0; k < b->members.size(); ++k) {
+        lbm2d_solver* h = b->members[k].h;
+        const auto key = std::make_pair(h->storage, h->thermal ? 1 : 0);
+        auto it = gi.find(key);
+        if (it == gi.end()) {
+            gi[key] = (int)b->groups.size();
+            Group g;
+            g.storage = key.first;
+            g.thermal = key.second;
+            b->groups.push_back(g);
+            it = gi.find(key);
+        }
+        b->groups[it->second].members.push_back((int)k);
+    }
+    for (auto& g : b->groups) {
+        const size_t m = g.members.size();
+        BCK(cudaMalloc(&g.d_params[0], m * sizeof(KParams)), "batch params");
+        BCK(cudaMalloc(&g.d_params[1], m * sizeof(KParams)), "batch params");
+        BCK(cudaMalloc(&g.d_block_start, (m + 1) * sizeof(int)), "batch table");
+        BCK(cudaMalloc(&g.d_jobs, m * sizeof(ReduceJob)), "batch jobs");
+        g.cap_members = m;
+    }
+    b->layout_dirty = false;
+    return LBM2D_OK;
+}
+
+int ensure_host_params(lbm2d_batch* b, size_t n) {
+    if (n <= b->h_params_cap) return LBM2D_OK;
+    if (b->h_params) cudaFreeHost(b->h_params);
+    b->h_params = nullptr;
+    BCK(cudaMallocHost(&b->h_params, n * sizeof(KParams)), "pinned params");
+    b->h_params_cap = n;
+    return LBM2D_OK;
+}
+
+// Steps 1-2 of the file comment; fills every group's device arrays.
+int prepare(lbm2d_batch* b) {
+    int rc;
+    if ((rc = build_layout(b))) return rc;
+    size_t total = 0;
+    for (auto& g : b->groups) total += 2 * g.members.size();
+    if ((rc = ensure_host_params(b, std::max<size_t>(total, 1)))) return rc;
+    size_t off = 0;
+    for (auto& g : b->groups) {
+        const size_t m = g.members.size();
+        KParams* p0 = b->h_params + off;
+        KParams* p1 = p0 + m;
+        std::vector<int> start(m + 1, 0);
+        std::vector<ReduceJob> jobs;
+        for (size_t k = 0; k < m; ++k) {
+            Member& mem = b->members[g.members[k]];
+            lbm2d_solver* h = mem.h;
+            if ((rc = check_handle(h))) return bfail(b, rc, std::string("member: ") + h->err);
+            if (h->bx != b->bx || h->by != b->by) {
+                h->bx = b->bx;
+                h->by = b->by;
+            }
+            KParams p;
+            if ((rc = prepare_steps(h, mem.tau, mem.u, p))) return bfail(b, rc, std::string("member: ") + h->err);
+            p0[k] = p;
+            p1[k] = p;
+            p1[k].fin = p.fout;
+            p1[k].fout = const_cast<void*>(p.fin);
+            p1[k].gin = p.gout;
+            p1[k].gout = const_cast<void*>(p.gin);
+            // order the batch stream after the member's own preparation
+            BCK(cudaEventRecord(b->ev, h->stream), "event");
+            BCK(cudaStreamWaitEvent(b->stream, b->ev, 0), "wait");
+            const int gy = (h->ny + b->by - 1) / b->by;
+            start[k + 1] = start[k] + p.gx * gy;
+            if (h->nslots > 0)
+                jobs.push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last});
+        }
+        g.nblocks = start[m];
+        g.njobs = (int)jobs.size();
+        BCK(cudaMemcpyAsync(g.d_params[0], p0, m * sizeof(KParams), cudaMemcpyHostToDevice, b->stream), "params");
+        BCK(cudaMemcpyAsync(g.d_params[1], p1, m * sizeof(KParams), cudaMemcpyHostToDevice, b->stream), "params");
+        BCK(cudaMemcpyAsync(g.d_block_start, start.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice, b->stream),
+            "table");
+        if (!jobs.empty())
+            BCK(cudaMemcpyAsync(g.d_jobs, jobs.data(), jobs.size() * sizeof(ReduceJob), cudaMemcpyHostToDevice,
+                                b->stream),
+                "jobs");
+        off += 2 * m;
+    }
+    // the staging buffers may be rewritten by the next call: wait for the copies
+    BCK(cudaStreamSynchronize(b->stream), "params sync");
+    return LBM2D_OK;
+}
+
+int launch_one(lbm2d_batch* b, int parity) {
+    for (auto& g : b->groups) {
+        int e = launch_batch_step(g.storage, g.d_params[parity], g.d_block_start, (int)g.members.size(), g.nblocks,
+                                  g.thermal, b->bx, b->by, b->stream);
+        ++b->launches;
+        if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
+        if (g.njobs > 0) {
+            e = launch_batch_force_reduce(g.d_jobs, g.njobs, b->stream);
+            ++b->launches;
+            if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch reduce: ") + cudaGetErrorString((cudaError_t)e));
+        }
+    }
+    return LBM2D_OK;
+}
+
+int capture_pair(lbm2d_batch* b) {
+    if (b->graph_valid) return LBM2D_OK;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const long long l0 = b->launches;
+    int rc = launch_one(b, 0);
+    if (!rc) rc = launch_one(b, 1);
+    b->launches = l0;  // captured launches are counted when replayed
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return bfail(b, LBM2D_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(b, LBM2D_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    b->graph_valid = true;
+    return LBM2D_OK;
+}
+
+long long launches_per_step(const lbm2d_batch* b) {
+    long long n = 0;
+    for (auto& g : b->groups) n += 1 + (g.njobs > 0 ? 1 : 0);
+    return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm2d_batch_create(int device, lbm2d_batch** out) {
+    if (!out) return LBM2D_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return LBM2D_ERR_NO_DEVICE;
+    }
+    auto* b = new lbm2d_batch();
+    b->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+        delete b;
+        return LBM2D_ERR_CUDA;
+    }
+    *out = b;
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_destroy(lbm2d_batch* b) {
+    if (!b) return LBM2D_OK;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    free_groups(b);
+    if (b->h_params) cudaFreeHost(b->h_params);
+    cudaEventDestroy(b->ev);
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return LBM2D_OK;
+}
+
+const char* lbm2d_batch_last_error(const lbm2d_batch* b) { return b ? b->err.c_str() : ""; }
+
+int lbm2d_batch_add(lbm2d_batch* b, lbm2d_solver* h, double tau, double u) {
+    if (!b || !h) return LBM2D_ERR_INVALID;
+    if (h->device != b->device) return bfail(b, LBM2D_ERR_INVALID, "member lives on another device");
+    if (!(tau > 0.0)) return bfail(b, LBM2D_ERR_INVALID, "tau must be positive");
+    if (member_index(b, h) >= 0) return bfail(b, LBM2D_ERR_INVALID, "already a member");
+    b->members.push_back({h, tau, u});
+    b->layout_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_remove(lbm2d_batch* b, lbm2d_solver* h) {
+    if (!b || !h) return LBM2D_ERR_INVALID;
+    const int k = member_index(b, h);
+    if (k < 0) return bfail(b, LBM2D_ERR_INVALID, "not a member");
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);  // no batched work may still touch h
+    b->members.erase(b->members.begin() + k);
+    b->layout_dirty = true;
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_set_params(lbm2d_batch* b, lbm2d_solver* h, double tau, double u) {
+    if (!b || !h) return LBM2D_ERR_INVALID;
+    const int k = member_index(b, h);
+    if (k < 0) return bfail(b, LBM2D_ERR_INVALID, "not a member");
+    if (!(tau > 0.0)) return bfail(b, LBM2D_ERR_INVALID, "tau must be positive");
+    b->members[k].tau = tau;
+    b->members[k].u = u;
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_size(lbm2d_batch* b) { return b ? (int)b->members.size() : 0; }
+
+int lbm2d_batch_step(lbm2d_batch* b, int nsteps) {
+    if (!b || nsteps < 0) return LBM2D_ERR_INVALID;
+    if (nsteps == 0 || b->members.empty()) return LBM2D_OK;
+    if (cudaSetDevice(b->device) != cudaSuccess) return LBM2D_ERR_CUDA;
+    const bool relayout = b->layout_dirty;
+    int rc = prepare(b);
+    if (rc) return rc;
+    if (relayout) b->graph_valid = false;
+    const int pairs = nsteps / 2;
+    if (pairs > 0) {
+        if ((rc = capture_pair(b))) return rc;
+        for (int k = 0; k < pairs; ++k) {
+            BCK(cudaGraphLaunch(b->graph, b->stream), "graph launch");
+            b->launches += 2 * launches_per_step(b);
+        }
+    }
+    if (nsteps & 1) {
+        if ((rc = launch_one(b, 0))) return rc;
+    }
+    for (auto& m : b->members) {
+        lbm2d_solver* h = m.h;
+        h->cur ^= (nsteps & 1);
+        h->steps_since_collide += nsteps;
+        h->steps_done += nsteps;
+        h->u_last = m.u;
+    }
+    BCK(cudaEventRecord(b->ev, b->stream), "event");
+    for (auto& m : b->members) BCK(cudaStreamWaitEvent(m.h->stream, b->ev, 0), "member wait");
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_synchronize(lbm2d_batch* b) {
+    if (!b) return LBM2D_ERR_INVALID;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->stream), "batch sync");
+    for (auto& m : b->members) {
+        int rc = lbm2d_synchronize(m.h);
+        if (rc) return bfail(b, rc, std::string("member: ") + m.h->err);
+    }
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_set_block(lbm2d_batch* b, int bx, int by) {
+    if (!b) return LBM2D_ERR_INVALID;
+    if (bx == 0 && by == 0) {
+        bx = 128;
+        by = 2;
+    }
+    if (bx <= 0 || by <= 0 || bx * by > 512 || (bx * by) % 32 != 0)
+        return bfail(b, LBM2D_ERR_INVALID, "block must have a multiple of 32 threads, at most 512");
+    if (bx != b->bx || by != b->by) {
+        b->bx = bx;
+        b->by = by;
+        b->layout_dirty = true;
+    }
+    return LBM2D_OK;
+}
+
+void* lbm2d_batch_stream(lbm2d_batch* b) { return b ? (void*)b->stream : nullptr; }
+long long lbm2d_batch_launch_count(lbm2d_batch* b) { return b ? b->launches : 0; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- autotuner
+namespace {
+const int kShapes[][2] = {{32, 4}, {32, 8}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {128, 4}, {256, 1}, {256, 2},
+                          {512, 1}, {32, 16}, {64, 8}};
+
+// Save a member's state (rebuild S into staging) so tuning steps can be undone.
+int save_state(lbm2d_solver* h, unsigned long long& counter) {
+    int rc;
+    if ((rc = materialize(h))) return rc;
+    // the handle's stream is non-blocking: read the counter on it, after its work
+    if (cudaMemcpyAsync(&counter, h->d_counter, sizeof(counter), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return LBM2D_ERR_CUDA;
+    return LBM2D_OK;
+}
+
+int restore_state(lbm2d_solver* h, unsigned long long counter, long long steps_done) {
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return LBM2D_ERR_CUDA;
+    h->staged = true;  // staging still holds the saved S; the next step re-collides it
+    h->steps_done = steps_done;
+    if (cudaMemcpyAsync(h->d_counter, &counter, sizeof(counter), cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return LBM2D_ERR_CUDA;
+    return LBM2D_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int lbm2d_autotune(lbm2d_solver* h, int steps, double tau, double u, int* best_bx, int* best_by) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (steps < 1) steps = 1;
+    unsigned long long counter = 0;
+    const long long done = h->steps_done;
+    if ((rc = save_state(h, counter))) return rc;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bbx = h->bx, bby = h->by;
+    for (auto& s : kShapes) {
+        if (s[0] > 2 * h->nx && s[0] > 32) continue;
+        h->bx = s[0];
+        h->by = s[1];
+        h->staged = true;
+        if ((rc = lbm2d_step(h, tau, u, 2))) break;  // prologue + warm-up
+        cudaEventRecord(e0, h->stream);
+        if ((rc = lbm2d_step(h, tau, u, steps))) break;
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            bbx = s[0];
+            bby = s[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->bx = bbx;
+    h->by = bby;
+    const int rc2 = restore_state(h, counter, done);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (best_bx) *best_bx = bbx;
+    if (best_by) *best_by = bby;
+    return LBM2D_OK;
+}
+
+int lbm2d_batch_autotune(lbm2d_batch* b, int steps, int* best_bx, int* best_by) {
+    if (!b) return LBM2D_ERR_INVALID;
+    if (b->members.empty()) return LBM2D_OK;
+    if (steps < 1) steps = 1;
+    cudaSetDevice(b->device);
+    std::vector<unsigned long long> counters(b->members.size());
+    std::vector<long long> done(b->members.size());
+    int rc;
+    for (size_t k = 0; k < b->members.size(); ++k) {
+        done[k] = b->members[k].h->steps_done;
+        if ((rc = save_state(b->members[k].h, counters[k]))) return bfail(b, rc, "autotune save");
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bbx = b->bx, bby = b->by;
+    rc = LBM2D_OK;
+    for (auto& s : kShapes) {
+        if ((rc = lbm2d_batch_set_block(b, s[0], s[1]))) break;
+        for (auto& m : b->members) m.h->staged = true;
+        if ((rc = lbm2d_batch_step(b, 2))) break;
+        cudaEventRecord(e0, b->stream);
+        if ((rc = lbm2d_batch_step(b, steps))) break;
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            bbx = s[0];
+            bby = s[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    lbm2d_batch_set_block(b, bbx, bby);
+    for (size_t k = 0; k < b->members.size(); ++k) {
+        const int r2 = restore_state(b->members[k].h, counters[k], done[k]);
+        if (!rc && r2) rc = r2;
+    }
+    if (rc) return rc;
+    if (best_bx) *best_bx = bbx;
+    if (best_by) *best_by = bby;
+    return LBM2D_OK;
+}
+
+}  // extern "C"

@@ -20,98 +20,16 @@
 #include <string>
 #include <vector>
 
-#include "../../include/lbm2d.h"
-#include "lbm2d_geometry.h"
-#include "lbm2d_internal.h"
+#include "lbm2d_runtime.h"
 
 using namespace lbm2d;
 
 namespace {
 thread_local std::string g_global_err;
-
-constexpr double W[9] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0,
-                         1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
-constexpr int CASE_CAVITY = 1, CASE_STEP = 2, CASE_RIBS = 3, CASE_HILLS = 9;
-
-size_t elem_size(int storage) {
-    switch (storage) {
-        case ST_FP32: return 4;
-        case ST_FP16:
-        case ST_BF16: return 2;
-        case ST_FP64: return 8;
-    }
-    return 0;
-}
-
-struct CollideParams {
-    int collision = 0, les = 0, thermal = 0;
-    double s_shear = 0, s_bulk = 0, s_normal = 0, tau = 0, cs_sq = 0, nu = 0, Fscale = 0;
-    double omega_k = 0, beta = 0, g_buoy = 0, T_ref = 0;
-    bool operator==(const CollideParams& o) const {
-        return collision == o.collision && les == o.les && thermal == o.thermal && s_shear == o.s_shear &&
-               s_bulk == o.s_bulk && s_normal == o.s_normal && tau == o.tau && cs_sq == o.cs_sq && nu == o.nu &&
-               Fscale == o.Fscale && omega_k == o.omega_k && beta == o.beta && g_buoy == o.g_buoy &&
-               T_ref == o.T_ref;
-    }
-};
 }  // namespace
 
-struct lbm2d_solver {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int nx = 0, ny = 0;
-    size_t N = 0;
-    int case_type = 0, collision = 0, use_les = 0, storage = 0;
-    double cs = 0.12;
-    std::vector<uint8_t> mask;
-    BBGeometry bb;
-    double body_force = 0.0;
-    bool thermal = false;
-    double T_ref = 1.0, alpha = 0.1666666667, omega_k = 1.0, beta = 0.0, g_buoy = 0.0;
-    int hook = 0;
-    double hook_a = 0.0, hook_b = 0.0;
-
-    // device buffers
-    void* P[2] = {nullptr, nullptr};
-    void* G[2] = {nullptr, nullptr};
-    int cur = 0;
-    uint32_t* d_flags = nullptr;
-    uint32_t* d_rec_info = nullptr;
-    uint32_t* d_rec_force = nullptr;
-    double* d_rec_wd = nullptr;
-    double* d_rec_q = nullptr;
-    double* d_rec_uw = nullptr;
-    double* d_partials = nullptr;
-    int* d_block_slot = nullptr;
-    int nslots = 0, slot_bx = 0, slot_by = 0;
-    double* d_hist = nullptr;
-    int hist_cap = 1 << 18;
-    unsigned long long* d_counter = nullptr;
-    double* d_last = nullptr;
-    unsigned int* d_nan = nullptr;
-    double* d_stage_f = nullptr;
-    double* d_stage_g = nullptr;
-    double* d_fx = nullptr;
-    double* d_fy = nullptr;
-    size_t device_bytes = 0;
-
-    GeometryTables geo;
-    bool geom_dirty = true;
-    bool staged = true;  // STAGED (true) or COLLIDED (false)
-    bool stage_f_valid = false, stage_g_valid = false;  // staging holds S (else defaults)
-    CollideParams cp_of_P;
-    double u_last = 0.0;
-    long long steps_since_collide = 0;
-    long long steps_done = 0;
-    long long launches = 0;
-    int bx = 128, by = 2;
-    bool profiling = false;
-    std::vector<cudaEvent_t> ev_pool;  // even/odd = start/stop
-    size_t ev_used = 0;
-    std::string err;
-};
-
-namespace {
+namespace lbm2d {
+namespace rt {
 
 int fail(lbm2d_solver* h, int code, const std::string& msg) {
     if (h) h->err = msg;
@@ -415,7 +333,39 @@ int check_handle(lbm2d_solver* h) {
     return LBM2D_OK;
 }
 
-}  // namespace
+// Prepare a handle for steps with (tau, u): re-collide on parameter change,
+// push geometry, force slots and the prologue, then fill the kernel
+// parameters of the next step.
+int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p) {
+    int rc;
+    if (!(tau > 0.0)) return fail(h, LBM2D_ERR_INVALID, "tau must be positive");
+    const CollideParams c = collide_params(h, tau);
+    if (!h->staged && !(c == h->cp_of_P)) {
+        if ((rc = materialize(h))) return rc;
+    }
+    if ((rc = upload_geometry(h))) return rc;
+    if ((rc = ensure_slots(h))) return rc;
+    if (h->staged) {
+        if ((rc = prologue(h, c))) return rc;
+    }
+    p = base_params(h);
+    apply_collide(p, c);
+    set_u_bc(p, u_inflow);
+    p.block_slot = h->nslots > 0 ? h->d_block_slot : nullptr;
+    p.partials = h->d_partials;
+    p.fin = h->P[h->cur];
+    p.fout = h->P[h->cur ^ 1];
+    p.gin = h->G[h->cur];
+    p.gout = h->G[h->cur ^ 1];
+    p.gx = (h->nx + h->bx - 1) / h->bx;
+    p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
+    return LBM2D_OK;
+}
+
+}  // namespace rt
+}  // namespace lbm2d
+
+using namespace lbm2d::rt;
 
 extern "C" {
 
@@ -644,26 +594,28 @@ int lbm2d_upload_f_device(lbm2d_solver* h, const double* d_f) {
     return upload_common(h, d_f, false, cudaMemcpyDeviceToDevice);
 }
 
+int lbm2d_init_equilibrium(lbm2d_solver* h, double rho, double u, double v, double T) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if ((rc = materialize(h))) return rc;
+    if ((rc = ensure_stage(h, true))) return rc;
+    const int e = launch_fill_equilibrium(h->d_stage_f, h->d_stage_g, (long long)h->N, rho, u, v, T, h->stream);
+    ++h->launches;
+    if (e) return cuda_fail(h, (cudaError_t)e, "fill equilibrium");
+    h->staged = true;
+    h->stage_f_valid = h->stage_g_valid = true;
+    CK(cudaMemsetAsync(h->d_counter, 0, 8, h->stream), "reset history");
+    h->steps_done = 0;
+    return LBM2D_OK;
+}
+
 int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
     int rc;
     if ((rc = check_handle(h))) return rc;
     if (nsteps < 0) return fail(h, LBM2D_ERR_INVALID, "negative step count");
     if (nsteps == 0) return LBM2D_OK;
-    if (!(tau > 0.0)) return fail(h, LBM2D_ERR_INVALID, "tau must be positive");
-    const CollideParams c = collide_params(h, tau);
-    if (!h->staged && !(c == h->cp_of_P)) {
-        if ((rc = materialize(h))) return rc;
-    }
-    if ((rc = upload_geometry(h))) return rc;
-    if ((rc = ensure_slots(h))) return rc;
-    if (h->staged) {
-        if ((rc = prologue(h, c))) return rc;
-    }
-    KParams p = base_params(h);
-    apply_collide(p, c);
-    set_u_bc(p, u_inflow);
-    p.block_slot = h->nslots > 0 ? h->d_block_slot : nullptr;
-    p.partials = h->d_partials;
+    KParams p;
+    if ((rc = prepare_steps(h, tau, u_inflow, p))) return rc;
     for (int k = 0; k < nsteps; ++k) {
         p.fin = h->P[h->cur];
         p.fout = h->P[h->cur ^ 1];

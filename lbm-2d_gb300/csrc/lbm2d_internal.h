@@ -88,6 +88,7 @@ struct KParams {
     unsigned int* nan_flag;
     // solid nodes whose state can no longer change may skip their stores
     int skip_settled_solids;
+    int gx;  // width of the instance's block grid (batched launches)
 };
 
 // Readback outputs (any may be null).
@@ -98,11 +99,28 @@ struct ROut {
     double *fx, *fy;
 };
 
+// One instance's second-stage force reduction in a batched launch.
+struct ReduceJob {
+    const double* partials;
+    int nslots, cap;
+    double* hist;
+    unsigned long long* counter;
+    double* last;
+};
+
 // Launchers (lbm2d_kernels.cu).  All return a cudaError_t as int.
 int launch_step(int storage, const KParams& p, int bx, int by, void* stream);
 int launch_readback(int storage, const KParams& p, const ROut& o, void* stream);
 // Collide an FP64 AoS state S (device) into the stored post-collision state.
 int launch_prologue(int storage, const KParams& p, const double* f_aos, const double* g_aos, void* stream);
+// Step several instances at once: inst[] holds one KParams per instance and
+// block_start[] (ninst+1 entries, device memory) the first launch block of
+// each instance; nblocks = block_start[ninst].
+int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
+                      int bx, int by, void* stream);
+int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream);
+int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, double u, double v, double T,
+                            void* stream);
 int launch_force_reduce(const double* partials, int nslots, double* hist, int hist_cap,
                         unsigned long long* counter, double* last, void* stream);
 

@@ -374,7 +374,7 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
 #pragma unroll
         for (int i = 0; i < 9; ++i) f[i] -= it * (f[i] - feq<R>(i, rho, u, v));
     }
-    if (p.Fscale != 0.0) {
+    if (q.Fscale != R(0)) {
         const R F = q.Fscale;
         const R fa = R(1.0 / 9.0) * F, fd = R(1.0 / 36.0) * F;
         f[1] += fa;
@@ -391,7 +391,7 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
         const R om = q.omega_k;
 #pragma unroll
         for (int i = 0; i < 9; ++i) g[i] -= om * (g[i] - feq<R>(i, T, u2, v2));
-        if (p.pd.beta > 0.0 && p.pd.g_buoy != 0.0) {
+        if (q.beta > R(0) && q.g_buoy != R(0)) {
             const R fyb = -q.beta * (T - q.T_ref) * q.g_buoy;
 #pragma unroll
             for (int i = 0; i < 9; ++i) {
@@ -429,11 +429,12 @@ __device__ __forceinline__ void block_reduce2(double& a, double& b) {
 }
 
 // ----------------------------------------------------------------- kernels
+// One step of the block (bxi, byi) of an instance whose block grid is gx wide.
 template <class T, bool TH>
-__global__ void __launch_bounds__(512) step_kernel(const KParams p) {
+__device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, int gx) {
     using R = typename Pop<T>::R;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = bxi * blockDim.x + threadIdx.x;
+    const int y = byi * blockDim.y + threadIdx.y;
     R fxs = R(0), fys = R(0);
     if (x < p.nx && y < p.ny) {
         const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
@@ -466,22 +467,68 @@ __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
         }
     }
     if (p.block_slot) {
-        const int base = p.block_slot[blockIdx.y * gridDim.x + blockIdx.x];
+        const int base = p.block_slot[byi * gx + bxi];
         if (base >= 0) {  // uniform per block; no barrier: one slot per warp
-            double a = double(fxs), b = double(fys);
+            // Warp sum in the compute precision (FP32 per-node terms carry FP32
+            // rounding already; the FP64 variant stays FP64), only in warps that
+            // hold a force node; the cross-warp sum is FP64.
+            R a = fxs, b = fys;
+            if (__any_sync(0xffffffffu, a != R(0) || b != R(0))) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_down_sync(0xffffffffu, a, o);
-                b += __shfl_down_sync(0xffffffffu, b, o);
+                for (int o = 16; o > 0; o >>= 1) {
+                    a += __shfl_down_sync(0xffffffffu, a, o);
+                    b += __shfl_down_sync(0xffffffffu, b, o);
+                }
             }
             const int tid = threadIdx.y * blockDim.x + threadIdx.x;
             if ((tid & 31) == 0) {
                 const int slot = base + (tid >> 5);
-                p.partials[2 * slot] = a;
-                p.partials[2 * slot + 1] = b;
+                p.partials[2 * slot] = double(a);
+                p.partials[2 * slot + 1] = double(b);
             }
         }
     }
+}
+
+template <class T, bool TH>
+__global__ void __launch_bounds__(512) step_kernel(const KParams p) {
+    step_block<T, TH>(p, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+// Many independent instances in one launch (the tile-to-instance table):
+// instance k owns the launch blocks [block_start[k], block_start[k+1]) and
+// walks its own block grid (gx = p.gx blocks wide).  The block finds its
+// instance by binary search and stages that instance's parameters in shared
+// memory once.
+template <class T, bool TH>
+__global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restrict__ inst,
+                                                         const int* __restrict__ block_start, int ninst) {
+    __shared__ KParams sp;
+    __shared__ int s_inst;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
+    if (tid == 0) {
+        int lo = 0, hi = ninst - 1;  // last k with block_start[k] <= b
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (block_start[mid] <= b)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        s_inst = lo;
+    }
+    __syncthreads();
+    const int k = s_inst;
+    {
+        const int* src = reinterpret_cast<const int*>(inst + k);
+        int* dst = reinterpret_cast<int*>(&sp);
+        const int nw = (int)(sizeof(KParams) / sizeof(int));
+        for (int w = tid; w < nw; w += blockDim.x * blockDim.y) dst[w] = src[w];
+    }
+    __syncthreads();
+    const int local = b - block_start[k];
+    step_block<T, TH>(sp, local % sp.gx, local / sp.gx, sp.gx);
 }
 
 template <class T, bool TH>
@@ -551,6 +598,22 @@ __global__ void prologue_kernel(const KParams p, const double* __restrict__ fa, 
     }
 }
 
+// Uniform equilibrium state written into the FP64 AoS staging buffers, as
+// the drivers' initialisation loops do (every node, solids included).
+__global__ void fill_equilibrium_kernel(double* __restrict__ fa, double* __restrict__ ga, long long N, double rho,
+                                        double u, double v, double T) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const double ed = double(CXf(i)) * u + double(CYf(i)) * v;
+        const double usq = u * u + v * v;
+        const double poly = 1.0 + 3.0 * ed + 4.5 * ed * ed - 1.5 * usq;
+        fa[n * 9 + i] = wgt(i) * rho * poly;
+        if (ga) ga[n * 9 + i] = wgt(i) * T * poly;
+    }
+}
+
 // Deterministic second stage of the force reduction: one block sums the
 // per-block partials in a fixed order and appends (fx, fy) to the history.
 __global__ void force_reduce_kernel(const double* __restrict__ part, int nslots, double* hist, int cap,
@@ -571,6 +634,39 @@ __global__ void force_reduce_kernel(const double* __restrict__ part, int nslots,
         last[1] = b;
         *counter = k + 1;
     }
+}
+
+// Force reduction of several instances: block b reduces job b.
+__global__ void batch_force_reduce_kernel(const ReduceJob* __restrict__ jobs) {
+    const ReduceJob j = jobs[blockIdx.x];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < j.nslots; k += blockDim.x) {
+        a += j.partials[2 * k];
+        b += j.partials[2 * k + 1];
+    }
+    block_reduce2(a, b);
+    if (threadIdx.x == 0) {
+        const unsigned long long k = *j.counter;
+        if (k < (unsigned long long)j.cap) {
+            j.hist[2 * k] = a;
+            j.hist[2 * k + 1] = b;
+        }
+        j.last[0] = a;
+        j.last[1] = b;
+        *j.counter = k + 1;
+    }
+}
+
+template <class T>
+int launch_batch_t(const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal, int bx, int by,
+                   cudaStream_t s) {
+    if (nblocks <= 0 || ninst <= 0) return 0;
+    dim3 blk(bx, by);
+    if (thermal)
+        batch_step_kernel<T, true><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
+    else
+        batch_step_kernel<T, false><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
+    return (int)cudaGetLastError();
 }
 
 template <class T>
@@ -636,6 +732,32 @@ int launch_prologue(int storage, const KParams& p, const double* fa, const doubl
         case ST_FP64: return launch_prologue_t<double>(p, fa, ga, s);
     }
     return (int)cudaErrorInvalidValue;
+}
+
+int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
+                      int bx, int by, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_batch_t<float>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
+        case ST_FP16: return launch_batch_t<__half>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
+        case ST_BF16: return launch_batch_t<__nv_bfloat16>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
+        case ST_FP64: return launch_batch_t<double>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream) {
+    if (njobs <= 0) return 0;
+    batch_force_reduce_kernel<<<njobs, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
+    return (int)cudaGetLastError();
+}
+
+int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, double u, double v, double T,
+                            void* stream) {
+    const int bs = 256;
+    fill_equilibrium_kernel<<<(unsigned)((N + bs - 1) / bs), bs, 0, static_cast<cudaStream_t>(stream)>>>(fa, ga, N, rho,
+                                                                                                   u, v, T);
+    return (int)cudaGetLastError();
 }
 
 int launch_force_reduce(const double* partials, int nslots, double* hist, int cap, unsigned long long* counter,

@@ -1,0 +1,128 @@
+// lbm2d_runtime.h -- the solver handle and its state machine (host runtime),
+// shared by the single-instance C-ABI (lbm2d_capi.cpp) and the batched /
+// serving layer (lbm2d_batch.cpp).  Not part of the public interface.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm2d.h"
+#include "lbm2d_geometry.h"
+#include "lbm2d_internal.h"
+
+namespace lbm2d {
+namespace rt {
+
+inline constexpr double W[9] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0,
+                         1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
+inline constexpr int CASE_CAVITY = 1, CASE_STEP = 2, CASE_RIBS = 3, CASE_HILLS = 9;
+
+inline size_t elem_size(int storage) {
+    switch (storage) {
+        case ST_FP32: return 4;
+        case ST_FP16:
+        case ST_BF16: return 2;
+        case ST_FP64: return 8;
+    }
+    return 0;
+}
+
+struct CollideParams {
+    int collision = 0, les = 0, thermal = 0;
+    double s_shear = 0, s_bulk = 0, s_normal = 0, tau = 0, cs_sq = 0, nu = 0, Fscale = 0;
+    double omega_k = 0, beta = 0, g_buoy = 0, T_ref = 0;
+    bool operator==(const CollideParams& o) const {
+        return collision == o.collision && les == o.les && thermal == o.thermal && s_shear == o.s_shear &&
+               s_bulk == o.s_bulk && s_normal == o.s_normal && tau == o.tau && cs_sq == o.cs_sq && nu == o.nu &&
+               Fscale == o.Fscale && omega_k == o.omega_k && beta == o.beta && g_buoy == o.g_buoy &&
+               T_ref == o.T_ref;
+    }
+};
+
+}  // namespace rt
+}  // namespace lbm2d
+
+struct lbm2d_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nx = 0, ny = 0;
+    size_t N = 0;
+    int case_type = 0, collision = 0, use_les = 0, storage = 0;
+    double cs = 0.12;
+    std::vector<uint8_t> mask;
+    lbm2d::BBGeometry bb;
+    double body_force = 0.0;
+    bool thermal = false;
+    double T_ref = 1.0, alpha = 0.1666666667, omega_k = 1.0, beta = 0.0, g_buoy = 0.0;
+    int hook = 0;
+    double hook_a = 0.0, hook_b = 0.0;
+
+    // device buffers
+    void* P[2] = {nullptr, nullptr};
+    void* G[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint32_t* d_flags = nullptr;
+    uint32_t* d_rec_info = nullptr;
+    uint32_t* d_rec_force = nullptr;
+    double* d_rec_wd = nullptr;
+    double* d_rec_q = nullptr;
+    double* d_rec_uw = nullptr;
+    double* d_partials = nullptr;
+    int* d_block_slot = nullptr;
+    int nslots = 0, slot_bx = 0, slot_by = 0;
+    double* d_hist = nullptr;
+    int hist_cap = 1 << 18;
+    unsigned long long* d_counter = nullptr;
+    double* d_last = nullptr;
+    unsigned int* d_nan = nullptr;
+    double* d_stage_f = nullptr;
+    double* d_stage_g = nullptr;
+    double* d_fx = nullptr;
+    double* d_fy = nullptr;
+    size_t device_bytes = 0;
+
+    lbm2d::GeometryTables geo;
+    bool geom_dirty = true;
+    bool staged = true;  // STAGED (true) or COLLIDED (false)
+    bool stage_f_valid = false, stage_g_valid = false;  // staging holds S (else defaults)
+    lbm2d::rt::CollideParams cp_of_P;
+    double u_last = 0.0;
+    long long steps_since_collide = 0;
+    long long steps_done = 0;
+    long long launches = 0;
+    int bx = 128, by = 2;
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;  // even/odd = start/stop
+    size_t ev_used = 0;
+    std::string err;
+};
+
+
+namespace lbm2d {
+namespace rt {
+
+int fail(lbm2d_solver* h, int code, const std::string& msg);
+int cuda_fail(lbm2d_solver* h, cudaError_t e, const char* what);
+int bc_kind(int case_type);
+CollideParams collide_params(const lbm2d_solver* h, double tau);
+KParams base_params(const lbm2d_solver* h);
+void set_u_bc(KParams& p, double u);
+void apply_collide(KParams& p, const CollideParams& c);
+int ensure_populations(lbm2d_solver* h);
+int ensure_stage(lbm2d_solver* h, bool want_g);
+int upload_geometry(lbm2d_solver* h);
+int ensure_slots(lbm2d_solver* h);
+KParams rebuild_params(const lbm2d_solver* h);
+int materialize(lbm2d_solver* h);
+int before_setting_change(lbm2d_solver* h);
+int prologue(lbm2d_solver* h, const CollideParams& c);
+int check_handle(lbm2d_solver* h);
+// Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
+// kernel parameters of the next step (fin = current buffer); returns status.
+int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p);
+
+}  // namespace rt
+}  // namespace lbm2d

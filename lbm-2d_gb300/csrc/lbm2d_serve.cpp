@@ -1,0 +1,333 @@
+// lbm2d_serve.cpp -- a serving loop for many concurrent solves on one GPU.
+//
+// Requests (grid, geometry, Reynolds number, step budget, storage) arrive at
+// any time through lbm2d_server_submit.  A worker thread
+//   * admits queued requests in arrival order while the device-memory
+//     footprint of the active solves stays within the budget and a slot is
+//     free: it builds the case the way the reference's drivers do (mask,
+//     bounce-back geometry, tau from Re, LES when tau < 0.55, thermal set-up)
+//     and initialises the state on the device;
+//   * advances every active solve together: one lbm2d_batch_step per tick
+//     (one packed launch per step per storage group, CUDA-graph replay), the
+//     tick being the smallest remaining budget capped at steps_per_tick, so
+//     every solve stops exactly at its budget;
+//   * retires finished solves (drag/lift read back, memory freed) and
+//     records arrival, admission and completion times.
+// New requests are admitted while the GPU works on the current tick.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "lbm2d_runtime.h"
+
+using namespace lbm2d;
+
+namespace {
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Pending {
+    long long id;
+    lbm2d_request req;
+    double t_submit;
+};
+
+struct Active {
+    long long id;
+    lbm2d_request req;
+    lbm2d_solver* h = nullptr;
+    long long left = 0;
+    double t_submit = 0, t_admit = 0;
+    size_t footprint = 0;
+};
+
+size_t footprint_bytes(const lbm2d_request& r) {
+    const size_t n = (size_t)r.nx * r.ny;
+    const size_t es = r.storage == LBM2D_STORE_FP64 ? 8 : (r.storage == LBM2D_STORE_FP32 ? 4 : 2);
+    const int sets = r.geometry == LBM2D_GEOM_HEATED_CAVITY ? 2 : 1;
+    // populations (2 buffers) + FP64 staging + flags + boundary records (generous)
+    return sets * (2 * 9 * n * es + 72 * n) + 4 * n + 256 * (size_t)(2 * (r.nx + r.ny)) + (1 << 20);
+}
+
+}  // namespace
+
+struct lbm2d_server {
+    int device = 0;
+    size_t budget = 0;
+    int max_active = 0;
+    int steps_per_tick = 0;
+    lbm2d_batch* batch = nullptr;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Pending> queue;
+    std::vector<lbm2d_result> results;
+    std::vector<Active> active;
+    size_t used = 0;
+    long long next_id = 0, submitted = 0, finished = 0;
+    bool stop = false, running = false;
+    double busy_s = 0.0;
+    long long lattice_updates = 0;
+    std::string err;
+};
+
+namespace {
+
+// Build one solve the way the reference's drivers do.
+int setup_request(lbm2d_server* s, Active& a) {
+    const lbm2d_request& r = a.req;
+    const int nx = r.nx, ny = r.ny;
+    const double u = r.u > 0 ? r.u : 0.1;
+    int case_type = LBM2D_CASE_CAVITY;
+    double L = nx, tau = 0.0;
+    std::vector<uint8_t> mask((size_t)nx * ny, 0);
+    double bcx = 0, bcy = 0, br = 0;
+    bool thermal = false;
+    switch (r.geometry) {
+        case LBM2D_GEOM_CAVITY:  // src/cavity.cpp:27-29, :72
+            case_type = LBM2D_CASE_CAVITY;
+            lbm2d_mask_walls(nx, ny, mask.data());
+            L = nx;
+            break;
+        case LBM2D_GEOM_STEP: {  // src/step.cpp:37-45, :89-104
+            case_type = LBM2D_CASE_STEP;
+            const int hs = ny / 3, hin = ny - 1 - hs;
+            for (int y = 0; y < ny; ++y)
+                for (int x = 0; x < nx; ++x)
+                    if (y == 0 || y == ny - 1 || (x < nx / 4 && y < hs)) mask[(size_t)y * nx + x] = 1;
+            L = 2.0 * hin;
+            break;
+        }
+        case LBM2D_GEOM_CYLINDER:  // D = NY/5, src/main.cpp:32-36, :55-58
+            case_type = LBM2D_CASE_CYLINDER;
+            br = ny / 10;
+            bcx = nx / 4;
+            bcy = ny / 2 + 1;
+            lbm2d_mask_cylinder(nx, ny, mask.data(), (int)bcx, (int)bcy, (int)br);
+            L = ny / 5.0;
+            break;
+        case LBM2D_GEOM_SIDE_BY_SIDE: {  // two cylinders D = H/5 at S/D = param, src/side_by_side_cylinders.cpp:50-62
+            case_type = LBM2D_CASE_SIDE_BY_SIDE;
+            const int rad = ny / 10, D = 2 * rad;
+            const double sd = r.param > 0 ? r.param : 3.0;
+            const int spacing = (int)(sd * D), cx = nx / 4;
+            const int cy1 = ny / 2 - spacing / 2, cy2 = cy1 + spacing;
+            lbm2d_mask_cylinder(nx, ny, mask.data(), cx, cy1, rad);
+            lbm2d_mask_cylinder(nx, ny, mask.data(), cx, cy2, rad);
+            bcx = cx;
+            bcy = cy2;
+            br = rad;
+            L = D;
+            break;
+        }
+        case LBM2D_GEOM_HEATED_CAVITY:  // src/thermal_cavity.cpp:57-115 (tau 0.8)
+            case_type = LBM2D_CASE_CYLINDER;
+            for (int y = 0; y < ny; ++y)
+                for (int x = 0; x < nx; ++x)
+                    if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) mask[(size_t)y * nx + x] = 1;
+            thermal = true;
+            tau = 0.8;
+            break;
+        default:
+            return LBM2D_ERR_INVALID;
+    }
+    const double re = r.re > 0 ? r.re : 100.0;
+    if (!thermal) tau = 0.5 + 3.0 * (u * L / re);
+    const int les = tau < 0.55 ? 1 : 0;  // the drivers' auto-LES (e.g. src/main.cpp:174-182)
+    lbm2d_config cfg{nx, ny, case_type, LBM2D_MRT, les, 0.12, r.storage, s->device};
+    int rc = lbm2d_create(&cfg, &a.h);
+    if (rc) return rc;
+    if ((rc = lbm2d_set_mask(a.h, mask.data()))) return rc;
+    if (br > 0 && (rc = lbm2d_set_bb_cylinder(a.h, bcx, bcy, br))) return rc;
+    double u_init = 0.0, u_bc = u;
+    if (thermal) {
+        const double Pr = 0.71, Th = 1.5, Tc = 0.5, Lc = ny;
+        const double nu = (tau - 0.5) / 3.0, alpha = nu / Pr;
+        const double ra = r.param > 0 ? r.param : 1e4;
+        const double gb = ra * nu * alpha / ((Th - Tc) * Lc * Lc * Lc);
+        const double beta = 0.001;
+        if ((rc = lbm2d_set_thermal(a.h, 1, 1.0, alpha, 1.0 / (0.5 + 3.0 * alpha), beta, -gb / beta))) return rc;
+        if ((rc = lbm2d_set_thermal_hook(a.h, LBM2D_HOOK_HEATED_CAVITY, Th, Tc))) return rc;
+        u_bc = 0.0;
+    } else if (case_type == LBM2D_CASE_CYLINDER || case_type == LBM2D_CASE_SIDE_BY_SIDE) {
+        u_init = u;  // uniform inflow initial state
+    }
+    if ((rc = lbm2d_init_equilibrium(a.h, 1.0, u_init, 0.0, 1.0))) return rc;
+    return lbm2d_batch_add(s->batch, a.h, tau, u_bc);
+}
+
+void record(lbm2d_server* s, const Active& a, int status) {
+    lbm2d_result res{};
+    res.id = a.id;
+    res.status = status;
+    res.t_submit = a.t_submit;
+    res.t_admit = a.t_admit;
+    res.t_done = now_s();
+    res.steps = a.req.steps - a.left;
+    res.nodes = (long long)a.req.nx * a.req.ny;
+    if (a.h && status == LBM2D_OK) lbm2d_force_sums(a.h, &res.fx, &res.fy);
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->results.push_back(res);
+    ++s->finished;
+    s->cv.notify_all();
+}
+
+void retire(lbm2d_server* s, size_t k, int status) {
+    Active a = s->active[k];
+    if (a.h) lbm2d_batch_remove(s->batch, a.h);
+    record(s, a, status);
+    if (a.h) lbm2d_destroy(a.h);
+    s->used -= a.footprint;
+    s->active.erase(s->active.begin() + k);
+}
+
+// Admit queued requests while the budget allows (arrival order).
+void admit(lbm2d_server* s) {
+    for (;;) {
+        Pending p;
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            if (s->queue.empty()) return;
+            const size_t fp = footprint_bytes(s->queue.front().req);
+            if ((int)s->active.size() >= s->max_active) return;
+            if (s->used + fp > s->budget && !s->active.empty()) return;
+            p = s->queue.front();
+            s->queue.pop_front();
+        }
+        Active a;
+        a.id = p.id;
+        a.req = p.req;
+        a.left = p.req.steps;
+        a.t_submit = p.t_submit;
+        a.t_admit = now_s();
+        a.footprint = footprint_bytes(p.req);
+        s->used += a.footprint;
+        const int rc = setup_request(s, a);
+        s->active.push_back(a);
+        if (rc) retire(s, s->active.size() - 1, rc);
+    }
+}
+
+void worker_loop(lbm2d_server* s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        admit(s);
+        if (s->active.empty()) {
+            std::unique_lock<std::mutex> lock(s->mu);
+            if (s->stop) return;
+            s->cv.wait(lock, [&] { return s->stop || !s->queue.empty(); });
+            if (s->stop && s->queue.empty()) return;
+            continue;
+        }
+        long long k = s->steps_per_tick;
+        for (auto& a : s->active) k = std::min(k, a.left);
+        const double t0 = now_s();
+        int rc = lbm2d_batch_step(s->batch, (int)k);
+        admit(s);  // host set-up of new arrivals overlaps the GPU work
+        if (!rc) rc = lbm2d_batch_synchronize(s->batch);
+        s->busy_s += now_s() - t0;
+        for (auto& a : s->active) {
+            a.left -= k;
+            s->lattice_updates += k * (long long)a.req.nx * a.req.ny;
+        }
+        for (size_t i = s->active.size(); i-- > 0;) {
+            Active& a = s->active[i];
+            if (a.left <= 0 || rc) {
+                int st = rc;
+                if (!st && a.h) st = lbm2d_synchronize(a.h);  // non-finite density -> LBM2D_ERR_NAN
+                retire(s, i, st);
+            }
+        }
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (s->stop && s->queue.empty() && s->active.empty()) return;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm2d_server_create(int device, double budget_bytes, int max_active, int steps_per_tick, lbm2d_server** out) {
+    if (!out || max_active < 1 || steps_per_tick < 1) return LBM2D_ERR_INVALID;
+    auto* s = new lbm2d_server();
+    s->device = device;
+    s->budget = budget_bytes > 0 ? (size_t)budget_bytes : (size_t)64 << 30;
+    s->max_active = max_active;
+    s->steps_per_tick = steps_per_tick;
+    int rc = lbm2d_batch_create(device, &s->batch);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    s->running = true;
+    s->worker = std::thread(worker_loop, s);
+    *out = s;
+    return LBM2D_OK;
+}
+
+int lbm2d_server_submit(lbm2d_server* s, const lbm2d_request* r, long long* id) {
+    if (!s || !r || r->nx < 3 || r->ny < 3 || r->steps < 0) return LBM2D_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (s->stop) return LBM2D_ERR_STATE;
+    Pending p{s->next_id++, *r, now_s()};
+    s->queue.push_back(p);
+    ++s->submitted;
+    if (id) *id = p.id;
+    s->cv.notify_all();
+    return LBM2D_OK;
+}
+
+int lbm2d_server_wait(lbm2d_server* s, long long n_finished, double timeout_s) {
+    if (!s) return LBM2D_ERR_INVALID;
+    std::unique_lock<std::mutex> lock(s->mu);
+    const bool ok = s->cv.wait_for(lock, std::chrono::duration<double>(timeout_s),
+                                   [&] { return s->finished >= n_finished; });
+    return ok ? LBM2D_OK : LBM2D_ERR_TIMEOUT;
+}
+
+int lbm2d_server_results(lbm2d_server* s, lbm2d_result* out, int capacity, int* count) {
+    if (!s || !count) return LBM2D_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(s->mu);
+    const int n = (int)s->results.size();
+    for (int k = 0; k < std::min(n, capacity); ++k) out[k] = s->results[k];
+    *count = n;
+    return LBM2D_OK;
+}
+
+int lbm2d_server_stats(lbm2d_server* s, lbm2d_server_stats_t* st) {
+    if (!s || !st) return LBM2D_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(s->mu);
+    st->submitted = s->submitted;
+    st->finished = s->finished;
+    st->queued = (long long)s->queue.size();
+    st->active = (long long)s->active.size();
+    st->busy_s = s->busy_s;
+    st->lattice_updates = s->lattice_updates;
+    st->device_bytes_in_use = (double)s->used;
+    return LBM2D_OK;
+}
+
+int lbm2d_server_destroy(lbm2d_server* s) {
+    if (!s) return LBM2D_OK;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop = true;
+        s->queue.clear();
+        s->cv.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    for (size_t k = s->active.size(); k-- > 0;) retire(s, k, LBM2D_ERR_STATE);
+    lbm2d_batch_destroy(s->batch);
+    delete s;
+    return LBM2D_OK;
+}
+
+}  // extern "C"

@@ -52,6 +52,25 @@ class BBGeometry(C.Structure):
                 ("omega", C.c_double), ("rot_cx", C.c_double), ("rot_cy", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("geometry", C.c_int), ("re", C.c_double),
+                ("param", C.c_double), ("u", C.c_double), ("steps", C.c_int), ("storage", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("status", C.c_int), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("steps", C.c_longlong), ("nodes", C.c_longlong), ("fx", C.c_double),
+                ("fy", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("finished", C.c_longlong), ("queued", C.c_longlong),
+                ("active", C.c_longlong), ("busy_s", C.c_double), ("lattice_updates", C.c_longlong),
+                ("device_bytes_in_use", C.c_double)]
+
+
+GEOM_CAVITY, GEOM_STEP, GEOM_CYLINDER, GEOM_SIDE_BY_SIDE, GEOM_HEATED_CAVITY = range(5)
+
 _D, _I, _P = C.c_double, C.c_int, C.c_void_p
 _DP = C.POINTER(C.c_double)
 _U8P = C.POINTER(C.c_uint8)
@@ -75,6 +94,7 @@ _SIGS = {
     "lbm2d_upload_f_device": ([_P, _P], _I),
     "lbm2d_download_f_device": ([_P, _P], _I),
     "lbm2d_step": ([_P, _D, _D, _I], _I),
+    "lbm2d_init_equilibrium": ([_P, _D, _D, _D, _D], _I),
     "lbm2d_force_sums": ([_P, _DP, _DP], _I),
     "lbm2d_force_history": ([_P, _DP, _DP, _I, C.POINTER(_I)], _I),
     "lbm2d_force_history_reset": ([_P], _I),
@@ -90,6 +110,26 @@ _SIGS = {
     "lbm2d_set_profiling": ([_P, _I], _I),
     "lbm2d_profile": ([_P, _DP, C.POINTER(C.c_longlong)], _I),
     "lbm2d_launch_count": ([_P], C.c_longlong),
+    "lbm2d_batch_create": ([_I, C.POINTER(_P)], _I),
+    "lbm2d_batch_destroy": ([_P], _I),
+    "lbm2d_batch_last_error": ([_P], C.c_char_p),
+    "lbm2d_batch_add": ([_P, _P, _D, _D], _I),
+    "lbm2d_batch_remove": ([_P, _P], _I),
+    "lbm2d_batch_set_params": ([_P, _P, _D, _D], _I),
+    "lbm2d_batch_size": ([_P], _I),
+    "lbm2d_batch_step": ([_P, _I], _I),
+    "lbm2d_batch_synchronize": ([_P], _I),
+    "lbm2d_batch_set_block": ([_P, _I, _I], _I),
+    "lbm2d_batch_stream": ([_P], _P),
+    "lbm2d_batch_launch_count": ([_P], C.c_longlong),
+    "lbm2d_autotune": ([_P, _I, _D, _D, C.POINTER(_I), C.POINTER(_I)], _I),
+    "lbm2d_server_create": ([_I, _D, _I, _I, C.POINTER(_P)], _I),
+    "lbm2d_server_submit": ([_P, C.POINTER(Request), C.POINTER(C.c_longlong)], _I),
+    "lbm2d_server_wait": ([_P, C.c_longlong, _D], _I),
+    "lbm2d_server_results": ([_P, C.POINTER(Result), _I, C.POINTER(_I)], _I),
+    "lbm2d_server_stats": ([_P, C.POINTER(ServerStats)], _I),
+    "lbm2d_server_destroy": ([_P], _I),
+    "lbm2d_batch_autotune": ([_P, _I, C.POINTER(_I), C.POINTER(_I)], _I),
     # host services
     "lbm2d_equilibrium": ([_I, _D, _D, _D], _D),
     "lbm2d_mask_walls": ([_I, _I, _U8P], _I),
@@ -321,6 +361,10 @@ class Solver:
     def init_uniform(self, rho, u, v):
         self.upload_f(equilibrium_field(self.nx, self.ny, rho, u, v))
 
+    def init_equilibrium(self, rho, u, v, T=1.0):
+        """Uniform equilibrium f (and g at temperature T) written on the device."""
+        self._ck(self.L.lbm2d_init_equilibrium(self.h, float(rho), float(u), float(v), float(T)))
+
     def step(self, tau, u_in, n=1):
         self._ck(self.L.lbm2d_step(self.h, float(tau), float(u_in), int(n)))
 
@@ -403,6 +447,12 @@ class Solver:
     def download_f_ptr(self, host_ptr: int):
         self._ck(self.L.lbm2d_download_f(self.h, C.cast(host_ptr, _DP)))
 
+    def autotune(self, tau, u_in, steps=20):
+        """Pick the fastest launch shape for this solver (state is preserved)."""
+        bx, by = _I(), _I()
+        self._ck(self.L.lbm2d_autotune(self.h, int(steps), float(tau), float(u_in), C.byref(bx), C.byref(by)))
+        return bx.value, by.value
+
     @property
     def stream(self) -> int:
         return int(self.L.lbm2d_stream(self.h) or 0)
@@ -410,3 +460,117 @@ class Solver:
     @property
     def launches(self) -> int:
         return int(self.L.lbm2d_launch_count(self.h))
+
+
+class Batch:
+    """Many independent solvers stepped by one packed launch per step."""
+
+    def __init__(self, device: int = 0):
+        L = lib()
+        h = _P()
+        rc = L.lbm2d_batch_create(int(device), C.byref(h))
+        if rc:
+            raise LBMError(rc, "batch create")
+        self.L, self.h = L, h
+        self.members: list[Solver] = []
+
+    def _ck(self, rc):
+        if rc:
+            raise LBMError(rc, self.L.lbm2d_batch_last_error(self.h).decode())
+
+    def add(self, solver: Solver, tau: float, u_in: float):
+        self._ck(self.L.lbm2d_batch_add(self.h, solver.h, float(tau), float(u_in)))
+        self.members.append(solver)
+
+    def remove(self, solver: Solver):
+        self._ck(self.L.lbm2d_batch_remove(self.h, solver.h))
+        self.members.remove(solver)
+
+    def set_params(self, solver: Solver, tau: float, u_in: float):
+        self._ck(self.L.lbm2d_batch_set_params(self.h, solver.h, float(tau), float(u_in)))
+
+    def step(self, n: int = 1):
+        self._ck(self.L.lbm2d_batch_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._ck(self.L.lbm2d_batch_synchronize(self.h))
+
+    def set_block(self, bx, by):
+        self._ck(self.L.lbm2d_batch_set_block(self.h, int(bx), int(by)))
+
+    def autotune(self, steps=10):
+        bx, by = _I(), _I()
+        self._ck(self.L.lbm2d_batch_autotune(self.h, int(steps), C.byref(bx), C.byref(by)))
+        return bx.value, by.value
+
+    @property
+    def stream(self) -> int:
+        return int(self.L.lbm2d_batch_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.lbm2d_batch_launch_count(self.h))
+
+    def __len__(self):
+        return int(self.L.lbm2d_batch_size(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lbm2d_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop: concurrent solves admitted by device-memory footprint and
+    stepped together (see include/lbm2d.h, lbm2d_server_*)."""
+
+    def __init__(self, device=0, budget_bytes=64 << 30, max_active=512, steps_per_tick=200):
+        L = lib()
+        h = _P()
+        rc = L.lbm2d_server_create(int(device), float(budget_bytes), int(max_active), int(steps_per_tick),
+                                   C.byref(h))
+        if rc:
+            raise LBMError(rc, "server create")
+        self.L, self.h = L, h
+
+    def submit(self, nx, ny, geometry, re, steps, storage="fp16", param=0.0, u=0.1) -> int:
+        r = Request(int(nx), int(ny), int(geometry), float(re), float(param), float(u), int(steps),
+                    STORAGE[storage] if isinstance(storage, str) else int(storage))
+        rid = C.c_longlong()
+        rc = self.L.lbm2d_server_submit(self.h, C.byref(r), C.byref(rid))
+        if rc:
+            raise LBMError(rc, "submit")
+        return rid.value
+
+    def wait(self, n_finished, timeout_s=600.0) -> bool:
+        return self.L.lbm2d_server_wait(self.h, int(n_finished), float(timeout_s)) == 0
+
+    def results(self) -> list[dict]:
+        n = _I()
+        self.L.lbm2d_server_results(self.h, None, 0, C.byref(n))
+        arr = (Result * max(n.value, 1))()
+        self.L.lbm2d_server_results(self.h, arr, n.value, C.byref(n))
+        keys = [k for k, _ in Result._fields_]
+        return [{k: getattr(arr[i], k) for k in keys} for i in range(n.value)]
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self.L.lbm2d_server_stats(self.h, C.byref(st))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lbm2d_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
