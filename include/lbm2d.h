@@ -196,6 +196,20 @@ long long lbm2d_launch_count(lbm2d_solver *h);
 int lbm2d_set_profiling(lbm2d_solver *h, int on);
 int lbm2d_profile(lbm2d_solver *h, double *step_kernel_ms, long long *n_launches);
 
+/* Step without any allocation, for callers that may not allocate device
+ * memory once running: real-time or co-simulation loops with a per-step
+ * deadline (cudaMalloc/cudaFree can synchronize the device and take
+ * milliseconds) and processes whose device footprint is fixed at start-up.
+ * No counterpart in the reference.  The solver must have been prepared by a
+ * prior lbm2d_step with the same tau and settings (else LBM2D_ERR_STATE);
+ * the force-reduction scratch is a fixed 2 MiB array inside the library
+ * (at most 131072 per-warp force slots, else LBM2D_ERR_INVALID), held on
+ * every GPU that loads the library until the process exits.  The first call
+ * on a device looks the array's address up (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All callers share the array: calls
+ * that overlap on the GPU (e.g. two solvers on different streams) race. */
+int lbm2d_step_noalloc(lbm2d_solver *h, double tau, double u_inflow, int nsteps);
+
 /* Device-resident variants for callers that keep populations on the GPU:
  * pointers to device memory, same FP64 AoS layout, stream-ordered on the
  * handle's stream (no host synchronization). */

@@ -95,6 +95,7 @@ _SIGS = {
     "lbm2d_download_f_device": ([_P, _P], _I),
     "lbm2d_step": ([_P, _D, _D, _I], _I),
     "lbm2d_init_equilibrium": ([_P, _D, _D, _D, _D], _I),
+    "lbm2d_step_noalloc": ([_P, _D, _D, _I], _I),
     "lbm2d_force_sums": ([_P, _DP, _DP], _I),
     "lbm2d_force_history": ([_P, _DP, _DP, _I, C.POINTER(_I)], _I),
     "lbm2d_force_history_reset": ([_P], _I),
