@@ -329,12 +329,16 @@ def run_serve(args):
         lat_s = []
         lu_s = 0
         wall0 = time.perf_counter()
+        failed = 0
         for r, at in zip(reqs, arrivals):
             start = max(clock, at)
             ts = time.perf_counter()
             s = _plain_solver(lbm2d, r, storage)
             s.step(s._tau, s._ubc, r["steps"])
-            s.synchronize()
+            try:
+                s.synchronize()
+            except lbm2d.LBMError:  # diverged (non-finite density), as the reference would
+                failed += 1
             s.close()
             dt = time.perf_counter() - ts
             clock = start + dt
@@ -342,7 +346,7 @@ def run_serve(args):
             lu_s += r["steps"] * r["nx"] * r["ny"]
         busy = time.perf_counter() - wall0
         lat_s = np.array(lat_s)
-        seq = {"p50_s": float(np.percentile(lat_s, 50)), "p99_s": float(np.percentile(lat_s, 99)),
+        seq = {"p50_s": float(np.percentile(lat_s, 50)), "p99_s": float(np.percentile(lat_s, 99)), "failed": failed,
                "makespan_s": clock, "glups": lu_s / clock / 1e9, "busy_glups": lu_s / busy / 1e9,
                "note": "same requests and arrival times, solved one at a time with lbm2d_step (FIFO)"}
     line = {"metric": "serving: p50/p99 time-to-solution and aggregate GLUPS", "unit": "GLUPS",
@@ -515,6 +519,7 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--storages", default="fp32,fp16,bf16")
     ap.add_argument("--plain", default="fp32,fp16", help="storages also timed without LES (plain MRT)")
+    ap.add_argument("--variant", type=int, default=0, help="step kernel: 0 paired nodes per thread, 1 one node")
     ap.add_argument("--cpu-size", type=int, default=1024)
     ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
@@ -562,6 +567,7 @@ def main():
     results = {}
     for label, storage, les in runs:
         s = configure(lbm2d, storage, mask, circles, local, nx, ny, les)
+        s.set_kernel_variant(args.variant)
         s.upload_f(f0)
         reps.barrier()
         clocks.active = True
@@ -648,7 +654,8 @@ def main():
         "config": {"workload": workload_name(nx, ny), "nx": nx, "ny": ny, "storage": main_st, "tau": TAU,
                    "body_force_x": BODY_FORCE, "l2": "inputs larger than L2 (populations >= 129 MB, no flush)",
                    "parallelism": "replicas" if world > 1 else "single GPU", "block": list(r0["block"]),
-                   "boundary_nodes": r0["boundary"], "force_nodes": r0["force_nodes"], "diverged": r0["nan"]},
+                   "boundary_nodes": r0["boundary"], "force_nodes": r0["force_nodes"], "diverged": r0["nan"],
+                   "kernel_variant": "paired nodes, packed FP32x2" if args.variant == 0 else "one node per thread"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
                      "kernel_ms": r0["kernel_ms"], "kernel": "step_kernel"},

@@ -177,6 +177,14 @@ int lbm2d_download_force_field(lbm2d_solver *h, double *fx_body, double *fy_body
 int lbm2d_download_macros(lbm2d_solver *h, double *rho, double *u, double *v, double *T);
 int lbm2d_download_wall_dist(lbm2d_solver *h, double *wall_dist);
 
+/* FP64 reductions over the fluid nodes of the current state: total mass
+ * (the quantity of the reference's conservation test, src/lbm_test.cpp:
+ * 173-198), x/y momentum, and the steady-state residual
+ * ||u - u_prev|| / ||u|| against the velocity field of the previous call
+ * (NaN on the first call) -- the field-level counterpart of the reference's
+ * check_convergence (src/lbm.hpp:93-104).  Any output may be NULL. */
+int lbm2d_diagnostics(lbm2d_solver *h, double *mass, double *mom_x, double *mom_y, double *residual);
+
 /* Wait for the handle's stream; reports LBM2D_ERR_NAN if any step since the
  * last check produced a non-finite density. */
 int lbm2d_synchronize(lbm2d_solver *h);
@@ -184,6 +192,11 @@ int lbm2d_get_info(lbm2d_solver *h, lbm2d_info *info);
 /* Launch shape of the step kernel (threads per block = bx*by, a multiple of
  * 32, at most 1024).  0,0 restores the tuned default. */
 int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
+/* Step-kernel variant: 0 (default) runs two x-neighbours per thread with
+ * packed FP32x2 arithmetic where the grid allows (nx even, non-thermal,
+ * FP32/FP16/BF16 storage), 1 forces one node per thread.  Same results to
+ * rounding. */
+int lbm2d_set_kernel_variant(lbm2d_solver *h, int variant);
 /* The CUDA stream the handle launches on (cudaStream_t as void*). */
 void *lbm2d_stream(lbm2d_solver *h);
 /* Count of kernel launches made by this handle since creation. */
@@ -317,6 +330,20 @@ int lbm2d_naca_coords(int series, int n, double *out);
 int lbm2d_transform_points(double *xy, int n, double cx, double cy, double scale, double angle_deg);
 /* compute_wall_distance's result, src/lbm_types.hpp:231-264 */
 int lbm2d_wall_distance(int nx, int ny, const uint8_t *mask, double *wall_dist);
+
+/* Statistics of a drag/lift series as the reference's post-processing
+ * computes them (scripts/extract_forces.py:91-121 and :137-158): means of
+ * v1 (Cd or Fx) and v2 (Cl or Fy) after skipping the first 20% of samples
+ * (none if that is fewer than 10), the standard deviation of v2, and the
+ * shedding frequency from upward crossings of the mean of v2 after a 40%
+ * (at least 50 samples) transient: crossings / (2 * duration * dt); st is
+ * NaN when the script reports None (fewer than 200 samples, fewer than 100
+ * after the skip, or fewer than 2 crossings). */
+typedef struct lbm2d_force_stats_t {
+    double mean_v1, mean_v2, std_v2, st;
+    int n_skip;
+} lbm2d_force_stats_t;
+int lbm2d_force_stats(const double *v1, const double *v2, int n, double dt, lbm2d_force_stats_t *out);
 
 /* Geometry of the interpolated bounce-back (BounceBackGeometry,
  * src/lbm_types.hpp:90-182) for the host link query below. */

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <chrono>
 #include <map>
+#include <tuple>
 
 #include "lbm2d_runtime.h"
 
@@ -29,7 +30,7 @@ struct Member {
 };
 
 struct Group {
-    int storage = 0, thermal = 0;
+    int storage = 0, thermal = 0, pair = 0;
     std::vector<int> members;  // indices into lbm2d_batch::members
     int nblocks = 0;
     int njobs = 0;
@@ -94,16 +95,17 @@ int member_index(lbm2d_batch* b, lbm2d_solver* h) {
 int build_layout(lbm2d_batch* b) {
     if (!b->layout_dirty) return LBM2D_OK;
     free_groups(b);
-    std::map<std::pair<int, int>, int> gi;
+    std::map<std::tuple<int, int, int>, int> gi;
     for (size_t k = 0; k < b->members.size(); ++k) {
         lbm2d_solver* h = b->members[k].h;
-        const auto key = std::make_pair(h->storage, h->thermal ? 1 : 0);
+        const auto key = std::make_tuple(h->storage, h->thermal ? 1 : 0, use_pair(h) ? 1 : 0);
         auto it = gi.find(key);
         if (it == gi.end()) {
             gi[key] = (int)b->groups.size();
             Group g;
-            g.storage = key.first;
-            g.thermal = key.second;
+            g.storage = std::get<0>(key);
+            g.thermal = std::get<1>(key);
+            g.pair = std::get<2>(key);
             b->groups.push_back(g);
             it = gi.find(key);
         }
@@ -188,7 +190,7 @@ int prepare(lbm2d_batch* b) {
 int launch_one(lbm2d_batch* b, int parity) {
     for (auto& g : b->groups) {
         int e = launch_batch_step(g.storage, g.d_params[parity], g.d_block_start, (int)g.members.size(), g.nblocks,
-                                  g.thermal, b->bx, b->by, b->stream);
+                                  g.thermal, b->bx, b->by, b->stream, g.pair);
         ++b->launches;
         if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
         if (g.njobs > 0) {

@@ -120,6 +120,9 @@ KParams base_params(const lbm2d_solver* h) {
     p.pd.T_ref = h->T_ref;
     p.pf.T_ref = float(h->T_ref);
     p.nan_flag = h->d_nan;
+    p.pair = use_pair(h) ? 1 : 0;
+    const int nbw = h->bx * (p.pair ? 2 : 1);  // node width of a block
+    p.gx = (h->nx + nbw - 1) / nbw;
     const bool shifted = h->storage == ST_FP16 || h->storage == ST_BF16;
     for (int j = 0; j < 9; ++j) {
         p.shf[j] = shifted ? float(W[j]) : 0.0f;
@@ -248,10 +251,16 @@ int upload_geometry(lbm2d_solver* h) {
     return LBM2D_OK;
 }
 
+bool use_pair(const lbm2d_solver* h) {
+    return h->variant == 0 && (h->nx % 2 == 0) && !h->thermal && h->storage != ST_FP64;
+}
+
 int ensure_slots(lbm2d_solver* h) {
-    if (h->slot_bx == h->bx && h->slot_by == h->by && h->d_block_slot) return LBM2D_OK;
+    const int pair = use_pair(h) ? 1 : 0;
+    if (h->slot_bx == h->bx && h->slot_by == h->by && h->slot_pair == pair && h->d_block_slot) return LBM2D_OK;
     std::vector<int> slots;
-    h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx, h->by, slots);  // per-warp slots
+    h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx * (pair ? 2 : 1), h->by, h->bx * h->by,
+                                  slots);  // per-warp slots
     dfree(h, &h->d_block_slot);
     dfree(h, &h->d_partials);
     int rc;
@@ -262,6 +271,7 @@ int ensure_slots(lbm2d_solver* h) {
     CK(cudaStreamSynchronize(h->stream), "slots");
     h->slot_bx = h->bx;
     h->slot_by = h->by;
+    h->slot_pair = pair;
     return LBM2D_OK;
 }
 
@@ -357,7 +367,6 @@ int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p) {
     p.fout = h->P[h->cur ^ 1];
     p.gin = h->G[h->cur];
     p.gout = h->G[h->cur ^ 1];
-    p.gx = (h->nx + h->bx - 1) / h->bx;
     p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
     return LBM2D_OK;
 }
@@ -447,7 +456,8 @@ int lbm2d_destroy(lbm2d_solver* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
                     h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
-                    h->d_counter, h->d_last, h->d_nan, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy};
+                    h->d_counter, h->d_last, h->d_nan, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
+                    h->d_diag, h->d_prev_uv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
@@ -811,6 +821,28 @@ int lbm2d_download_macros(lbm2d_solver* h, double* rho, double* u, double* v, do
     return ret;
 }
 
+int lbm2d_diagnostics(lbm2d_solver* h, double* mass, double* mom_x, double* mom_y, double* residual) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (h->staged || h->steps_since_collide == 0) return fail(h, LBM2D_ERR_STATE, "no step since the last upload");
+    if ((rc = dalloc(h, &h->d_diag, 5 * sizeof(double)))) return rc;
+    if ((rc = dalloc(h, &h->d_prev_uv, h->N * 2 * sizeof(float)))) return rc;
+    CK(cudaMemsetAsync(h->d_diag, 0, 5 * sizeof(double), h->stream), "diag reset");
+    KParams p = rebuild_params(h);
+    const int e = launch_diagnostics(h->storage, p, h->d_diag, h->d_prev_uv, h->have_prev_uv ? 1 : 0, h->stream);
+    ++h->launches;
+    if (e) return cuda_fail(h, (cudaError_t)e, "diagnostics");
+    double acc[5];
+    CK(cudaMemcpyAsync(acc, h->d_diag, sizeof(acc), cudaMemcpyDeviceToHost, h->stream), "diag D2H");
+    CK(cudaStreamSynchronize(h->stream), "diag sync");
+    if (mass) *mass = acc[0];
+    if (mom_x) *mom_x = acc[1];
+    if (mom_y) *mom_y = acc[2];
+    if (residual) *residual = h->have_prev_uv && acc[4] > 0.0 ? std::sqrt(acc[3] / acc[4]) : NAN;
+    h->have_prev_uv = true;
+    return LBM2D_OK;
+}
+
 int lbm2d_download_wall_dist(lbm2d_solver* h, double* wd) {
     int rc;
     if ((rc = check_handle(h))) return rc;
@@ -873,6 +905,16 @@ int lbm2d_profile(lbm2d_solver* h, double* ms, long long* n) {
     if (ms) *ms = total;
     if (n) *n = (long long)(h->ev_used / 2);
     h->ev_used = 0;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_kernel_variant(lbm2d_solver* h, int variant) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (variant < 0 || variant > 1) return fail(h, LBM2D_ERR_INVALID, "unknown kernel variant");
+    if (variant == h->variant) return LBM2D_OK;
+    if ((rc = before_setting_change(h))) return rc;  // the stored state stays valid; rebuild for safety
+    h->variant = variant;
     return LBM2D_OK;
 }
 

@@ -200,7 +200,7 @@ bool build_geometry(const GeometryInput& in, GeometryTables& t, std::string& err
     return true;
 }
 
-int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, std::vector<int>& slots) {
+int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, int threads, std::vector<int>& slots) {
     const int gx = (nx + bx - 1) / bx, gy = (ny + by - 1) / by;
     slots.assign(static_cast<size_t>(gx) * gy, -1);
     for (size_t r = 0; r < t.rec_force.size(); ++r) {
@@ -209,7 +209,7 @@ int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, s
         const int x = id % nx, y = id / nx;
         slots[static_cast<size_t>(y / by) * gx + x / bx] = 0;
     }
-    const int warps = (bx * by + 31) / 32;  // each force block owns one slot per warp
+    const int warps = (threads + 31) / 32;  // each force block owns one slot per warp
     int k = 0;
     for (auto& s : slots)
         if (s == 0) {

@@ -59,6 +59,7 @@ bool build_geometry(const GeometryInput& in, GeometryTables& out, std::string& e
 // Force-reduction slots for a launch shape (bx, by): every block holding a
 // force node gets one slot per warp starting at slots[block] (-1 otherwise);
 // returns the total slot count.
-int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, std::vector<int>& slots);
+// (bx, by) is the node footprint of a block; threads its thread count.
+int force_block_slots(const GeometryTables& t, int nx, int ny, int bx, int by, int threads, std::vector<int>& slots);
 
 }  // namespace lbm2d

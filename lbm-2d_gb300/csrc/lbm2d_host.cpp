@@ -135,6 +135,41 @@ int lbm2d_wall_distance(int nx, int ny, const uint8_t* mask, double* wd) {
     return LBM2D_OK;
 }
 
+int lbm2d_force_stats(const double* v1, const double* v2, int n, double dt, lbm2d_force_stats_t* out) {
+    if (!v1 || !v2 || !out || n < 0) return LBM2D_ERR_INVALID;
+    int n_skip = static_cast<int>(n * 0.2);  // main(): skip the first 20% as transient
+    if (n_skip < 10) n_skip = 0;
+    double s1 = 0.0, s2 = 0.0;
+    const int m = n - n_skip;
+    for (int k = n_skip; k < n; ++k) {
+        s1 += v1[k];
+        s2 += v2[k];
+    }
+    out->mean_v1 = m > 0 ? s1 / m : NAN;
+    out->mean_v2 = m > 0 ? s2 / m : NAN;
+    double var = 0.0;
+    for (int k = n_skip; k < n; ++k) var += (v2[k] - out->mean_v2) * (v2[k] - out->mean_v2);
+    out->std_v2 = m > 0 ? std::sqrt(var / m) : NAN;
+    out->n_skip = n_skip;
+    // compute_strouhal: zero crossings of the mean after a 40% transient
+    out->st = NAN;
+    if (n >= 200) {
+        int skip = static_cast<int>(n * 0.4);
+        if (skip < 50) skip = 50;
+        const int len = n - skip;
+        if (len >= 100) {
+            double mean = 0.0;
+            for (int k = skip; k < n; ++k) mean += v2[k];
+            mean /= len;
+            int crossings = 0;
+            for (int k = skip + 1; k < n; ++k)
+                if (v2[k - 1] < mean && v2[k] >= mean) ++crossings;
+            if (crossings >= 2) out->st = crossings / (2.0 * (len * dt));
+        }
+    }
+    return LBM2D_OK;
+}
+
 int lbm2d_boundary_links(int nx, int ny, int case_type, const uint8_t* mask, const lbm2d_bb_geometry* geom,
                          int capacity, int32_t* node, int8_t* dir, int8_t* kind, double* q, double* uwx, double* uwy,
                          int8_t* counts_force, int* count) {

@@ -88,7 +88,8 @@ struct KParams {
     unsigned int* nan_flag;
     // solid nodes whose state can no longer change may skip their stores
     int skip_settled_solids;
-    int gx;  // width of the instance's block grid (batched launches)
+    int gx;    // width of the instance's block grid (batched launches)
+    int pair;  // 1: two x-neighbours per thread (nx even, non-thermal, not FP64)
 };
 
 // Readback outputs (any may be null).
@@ -117,8 +118,10 @@ int launch_prologue(int storage, const KParams& p, const double* f_aos, const do
 // block_start[] (ninst+1 entries, device memory) the first launch block of
 // each instance; nblocks = block_start[ninst].
 int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
-                      int bx, int by, void* stream);
+                      int bx, int by, void* stream, int pair);
 int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream);
+// acc[0..4] += mass, x/y momentum, sum |u - u_prev|^2, sum |u|^2 (FP64).
+int launch_diagnostics(int storage, const KParams& p, double* acc, float* prev_uv, int have_prev, void* stream);
 int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, double u, double v, double T,
                             void* stream);
 int launch_force_reduce(const double* partials, int nslots, double* hist, int hist_cap,

@@ -25,6 +25,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "lbm2d_internal.h"
 
 namespace lbm2d {
@@ -298,7 +300,9 @@ template <class R>
 __device__ __forceinline__ R wall_distance(const KParams& p, uint32_t fl) {
     if (fl & FLAG_BOUNDARY) return R(p.rec_wd[fl >> 2]);
     const uint32_t d = fl >> 2;
-    return d == WD_UNREACHED ? R(1e9) : R(d);
+    if (d == WD_UNREACHED) return R(1e9);
+    if (d < (1u << 23)) return R(__uint_as_float(0x4B000000u | d) - 8388608.0f);  // exact integer
+    return R(d);
 }
 
 // Collision of one fluid node: src/lbm.hpp:300-354 (mrt_collide :128-218,
@@ -316,8 +320,6 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
         const R sd = f5 + f6 + f7 + f8, sa = f1 + f2 + f3 + f4;
         R me = R(-4) * f0 - sa + R(2) * sd;
         R meps = R(4) * f0 - R(2) * sa + sd;
-        R mqx = R(-2) * f1 + R(2) * f3 + f5 - f6 - f7 + f8;
-        R mqy = R(-2) * f2 + R(2) * f4 + f5 + f6 - f7 - f8;
         R mpxx = f1 - f2 + f3 - f4;
         R mpxy = f5 - f6 + f7 - f8;
         const R jx = rho * u, jy = rho * v;
@@ -347,8 +349,9 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
         }
         me -= q.s_bulk * (me - e_eq);
         meps -= q.s_bulk * (meps - eps_eq);
-        mqx -= q.s_normal * (mqx + jx);
-        mqy -= q.s_normal * (mqy + jy);
+        // MRTParams::from_tau fixes s_normal = 1 (src/lbm_types.hpp:75): the
+        // energy-flux moments relax exactly to their equilibrium -j
+        const R mqx = -jx, mqy = -jy;
         mpxx -= s_eff * (mpxx - pxx_eq);
         mpxy -= s_eff * (mpxy - pxy_eq);
         // closed-form inverse transform (src/lbm.hpp:193-217), common terms shared
@@ -490,6 +493,209 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
     }
 }
 
+// ----------------------------------------------------------------- paired nodes
+// A thread owns two x-neighbours (x0, x0+1) with x0 even (nx even).  The
+// reference state of each node is rebuilt with the same per-node functions
+// as above; the collision runs on both nodes at once with Blackwell's packed
+// FP32x2 arithmetic (one FFMA2/FADD2/FMUL2 per operation pair) and the
+// populations are written as 8-byte (FP32) or 4-byte (FP16/BF16) pairs.
+struct F2 {
+    float2 v;
+};
+__device__ __forceinline__ F2 mk2(float a, float b) { return {make_float2(a, b)}; }
+__device__ __forceinline__ F2 sp2(float s) { return {make_float2(s, s)}; }
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return {__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return {__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return {__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ F2 rcp2(F2 a) { return mk2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y)); }
+__device__ __forceinline__ F2 sqrt2(F2 a) { return mk2(Fm<float>::sqrt(a.v.x), Fm<float>::sqrt(a.v.y)); }
+
+// Same operator as collide<float, false> on two nodes; lane k is collided
+// only when fluid_k (a solid lane keeps its value).
+__device__ __forceinline__ void collide_pair(const KParams& p, uint32_t fla, uint32_t flb, bool fa_ok, bool fb_ok,
+                                             F2 f[9]) {
+    const Phys<float>& q = p.pf;
+    const F2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    const F2 mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    const F2 my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    const F2 inv = rcp2(rho);
+    const F2 u = mx * inv, v = my * inv;
+    if ((fa_ok && (!(rho.v.x == rho.v.x) || rho.v.x == 0.0f)) || (fb_ok && (!(rho.v.y == rho.v.y) || rho.v.y == 0.0f)))
+        atomicOr(p.nan_flag, 1u);
+    F2 o[9];
+    if (p.collision == 0) {
+        const F2 sd = (f[5] + f[6]) + (f[7] + f[8]), sa = (f[1] + f[2]) + (f[3] + f[4]);
+        F2 me = fma2(sp2(2.0f), sd, fma2(sp2(-4.0f), f[0], sp2(0.0f) - sa));
+        F2 meps = fma2(sp2(4.0f), f[0], sd - sp2(2.0f) * sa);
+        F2 mpxx = (f[1] - f[2]) + (f[3] - f[4]);
+        F2 mpxy = (f[5] - f[6]) + (f[7] - f[8]);
+        const F2 jx = rho * u, jy = rho * v;
+        const F2 usq = fma2(u, u, v * v);
+        const F2 r3u = sp2(3.0f) * rho * usq;
+        const F2 e_eq = fma2(sp2(-2.0f), rho, r3u);
+        const F2 eps_eq = rho - r3u;
+        const F2 pxx_eq = rho * (u * u - v * v);
+        const F2 pxy_eq = jx * v;
+        F2 s_eff = sp2(q.s_shear);
+        if (p.les) {
+            F2 csq = sp2(q.cs_sq);
+            if (q.nu > 0.0f) {
+                const F2 wd = mk2(wall_distance<float>(p, fla), wall_distance<float>(p, flb));
+                const F2 yp = wd * sqrt2(usq + sp2(1e-12f)) * sp2(q.inv_nu);
+                const float dxa = yp.v.x > 0.0f ? q.cs * (1.0f - __expf(-yp.v.x * (1.0f / 26.0f))) : 0.0f;
+                const float dxb = yp.v.y > 0.0f ? q.cs * (1.0f - __expf(-yp.v.y * (1.0f / 26.0f))) : 0.0f;
+                csq = mk2(yp.v.x > 0.0f ? dxa * dxa : q.cs_sq, yp.v.y > 0.0f ? dxb * dxb : q.cs_sq);
+            }
+            const F2 a = mpxx - pxx_eq, b = mpxy - pxy_eq;
+            const F2 Q = sqrt2(sp2(2.0f) * fma2(a, a, b * b));
+            const F2 A = sp2(4.5f) * csq * Q * inv;
+            const F2 te2 = sp2(q.tau) + sqrt2(fma2(sp2(q.tau), sp2(q.tau), sp2(4.0f) * A));
+            const F2 s2 = sp2(2.0f) * rcp2(te2);
+            s_eff = mk2(clamp_rate<float>(s2.v.x), clamp_rate<float>(s2.v.y));
+        }
+        const F2 sb = sp2(q.s_bulk);
+        me = me - sb * (me - e_eq);
+        meps = meps - sb * (meps - eps_eq);
+        mpxx = mpxx - s_eff * (mpxx - pxx_eq);
+        mpxy = mpxy - s_eff * (mpxy - pxy_eq);
+        // s_normal = 1: the energy-flux moments relax to -j (see collide)
+        const F2 a0 = sp2(1.0f / 9.0f) * rho;
+        const F2 ax = a0 - sp2(1.0f / 36.0f) * me - sp2(1.0f / 18.0f) * meps;
+        const F2 ad = fma2(sp2(1.0f / 18.0f), me, fma2(sp2(1.0f / 36.0f), meps, a0));
+        const F2 hx = sp2(1.0f / 3.0f) * jx, hy = sp2(1.0f / 3.0f) * jy;  // (j - q)/6 with q = -j
+        const F2 dx = sp2(1.0f / 12.0f) * jx, dy = sp2(1.0f / 12.0f) * jy;  // j/6 + q/12 with q = -j
+        const F2 px = sp2(0.25f) * mpxx, py = sp2(0.25f) * mpxy;
+        o[0] = a0 - sp2(1.0f / 9.0f) * (me - meps);
+        o[1] = ax + hx + px;
+        o[2] = ax + hy - px;
+        o[3] = ax - hx + px;
+        o[4] = ax - hy - px;
+        o[5] = ad + dx + dy + py;
+        o[6] = ad - dx + dy - py;
+        o[7] = ad - dx - dy + py;
+        o[8] = ad + dx - dy - py;
+    } else {
+        const F2 it = sp2(q.inv_tau), usq = fma2(u, u, v * v);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const F2 ed = sp2(float(CXf(i))) * u + sp2(float(CYf(i))) * v;
+            const F2 poly = fma2(sp2(4.5f) * ed, ed, fma2(sp2(3.0f), ed, sp2(1.0f))) - sp2(1.5f) * usq;
+            const F2 fe = sp2(float(wgt(i))) * rho * poly;
+            o[i] = f[i] - it * (f[i] - fe);
+        }
+    }
+    if (q.Fscale != 0.0f) {
+        const F2 fa = sp2((1.0f / 9.0f) * q.Fscale), fd = sp2((1.0f / 36.0f) * q.Fscale);
+        o[1] = o[1] + fa;
+        o[3] = o[3] - fa;
+        o[5] = o[5] + fd;
+        o[6] = o[6] - fd;
+        o[7] = o[7] - fd;
+        o[8] = o[8] + fd;
+    }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) f[j] = mk2(fa_ok ? o[j].v.x : f[j].v.x, fb_ok ? o[j].v.y : f[j].v.y);
+}
+
+template <class T>
+struct PairStore;
+template <>
+struct PairStore<float> {
+    static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, float) {
+        *reinterpret_cast<float2*>(p + i) = make_float2(a, b);
+    }
+};
+template <>
+struct PairStore<__half> {
+    static __device__ __forceinline__ void st(__half* p, size_t i, float a, float b, float sh) {
+        *reinterpret_cast<__half2*>(p + i) = __floats2half2_rn(a - sh, b - sh);
+    }
+};
+template <>
+struct PairStore<__nv_bfloat16> {
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, size_t i, float a, float b, float sh) {
+        *reinterpret_cast<__nv_bfloat162*>(p + i) = __floats2bfloat162_rn(a - sh, b - sh);
+    }
+};
+
+// One step of the paired block (bxi, byi) of an instance whose paired block
+// grid is gx wide (non-thermal, FP32/FP16/BF16 storage, nx even).
+template <class T>
+__device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int byi, int gx) {
+    const int x0 = 2 * (bxi * blockDim.x + threadIdx.x);
+    const int y = byi * blockDim.y + threadIdx.y;
+    float fxs = 0.0f, fys = 0.0f;
+    if (x0 < p.nx && y < p.ny) {
+        const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
+        const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
+        float fa[9], fb[9], ga[9], gb[9];
+        build_state<T, false>(p, x0, y, fl.x, fa, ga);
+        build_state<T, false>(p, x0 + 1, y, fl.y, fb, gb);
+        const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
+        if ((fl.x | fl.y) & FLAG_BOUNDARY) {
+            // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
+            const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
+            const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+#pragma unroll
+            for (int j = 1; j < 9; ++j) {
+                if (ma & (1u << j)) {
+                    fxs -= float(CXf(j)) * 2.0f * fa[j];
+                    fys -= float(CYf(j)) * 2.0f * fa[j];
+                }
+                if (mb & (1u << j)) {
+                    fxs -= float(CXf(j)) * 2.0f * fb[j];
+                    fys -= float(CYf(j)) * 2.0f * fb[j];
+                }
+            }
+        }
+        if (oka || okb) {
+            F2 f[9];
+#pragma unroll
+            for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
+            collide_pair(p, fl.x, fl.y, oka, okb, f);
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                fa[j] = f[j].v.x;
+                fb[j] = f[j].v.y;
+            }
+        }
+        const bool settled = p.skip_settled_solids && y < p.ny - 1;
+        const bool skip_a = !oka && settled && x0 > 0;
+        const bool skip_b = !okb && settled && x0 + 1 < p.nx - 1;
+        if (!(skip_a && skip_b)) {
+            T* __restrict__ Fo = static_cast<T*>(p.fout);
+            const size_t N = (size_t)p.N;
+#pragma unroll
+            for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], p.shf[j]);
+        }
+    }
+    if (p.block_slot) {
+        const int base = p.block_slot[byi * gx + bxi];
+        if (base >= 0) {
+            float a = fxs, b = fys;
+            if (__any_sync(0xffffffffu, a != 0.0f || b != 0.0f)) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    a += __shfl_down_sync(0xffffffffu, a, o);
+                    b += __shfl_down_sync(0xffffffffu, b, o);
+                }
+            }
+            const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+            if ((tid & 31) == 0) {
+                const int slot = base + (tid >> 5);
+                p.partials[2 * slot] = double(a);
+                p.partials[2 * slot + 1] = double(b);
+            }
+        }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(512) step_pair_kernel(const KParams p) {
+    step_pair_block<T>(p, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
 template <class T, bool TH>
 __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
     step_block<T, TH>(p, blockIdx.x, blockIdx.y, gridDim.x);
@@ -529,6 +735,37 @@ __global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restri
     __syncthreads();
     const int local = b - block_start[k];
     step_block<T, TH>(sp, local % sp.gx, local / sp.gx, sp.gx);
+}
+
+template <class T>
+__global__ void __launch_bounds__(512) batch_step_pair_kernel(const KParams* __restrict__ inst,
+                                                              const int* __restrict__ block_start, int ninst) {
+    __shared__ KParams sp;
+    __shared__ int s_inst;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
+    if (tid == 0) {
+        int lo = 0, hi = ninst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (block_start[mid] <= b)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        s_inst = lo;
+    }
+    __syncthreads();
+    const int k = s_inst;
+    {
+        const int* src = reinterpret_cast<const int*>(inst + k);
+        int* dst = reinterpret_cast<int*>(&sp);
+        const int nw = (int)(sizeof(KParams) / sizeof(int));
+        for (int w = tid; w < nw; w += blockDim.x * blockDim.y) dst[w] = src[w];
+    }
+    __syncthreads();
+    const int local = b - block_start[k];
+    step_pair_block<T>(sp, local % sp.gx, local / sp.gx, sp.gx);
 }
 
 template <class T, bool TH>
@@ -614,6 +851,77 @@ __global__ void fill_equilibrium_kernel(double* __restrict__ fa, double* __restr
     }
 }
 
+// FP64 diagnostics over the fluid nodes of the rebuilt reference state:
+// total mass, momentum, and the squared velocity change against (and update
+// of) the previous velocity field kept in prev_uv (2 floats per node).
+template <class T, bool TH>
+__global__ void diagnostics_kernel(const KParams p, double* __restrict__ acc, float* __restrict__ prev_uv,
+                                   int have_prev) {
+    using R = typename Pop<T>::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    double m = 0.0, jx = 0.0, jy = 0.0, du2 = 0.0, u2 = 0.0;
+    if (x < p.nx && y < p.ny) {
+        const size_t n = (size_t)y * p.nx + x;
+        const uint32_t fl = p.flags[n];
+        if (!(fl & FLAG_SOLID)) {
+            R f[9], g[9];
+            build_state<T, TH>(p, x, y, fl, f, g);
+            double rho = 0.0, mx = 0.0, my = 0.0;
+            for (int j = 0; j < 9; ++j) {
+                rho += double(f[j]);
+                mx += double(f[j]) * CXf(j);
+                my += double(f[j]) * CYf(j);
+            }
+            m = rho;
+            jx = mx;
+            jy = my;
+            const float u = float(mx / rho), v = float(my / rho);
+            if (have_prev) {
+                const double a = double(u) - prev_uv[2 * n], b = double(v) - prev_uv[2 * n + 1];
+                du2 = a * a + b * b;
+            }
+            u2 = double(u) * u + double(v) * v;
+            prev_uv[2 * n] = u;
+            prev_uv[2 * n + 1] = v;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_down_sync(0xffffffffu, m, o);
+        jx += __shfl_down_sync(0xffffffffu, jx, o);
+        jy += __shfl_down_sync(0xffffffffu, jy, o);
+        du2 += __shfl_down_sync(0xffffffffu, du2, o);
+        u2 += __shfl_down_sync(0xffffffffu, u2, o);
+    }
+    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31) == 0) {
+        atomicAdd(acc + 0, m);
+        atomicAdd(acc + 1, jx);
+        atomicAdd(acc + 2, jy);
+        atomicAdd(acc + 3, du2);
+        atomicAdd(acc + 4, u2);
+    }
+}
+
+// Prologue of a paired solver: the same packed collision as step_pair_block,
+// so a re-collided state (parameter change, autotuner restore) rounds exactly
+// as the steps do.
+template <class T>
+__global__ void prologue_pair_kernel(const KParams p, const double* __restrict__ fa) {
+    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x0 >= p.nx || y >= p.ny) return;
+    const size_t n0 = (size_t)y * p.nx + x0;
+    const uint32_t fla = p.flags[n0], flb = p.flags[n0 + 1];
+    const bool oka = !(fla & FLAG_SOLID), okb = !(flb & FLAG_SOLID);
+    F2 f[9];
+    for (int j = 0; j < 9; ++j) f[j] = mk2(float(fa[n0 * 9 + j]), float(fa[(n0 + 1) * 9 + j]));
+    if (oka || okb) collide_pair(p, fla, flb, oka, okb, f);
+    T* Fo = static_cast<T*>(p.fout);
+    const size_t N = (size_t)p.N;
+    for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, f[j].v.x, f[j].v.y, p.shf[j]);
+}
+
 // Deterministic second stage of the force reduction: one block sums the
 // per-block partials in a fixed order and appends (fx, fy) to the history.
 __global__ void force_reduce_kernel(const double* __restrict__ part, int nslots, double* hist, int cap,
@@ -659,9 +967,16 @@ __global__ void batch_force_reduce_kernel(const ReduceJob* __restrict__ jobs) {
 
 template <class T>
 int launch_batch_t(const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal, int bx, int by,
-                   cudaStream_t s) {
+                   cudaStream_t s, int pair) {
     if (nblocks <= 0 || ninst <= 0) return 0;
     dim3 blk(bx, by);
+    if (pair) {
+        if constexpr (!std::is_same<T, double>::value) {
+            batch_step_pair_kernel<T><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
+            return (int)cudaGetLastError();
+        }
+        return (int)cudaErrorInvalidValue;
+    }
     if (thermal)
         batch_step_kernel<T, true><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
     else
@@ -671,6 +986,14 @@ int launch_batch_t(const KParams* inst, const int* block_start, int ninst, int n
 
 template <class T>
 int launch_step_t(const KParams& p, int bx, int by, cudaStream_t s) {
+    if (p.pair) {
+        if constexpr (!std::is_same<T, double>::value) {
+            dim3 blk(bx, by), grd((p.nx / 2 + bx - 1) / bx, (p.ny + by - 1) / by);
+            step_pair_kernel<T><<<grd, blk, 0, s>>>(p);
+            return (int)cudaGetLastError();
+        }
+        return (int)cudaErrorInvalidValue;
+    }
     dim3 blk(bx, by), grd((p.nx + bx - 1) / bx, (p.ny + by - 1) / by);
     if (p.thermal)
         step_kernel<T, true><<<grd, blk, 0, s>>>(p);
@@ -691,6 +1014,14 @@ int launch_readback_t(const KParams& p, const ROut& o, cudaStream_t s) {
 
 template <class T>
 int launch_prologue_t(const KParams& p, const double* fa, const double* ga, cudaStream_t s) {
+    if (p.pair) {
+        if constexpr (!std::is_same<T, double>::value) {
+            dim3 blk(128, 2), grd((p.nx / 2 + 127) / 128, (p.ny + 1) / 2);
+            prologue_pair_kernel<T><<<grd, blk, 0, s>>>(p, fa);
+            return (int)cudaGetLastError();
+        }
+        return (int)cudaErrorInvalidValue;
+    }
     dim3 blk(128, 2), grd((p.nx + 127) / 128, (p.ny + 1) / 2);
     if (p.thermal)
         prologue_kernel<T, true><<<grd, blk, 0, s>>>(p, fa, ga);
@@ -735,13 +1066,13 @@ int launch_prologue(int storage, const KParams& p, const double* fa, const doubl
 }
 
 int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
-                      int bx, int by, void* stream) {
+                      int bx, int by, void* stream, int pair) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (storage) {
-        case ST_FP32: return launch_batch_t<float>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
-        case ST_FP16: return launch_batch_t<__half>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
-        case ST_BF16: return launch_batch_t<__nv_bfloat16>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
-        case ST_FP64: return launch_batch_t<double>(inst, block_start, ninst, nblocks, thermal, bx, by, s);
+        case ST_FP32: return launch_batch_t<float>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
+        case ST_FP16: return launch_batch_t<__half>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
+        case ST_BF16: return launch_batch_t<__nv_bfloat16>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
+        case ST_FP64: return launch_batch_t<double>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
     }
     return (int)cudaErrorInvalidValue;
 }
@@ -749,6 +1080,27 @@ int launch_batch_step(int storage, const KParams* inst, const int* block_start, 
 int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream) {
     if (njobs <= 0) return 0;
     batch_force_reduce_kernel<<<njobs, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
+    return (int)cudaGetLastError();
+}
+
+int launch_diagnostics(int storage, const KParams& p, double* acc, float* prev_uv, int have_prev, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dim3 blk(128, 2), grd((p.nx + 127) / 128, (p.ny + 1) / 2);
+#define LBM2D_DIAG(T)                                                                        \
+    do {                                                                                     \
+        if (p.thermal)                                                                       \
+            diagnostics_kernel<T, true><<<grd, blk, 0, s>>>(p, acc, prev_uv, have_prev);     \
+        else                                                                                 \
+            diagnostics_kernel<T, false><<<grd, blk, 0, s>>>(p, acc, prev_uv, have_prev);    \
+    } while (0)
+    switch (storage) {
+        case ST_FP32: LBM2D_DIAG(float); break;
+        case ST_FP16: LBM2D_DIAG(__half); break;
+        case ST_BF16: LBM2D_DIAG(__nv_bfloat16); break;
+        case ST_FP64: LBM2D_DIAG(double); break;
+        default: return (int)cudaErrorInvalidValue;
+    }
+#undef LBM2D_DIAG
     return (int)cudaGetLastError();
 }
 

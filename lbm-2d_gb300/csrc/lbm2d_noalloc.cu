@@ -61,7 +61,7 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
     // built the force-slot table for the current launch shape.
     const CollideParams c = collide_params(h, tau);
     if (h->staged || h->geom_dirty || !(c == h->cp_of_P) || h->slot_bx != h->bx || h->slot_by != h->by ||
-        !h->d_block_slot)
+        h->slot_pair != (use_pair(h) ? 1 : 0) || !h->d_block_slot)
         return fail(h, LBM2D_ERR_STATE,
                     "lbm2d_step_noalloc needs a solver prepared by lbm2d_step with the same tau and settings");
     if (h->nslots > kNoAllocMaxSlots)
@@ -79,7 +79,6 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
     // Every slot in [0, nslots) is written by exactly one warp before the
     // reduction reads it, so the shared array needs no clearing between calls.
     p.partials = scratch;
-    p.gx = (h->nx + h->bx - 1) / h->bx;
     for (int k = 0; k < nsteps; ++k) {
         p.fin = h->P[h->cur];
         p.fout = h->P[h->cur ^ 1];

@@ -72,7 +72,7 @@ struct lbm2d_solver {
     double* d_rec_uw = nullptr;
     double* d_partials = nullptr;
     int* d_block_slot = nullptr;
-    int nslots = 0, slot_bx = 0, slot_by = 0;
+    int nslots = 0, slot_bx = 0, slot_by = 0, slot_pair = -1;
     double* d_hist = nullptr;
     int hist_cap = 1 << 18;
     unsigned long long* d_counter = nullptr;
@@ -81,6 +81,9 @@ struct lbm2d_solver {
     double* d_stage_f = nullptr;
     double* d_stage_g = nullptr;
     double* d_fx = nullptr;
+    double* d_diag = nullptr;    // 5 FP64 accumulators
+    float* d_prev_uv = nullptr;  // velocity field of the last residual check
+    bool have_prev_uv = false;
     double* d_fy = nullptr;
     size_t device_bytes = 0;
 
@@ -94,6 +97,7 @@ struct lbm2d_solver {
     long long steps_done = 0;
     long long launches = 0;
     int bx = 128, by = 2;
+    int variant = 0;  // 0: paired kernel where possible, 1: one node per thread
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;  // even/odd = start/stop
     size_t ev_used = 0;
@@ -120,6 +124,9 @@ int materialize(lbm2d_solver* h);
 int before_setting_change(lbm2d_solver* h);
 int prologue(lbm2d_solver* h, const CollideParams& c);
 int check_handle(lbm2d_solver* h);
+// Two x-neighbours per thread (packed FP32x2 collision) when nx is even and
+// the step is non-thermal FP32/FP16/BF16.
+bool use_pair(const lbm2d_solver* h);
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
 // kernel parameters of the next step (fin = current buffer); returns status.
 int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p);

@@ -171,7 +171,11 @@ void record(lbm2d_server* s, const Active& a, int status) {
     res.t_submit = a.t_submit;
     res.t_admit = a.t_admit;
     res.t_done = now_s();
-    res.steps = a.req.steps - a.left;
+    res.steps = 0;  // the steps the solver actually took
+    if (a.h) {
+        lbm2d_info info{};
+        if (lbm2d_get_info(a.h, &info) == LBM2D_OK) res.steps = info.steps_done;
+    }
     res.nodes = (long long)a.req.nx * a.req.ny;
     if (a.h && status == LBM2D_OK) lbm2d_force_sums(a.h, &res.fx, &res.fy);
     std::lock_guard<std::mutex> lock(s->mu);
@@ -229,16 +233,19 @@ void worker_loop(lbm2d_server* s) {
         }
         long long k = s->steps_per_tick;
         for (auto& a : s->active) k = std::min(k, a.left);
+        // the members of this tick; arrivals admitted below join the next one
+        const size_t n_tick = s->active.size();
         const double t0 = now_s();
         int rc = lbm2d_batch_step(s->batch, (int)k);
         admit(s);  // host set-up of new arrivals overlaps the GPU work
         if (!rc) rc = lbm2d_batch_synchronize(s->batch);
         s->busy_s += now_s() - t0;
-        for (auto& a : s->active) {
+        for (size_t i = 0; i < n_tick; ++i) {
+            Active& a = s->active[i];
             a.left -= k;
             s->lattice_updates += k * (long long)a.req.nx * a.req.ny;
         }
-        for (size_t i = s->active.size(); i-- > 0;) {
+        for (size_t i = n_tick; i-- > 0;) {
             Active& a = s->active[i];
             if (a.left <= 0 || rc) {
                 int st = rc;

@@ -292,6 +292,27 @@ inline void save_forces_jsonl(const std::string& output_dir, int step, double cd
     out << "{\"step\":" << step << ",\"cd\":" << cd << ",\"cl\":" << cl << "}\n";
 }
 
+// Batched form of the per-step forces.jsonl stream (src/lbm.hpp:822-834 as
+// called by src/main.cpp:106-122): the drag/lift sums of every step since the
+// last upload are kept on the device; this reads them back once and writes
+// the same lines the driver's per-step loop writes, with Cd, Cl =
+// 2 F / (D u^2) (length_scale = 0 writes the raw sums, as the step, hills and
+// canyon drivers do).  Returns the number of lines written.
+inline int save_forces_history_jsonl(LBMCapabilities& sys, const std::string& output_dir, int first_step,
+                                     double length_scale, double u_ref) {
+    int n = 0;
+    if (!sys.handle() || lbm2d_force_history(sys.handle(), nullptr, nullptr, 0, &n) != LBM2D_OK || n <= 0) return 0;
+    std::vector<double> fx(n), fy(n);
+    lbm2d_force_history(sys.handle(), fx.data(), fy.data(), n, &n);
+    const double k = length_scale > 0.0 ? 2.0 / (length_scale * u_ref * u_ref) : 1.0;
+    std::ofstream out(output_dir + "/forces.jsonl", std::ios::trunc);
+    out.precision(6);
+    out << std::fixed;
+    for (int s = 0; s < n; ++s)
+        out << "{\"step\":" << first_step + s << ",\"cd\":" << k * fx[s] << ",\"cl\":" << k * fy[s] << "}\n";
+    return n;
+}
+
 // src/lbm.hpp:839-855
 inline void save_meta_json(const std::string& output_dir, double re, double tau, double u_inflow,
                            double length_scale, const std::string& shape_type, int nx, int ny) {

@@ -69,6 +69,11 @@ class ServerStats(C.Structure):
                 ("device_bytes_in_use", C.c_double)]
 
 
+class ForceStats(C.Structure):
+    _fields_ = [("mean_v1", C.c_double), ("mean_v2", C.c_double), ("std_v2", C.c_double), ("st", C.c_double),
+                ("n_skip", C.c_int)]
+
+
 GEOM_CAVITY, GEOM_STEP, GEOM_CYLINDER, GEOM_SIDE_BY_SIDE, GEOM_HEATED_CAVITY = range(5)
 
 _D, _I, _P = C.c_double, C.c_int, C.c_void_p
@@ -104,9 +109,11 @@ _SIGS = {
     "lbm2d_download_force_field": ([_P, _DP, _DP], _I),
     "lbm2d_download_macros": ([_P, _DP, _DP, _DP, _DP], _I),
     "lbm2d_download_wall_dist": ([_P, _DP], _I),
+    "lbm2d_diagnostics": ([_P, _DP, _DP, _DP, _DP], _I),
     "lbm2d_synchronize": ([_P], _I),
     "lbm2d_get_info": ([_P, C.POINTER(Info)], _I),
     "lbm2d_set_block": ([_P, _I, _I], _I),
+    "lbm2d_set_kernel_variant": ([_P, _I], _I),
     "lbm2d_stream": ([_P], _P),
     "lbm2d_set_profiling": ([_P, _I], _I),
     "lbm2d_profile": ([_P, _DP, C.POINTER(C.c_longlong)], _I),
@@ -140,6 +147,7 @@ _SIGS = {
     "lbm2d_naca_coords": ([_I, _I, _DP], _I),
     "lbm2d_transform_points": ([_DP, _I, _D, _D, _D, _D], _I),
     "lbm2d_wall_distance": ([_I, _I, _U8P, _DP], _I),
+    "lbm2d_force_stats": ([_DP, _DP, _I, _D, C.POINTER(ForceStats)], _I),
     "lbm2d_boundary_links": ([_I, _I, _I, _U8P, C.POINTER(BBGeometry), _I, C.POINTER(C.c_int32),
                               C.POINTER(C.c_int8), C.POINTER(C.c_int8), _DP, _DP, _DP,
                               C.POINTER(C.c_int8), C.POINTER(_I)], _I),
@@ -205,6 +213,24 @@ def transform_points(xy, cx, cy, scale, angle_deg) -> np.ndarray:
 def point_in_polygon(px, py, xy) -> bool:
     a = np.ascontiguousarray(xy, np.float64).reshape(-1)
     return bool(lib().lbm2d_point_in_polygon(float(px), float(py), _d(a), len(a) // 2))
+
+
+def force_stats(v1, v2, dt=1.0) -> dict:
+    """Mean Cd/Cl (or Fx/Fy), std of the lift and the shedding frequency, as
+    the reference's post-processing computes them."""
+    a = np.ascontiguousarray(v1, np.float64)
+    b = np.ascontiguousarray(v2, np.float64)
+    st = ForceStats()
+    rc = lib().lbm2d_force_stats(_d(a), _d(b), len(a), float(dt), C.byref(st))
+    if rc:
+        raise LBMError(rc, "force_stats")
+    return {k: getattr(st, k) for k, _ in ForceStats._fields_}
+
+
+def drag_lift_coefficients(fx, fy, length_scale, u):
+    """Cd, Cl = 2 F / (D u^2) as the cylinder driver normalises (src/main.cpp:112-115)."""
+    k = 2.0 / (length_scale * u * u)
+    return np.asarray(fx) * k, np.asarray(fy) * k
 
 
 def wall_distance(nx, ny, mask) -> np.ndarray:
@@ -348,6 +374,10 @@ class Solver:
     def set_block(self, bx, by):
         self._ck(self.L.lbm2d_set_block(self.h, int(bx), int(by)))
 
+    def set_kernel_variant(self, variant: int):
+        """0: paired nodes per thread where possible (default), 1: one node per thread."""
+        self._ck(self.L.lbm2d_set_kernel_variant(self.h, int(variant)))
+
     # -- state
     def upload_f(self, f):
         a = np.ascontiguousarray(f, np.float64).reshape(-1)
@@ -420,6 +450,12 @@ class Solver:
         T = np.empty(n) if thermal else None
         self._ck(self.L.lbm2d_download_macros(self.h, _d(rho), _d(u), _d(v), _d(T) if thermal else None))
         return (rho, u, v, T) if thermal else (rho, u, v)
+
+    def diagnostics(self):
+        """(mass, momentum x, momentum y, residual) in FP64 over fluid nodes."""
+        m, a, b, r = _D(), _D(), _D(), _D()
+        self._ck(self.L.lbm2d_diagnostics(self.h, C.byref(m), C.byref(a), C.byref(b), C.byref(r)))
+        return m.value, a.value, b.value, r.value
 
     @property
     def wall_dist(self):

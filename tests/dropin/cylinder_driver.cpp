@@ -57,5 +57,7 @@ int main(int argc, char** argv) {
     std::fclose(fo);
     // the output writers read the mirrors (downloaded lazily)
     save_json_frame(system, steps, "dropin_out");
-    return 0;
+    // the per-step drag/lift stream, read back once from the device history
+    const int lines = save_forces_history_jsonl(system, "dropin_out", 0, NY / 5.0, u);
+    return lines == (g_case == CaseType::CAVITY ? 0 : steps) ? 0 : 5;
 }

@@ -96,6 +96,8 @@ def test_autotune_preserves_state(product, oracle_lib):
     fx, _ = s.force_history()
     rfx, _ = ref.force_history()
     assert np.array_equal(s.f, ref.f)
-    assert len(fx) == 10 and np.allclose(fx, rfx, rtol=1e-12)
+    # the tuned shape groups nodes into warps differently: the FP32 per-warp
+    # partial sums of the force round differently
+    assert len(fx) == 10 and np.allclose(fx, rfx, rtol=1e-6)
     s.close()
     ref.close()

@@ -52,4 +52,10 @@ def test_dropin_driver_matches_oracle(product, oracle_lib, tmp_path, case):
     if case == "cylinder":
         assert rel_l2(got_sums, np.array(sums)) < 1e-5
     assert os.path.exists(tmp_path / "dropin_out" / "frames" / f"frame_{steps}.json")
+    if case == "cylinder":  # forces.jsonl from the device history: Cd = 2 Fx / (D u^2)
+        import json
+        rows = [json.loads(line) for line in open(tmp_path / "dropin_out" / "forces.jsonl")]
+        assert len(rows) == steps
+        k = 2.0 / ((ny / 5.0) * u * u)
+        assert abs(rows[-1]["cd"] - k * sums[-1][0]) <= 1e-5 * abs(k * sums[-1][0]) + 1e-6
     s.close()

@@ -26,8 +26,9 @@ TOL = {"fp64": 1e-11, "fp32": 1e-5, "fp16": 5e-3, "bf16": 3e-2}
 FORCE_TOL = {"fp64": 1e-10, "fp32": 1e-5, "fp16": 2e-2, "bf16": 1e-1}
 
 
-def run(product, O, spec, storage):
+def run(product, O, spec, storage, variant=0):
     g = gpu_solver(product, O, spec, storage)
+    g.set_kernel_variant(variant)
     sums = []
     for _ in range(spec["steps"]):
         g.step(spec["tau"], spec["u"])
@@ -44,12 +45,14 @@ def run(product, O, spec, storage):
     return out
 
 
-@pytest.mark.parametrize("storage", ["fp64", "fp32"])
+@pytest.mark.parametrize("storage,variant", [("fp64", 0), ("fp32", 0), ("fp32", 1)])
 @pytest.mark.parametrize("name", sorted(CS.CASES))
-def test_gpu_matches_reference(product, oracle_lib, name, storage):
+def test_gpu_matches_reference(product, oracle_lib, name, storage, variant):
+    """variant 0: paired nodes per thread (packed FP32x2) where possible;
+    variant 1: one node per thread."""
     spec = CS.CASES[name]
     gold = np.load(os.path.join(GOLD, f"{name}.npz"))
-    got = run(product, oracle_lib, spec, storage)
+    got = run(product, oracle_lib, spec, storage, variant)
     fm = fluid_pop_mask(gold["mask"])
     tol = TOL[storage]
     assert rel_l2(got["f"], gold["f"], fm) < tol
@@ -76,12 +79,13 @@ def test_gpu_matches_reference(product, oracle_lib, name, storage):
         assert np.array_equal(got["hist"], got["sums"])
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("storage", ["fp16", "bf16"])
-@pytest.mark.parametrize("name", ["cavity_mrt", "cylinder_mei", "ribs_les", "thermal_cavity"])
-def test_gpu_shifted_storage_bounds(product, oracle_lib, name, storage):
+@pytest.mark.parametrize("name", ["cavity_mrt", "cylinder_mei", "ribs_les", "thermal_cavity", "step"])
+def test_gpu_shifted_storage_bounds(product, oracle_lib, name, storage, variant):
     spec = CS.CASES[name]
     gold = np.load(os.path.join(GOLD, f"{name}.npz"))
-    got = run(product, oracle_lib, spec, storage)
+    got = run(product, oracle_lib, spec, storage, variant)
     fm = fluid_pop_mask(gold["mask"])
     assert rel_l2(got["f"], gold["f"], fm) < TOL[storage]
 
@@ -99,6 +103,31 @@ def test_mass_conservation_800x300(product):
     m1 = s.f[fluid].sum()
     s.close()
     assert abs(m1 - m0) < 0.01 * m0
+
+
+def test_device_diagnostics(product, oracle_lib):
+    """Mass/momentum reductions (FP64 on the device) against the oracle's
+    state, and the steady-state residual shrinking as a cavity converges."""
+    spec = CS.CASES["cavity_mrt"]
+    s = oracle_lib.Solver(spec["nx"], spec["ny"])
+    CS.apply_setup(s, spec)
+    g = gpu_solver(product, oracle_lib, spec, "fp64")
+    s.step(spec["tau"], spec["u"], 30)
+    g.step(spec["tau"], spec["u"], 30)
+    m, jx, jy, r0 = g.diagnostics()
+    f = s.f.reshape(-1, 9)[s.obstacle == 0]
+    cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+    cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+    assert abs(m - f.sum()) < 1e-12 * f.sum()
+    assert abs(jx - (f @ cx).sum()) < 1e-11 and abs(jy - (f @ cy).sum()) < 1e-11
+    assert np.isnan(r0)
+    res = []
+    for _ in range(4):
+        g.step(spec["tau"], spec["u"], 200)
+        res.append(g.diagnostics()[3])
+    assert all(np.isfinite(res)) and res[-1] < res[0]
+    s.close()
+    g.close()
 
 
 def test_parameter_change_between_steps(product, oracle_lib):
