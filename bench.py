@@ -56,6 +56,12 @@ def workload_name(nx, ny):
 
 WORKLOAD = workload_name(NX, NY)
 
+# lbm2d_info.kernel -> (kernel function, description)
+KERNEL_NAMES = {0: ("step_kernel", "one node per thread"),
+                1: ("step_pair_kernel", "two x-neighbours per thread, packed FP32x2, register pulls"),
+                2: ("step_rows_kernel", "row tiles staged by cp.async.bulk into shared memory, persistent grid, "
+                                        "packed FP32x2")}
+
 
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -316,7 +322,11 @@ def run_serve(args):
     lat = np.array([x["t_done"] - x["t_submit"] for x in res])
     lu = sum(x["steps"] * x["nodes"] for x in res)
     span = max(x["t_done"] for x in res) - min(x["t_submit"] for x in res)
-    serve = {"requests": len(res), "failed": int(sum(1 for x in res if x["status"] != 0)),
+    status = {}
+    for x in res:
+        status[str(x["status"])] = status.get(str(x["status"]), 0) + 1
+    serve = {"requests": len(res), "failed": int(sum(1 for x in res if x["status"] != 0)), "status": status,
+             "ticks": st["ticks"], "mean_solves_per_tick": st["member_ticks"] / max(st["ticks"], 1),
              "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
              "mean_s": float(lat.mean()), "makespan_s": span, "glups": lu / span / 1e9,
              "busy_glups": st["lattice_updates"] / max(st["busy_s"], 1e-9) / 1e9, "lattice_updates": lu}
@@ -581,7 +591,7 @@ def main():
         clocks.active = False
         ms = reps.max(ms)
         info = s.info()
-        results[label] = dict(ms=ms, kernel_ms=kms, launches=launches, nan=nan,
+        results[label] = dict(ms=ms, kernel_ms=kms, launches=launches, nan=nan, kernel=info.kernel,
                                 bytes_per_update=info.bytes_per_update, boundary=info.n_boundary_nodes,
                                 force_nodes=info.n_force_nodes, block=(info.block_x, info.block_y))
         if label == storages[0] and not nan:
@@ -626,6 +636,7 @@ def main():
         b = 2 * 9 * lbm2d.BYTES_PER_POP[st]
         kach = nodes * b / (r["kernel_ms"] * 1e-3) / 1e9
         prec[label] = {"glups": g, "vs_" + main_st: g / value, "kernel_ms": r["kernel_ms"], "les": les,
+                       "kernel": KERNEL_NAMES[r["kernel"]][0],
                        "roofline_frac": kach / peak, "bytes_per_update": b, "diverged": r["nan"]}
     e2e = None
     if "e2e" in results:
@@ -655,10 +666,10 @@ def main():
                    "body_force_x": BODY_FORCE, "l2": "inputs larger than L2 (populations >= 129 MB, no flush)",
                    "parallelism": "replicas" if world > 1 else "single GPU", "block": list(r0["block"]),
                    "boundary_nodes": r0["boundary"], "force_nodes": r0["force_nodes"], "diverged": r0["nan"],
-                   "kernel_variant": "paired nodes, packed FP32x2" if args.variant == 0 else "one node per thread"},
+                   "kernel_variant": KERNEL_NAMES[r0["kernel"]][1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
-                     "kernel_ms": r0["kernel_ms"], "kernel": "step_kernel"},
+                     "kernel_ms": r0["kernel_ms"], "kernel": KERNEL_NAMES[r0["kernel"]][0]},
         "precision": prec,
         "e2e": e2e,
         "gpu_launches": r0["launches"],

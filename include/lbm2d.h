@@ -95,7 +95,12 @@ typedef struct lbm2d_info {
     int n_force_nodes;         /* nodes with momentum-exchange links */
     long long steps_done;      /* steps executed since the last upload */
     int block_x, block_y;      /* launch shape of the step kernel */
+    int kernel;                /* LBM2D_KERNEL_* the next lbm2d_step runs */
 } lbm2d_info;
+
+#define LBM2D_KERNEL_SCALAR 0  /* one node per thread */
+#define LBM2D_KERNEL_PAIR 1    /* two x-neighbours per thread, packed FP32x2 */
+#define LBM2D_KERNEL_ROWS 2    /* row tiles staged by bulk copies, persistent grid */
 
 typedef struct lbm2d_solver lbm2d_solver;
 
@@ -192,10 +197,12 @@ int lbm2d_get_info(lbm2d_solver *h, lbm2d_info *info);
 /* Launch shape of the step kernel (threads per block = bx*by, a multiple of
  * 32, at most 1024).  0,0 restores the tuned default. */
 int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
-/* Step-kernel variant: 0 (default) runs two x-neighbours per thread with
- * packed FP32x2 arithmetic where the grid allows (nx even, non-thermal,
- * FP32/FP16/BF16 storage), 1 forces one node per thread.  Same results to
- * rounding. */
+/* Step-kernel variant.  0 (default): the fastest kernel the configuration
+ * allows -- the row pipeline (nx a multiple of 8, non-thermal, FP32/FP16/BF16
+ * storage, not a batch member), else two x-neighbours per thread with packed
+ * FP32x2 arithmetic (nx even), else one node per thread.  1: one node per
+ * thread.  2: two x-neighbours per thread where nx is even.  Same results to
+ * rounding; lbm2d_get_info reports the kernel in use. */
 int lbm2d_set_kernel_variant(lbm2d_solver *h, int variant);
 /* The CUDA stream the handle launches on (cudaStream_t as void*). */
 void *lbm2d_stream(lbm2d_solver *h);
@@ -258,11 +265,11 @@ void *lbm2d_batch_stream(lbm2d_batch *b);
 long long lbm2d_batch_launch_count(lbm2d_batch *b);
 
 /* ---- serving loop: requests of different grid sizes, geometries, Reynolds
- * numbers and step budgets arrive at any time; a worker thread admits them
- * by device-memory footprint, steps all active solves together through a
- * batch (one packed launch per step per storage group) and retires each one
- * exactly at its budget.  No counterpart in the reference (one solve per
- * process there). */
+ * numbers and step budgets arrive at any time; set-up threads admit them by
+ * device-memory footprint and build them on the host cores, a stepping
+ * thread steps all active solves together through a batch (one packed
+ * launch per step per storage group) and retires each one exactly at its
+ * budget.  No counterpart in the reference (one solve per process there). */
 #define LBM2D_GEOM_CAVITY 0        /* lid-driven cavity, src/cavity.cpp */
 #define LBM2D_GEOM_STEP 1          /* backward-facing step h = NY/3, src/step.cpp */
 #define LBM2D_GEOM_CYLINDER 2      /* cylinder D = NY/5, src/main.cpp */
@@ -292,6 +299,9 @@ typedef struct lbm2d_server_stats_t {
     double busy_s;                  /* wall time the worker spent stepping */
     long long lattice_updates;
     double device_bytes_in_use;
+    long long ticks;        /* batched step calls made */
+    long long member_ticks; /* sum over ticks of the solves in the tick */
+    double setup_s;         /* host time spent building requests (all set-up threads) */
 } lbm2d_server_stats_t;
 
 typedef struct lbm2d_server lbm2d_server;
@@ -303,9 +313,13 @@ int lbm2d_server_results(lbm2d_server *s, lbm2d_result *out, int capacity, int *
 int lbm2d_server_stats(lbm2d_server *s, lbm2d_server_stats_t *stats);
 int lbm2d_server_destroy(lbm2d_server *s);
 
-/* ---- launch-shape autotuner: times `steps` steps for each candidate block
- * shape (the state is saved before and restored after), keeps the fastest
- * and returns it.  No counterpart in the reference. */
+/* ---- launch-shape autotuner: times `steps` steps for each candidate (the
+ * row pipeline when the solver would run it, then each block shape of the
+ * paired or one-node kernel; the state is saved before and restored after),
+ * keeps the fastest and returns its block shape -- (0, 0) when the row
+ * pipeline won; otherwise the solver is left on that shape with kernel
+ * variant 2 (or its own variant).  The batch form tunes the shared shape of
+ * the batched kernels.  No counterpart in the reference. */
 int lbm2d_autotune(lbm2d_solver *h, int steps, double tau, double u_inflow, int *best_bx, int *best_by);
 int lbm2d_batch_autotune(lbm2d_batch *b, int steps, int *best_bx, int *best_by);
 

@@ -73,11 +73,13 @@ int bfail(lbm2d_batch* b, int code, const std::string& msg) {
     } while (0)
 
 void free_groups(lbm2d_batch* b) {
+    // stream-ordered: members join and leave a running serving loop without a
+    // device-wide synchronization
     for (auto& g : b->groups) {
-        cudaFree(g.d_params[0]);
-        cudaFree(g.d_params[1]);
-        cudaFree(g.d_block_start);
-        cudaFree(g.d_jobs);
+        cudaFreeAsync(g.d_params[0], b->stream);
+        cudaFreeAsync(g.d_params[1], b->stream);
+        cudaFreeAsync(g.d_block_start, b->stream);
+        cudaFreeAsync(g.d_jobs, b->stream);
     }
     b->groups.clear();
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -113,10 +115,10 @@ int build_layout(lbm2d_batch* b) {
     }
     for (auto& g : b->groups) {
         const size_t m = g.members.size();
-        BCK(cudaMalloc(&g.d_params[0], m * sizeof(KParams)), "batch params");
-        BCK(cudaMalloc(&g.d_params[1], m * sizeof(KParams)), "batch params");
-        BCK(cudaMalloc(&g.d_block_start, (m + 1) * sizeof(int)), "batch table");
-        BCK(cudaMalloc(&g.d_jobs, m * sizeof(ReduceJob)), "batch jobs");
+        BCK(cudaMallocAsync(&g.d_params[0], m * sizeof(KParams), b->stream), "batch params");
+        BCK(cudaMallocAsync(&g.d_params[1], m * sizeof(KParams), b->stream), "batch params");
+        BCK(cudaMallocAsync(&g.d_block_start, (m + 1) * sizeof(int), b->stream), "batch table");
+        BCK(cudaMallocAsync(&g.d_jobs, m * sizeof(ReduceJob), b->stream), "batch jobs");
         g.cap_members = m;
     }
     b->layout_dirty = false;
@@ -155,6 +157,7 @@ int prepare(lbm2d_batch* b) {
                 h->by = b->by;
             }
             KParams p;
+            const long long l0 = h->launches;
             if ((rc = prepare_steps(h, mem.tau, mem.u, p))) return bfail(b, rc, std::string("member: ") + h->err);
             p0[k] = p;
             p1[k] = p;
@@ -162,9 +165,15 @@ int prepare(lbm2d_batch* b) {
             p1[k].fout = const_cast<void*>(p.fin);
             p1[k].gin = p.gout;
             p1[k].gout = const_cast<void*>(p.gin);
-            // order the batch stream after the member's own preparation
-            BCK(cudaEventRecord(b->ev, h->stream), "event");
-            BCK(cudaStreamWaitEvent(b->stream, b->ev, 0), "wait");
+            p1[k].seed_in = p.seed_out;
+            p1[k].seed_out = const_cast<uint32_t*>(p.seed_in);
+            // order the batch stream after the member's own preparation (a
+            // prologue on the member's stream); nothing to order otherwise,
+            // the member's stream already waits for the batch's last step
+            if (h->launches != l0) {
+                BCK(cudaEventRecord(b->ev, h->stream), "event");
+                BCK(cudaStreamWaitEvent(b->stream, b->ev, 0), "wait");
+            }
             const int gy = (h->ny + b->by - 1) / b->by;
             start[k + 1] = start[k] + p.gx * gy;
             if (h->nslots > 0)
@@ -259,6 +268,7 @@ int lbm2d_batch_destroy(lbm2d_batch* b) {
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
     free_groups(b);
+    cudaStreamSynchronize(b->stream);
     if (b->h_params) cudaFreeHost(b->h_params);
     cudaEventDestroy(b->ev);
     cudaStreamDestroy(b->stream);
@@ -274,6 +284,7 @@ int lbm2d_batch_add(lbm2d_batch* b, lbm2d_solver* h, double tau, double u) {
     if (!(tau > 0.0)) return bfail(b, LBM2D_ERR_INVALID, "tau must be positive");
     if (member_index(b, h) >= 0) return bfail(b, LBM2D_ERR_INVALID, "already a member");
     b->members.push_back({h, tau, u});
+    h->in_batch = true;
     b->layout_dirty = true;
     return LBM2D_OK;
 }
@@ -285,6 +296,7 @@ int lbm2d_batch_remove(lbm2d_batch* b, lbm2d_solver* h) {
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);  // no batched work may still touch h
     b->members.erase(b->members.begin() + k);
+    h->in_batch = false;
     b->layout_dirty = true;
     return LBM2D_OK;
 }
@@ -403,12 +415,23 @@ int lbm2d_autotune(lbm2d_solver* h, int steps, double tau, double u, int* best_b
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    // Candidates: the row pipeline (when the solver would run it), then every
+    // block shape of the paired (or scalar) kernel.
+    const int v0 = h->variant;
+    const bool rows = kernel_kind(h) == KERNEL_ROWS;
+    const int shape_variant = rows ? 2 : v0;
     float best = 1e30f;
-    int bbx = h->bx, bby = h->by;
-    for (auto& s : kShapes) {
-        if (s[0] > 2 * h->nx && s[0] > 32) continue;
-        h->bx = s[0];
-        h->by = s[1];
+    int bbx = h->bx, bby = h->by, bvar = v0;
+    const int n_cand = (int)(sizeof(kShapes) / sizeof(kShapes[0])) + (rows ? 1 : 0);
+    for (int c = 0; c < n_cand; ++c) {
+        const bool is_rows = rows && c == 0;
+        const int* s = is_rows ? nullptr : kShapes[c - (rows ? 1 : 0)];
+        if (s && s[0] > 2 * h->nx && s[0] > 32) continue;
+        h->variant = is_rows ? 0 : shape_variant;
+        if (s) {
+            h->bx = s[0];
+            h->by = s[1];
+        }
         h->staged = true;
         if ((rc = lbm2d_step(h, tau, u, 2))) break;  // prologue + warm-up
         cudaEventRecord(e0, h->stream);
@@ -419,19 +442,24 @@ int lbm2d_autotune(lbm2d_solver* h, int steps, double tau, double u, int* best_b
         cudaEventElapsedTime(&ms, e0, e1);
         if (ms < best) {
             best = ms;
-            bbx = s[0];
-            bby = s[1];
+            bvar = h->variant;
+            if (s) {
+                bbx = s[0];
+                bby = s[1];
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    h->variant = bvar;
     h->bx = bbx;
     h->by = bby;
     const int rc2 = restore_state(h, counter, done);
     if (rc) return rc;
     if (rc2) return rc2;
-    if (best_bx) *best_bx = bbx;
-    if (best_by) *best_by = bby;
+    const bool rows_best = rows && bvar == 0;
+    if (best_bx) *best_bx = rows_best ? 0 : bbx;
+    if (best_by) *best_by = rows_best ? 0 : bby;
     return LBM2D_OK;
 }
 

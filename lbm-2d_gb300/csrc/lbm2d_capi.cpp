@@ -47,12 +47,15 @@ int cuda_fail(lbm2d_solver* h, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
     } while (0)
 
+// Device buffers come from the stream-ordered allocator on the handle's
+// stream: creating and destroying solves (the serving loop does it for every
+// request) then neither synchronizes the device nor stalls other streams.
 template <class T>
 int dalloc(lbm2d_solver* h, T** p, size_t bytes) {
     if (*p) return LBM2D_OK;
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+    cudaError_t e = cudaMallocAsync(&q, bytes ? bytes : 16, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
     *p = static_cast<T*>(q);
     h->device_bytes += bytes;
     return LBM2D_OK;
@@ -60,9 +63,8 @@ int dalloc(lbm2d_solver* h, T** p, size_t bytes) {
 
 template <class T>
 void dfree(lbm2d_solver* h, T** p) {
-    if (*p) cudaFree(*p);
+    if (*p) cudaFreeAsync(*p, h->stream);
     *p = nullptr;
-    (void)h;
 }
 
 int bc_kind(int case_type) {
@@ -252,15 +254,50 @@ int upload_geometry(lbm2d_solver* h) {
 }
 
 bool use_pair(const lbm2d_solver* h) {
-    return h->variant == 0 && (h->nx % 2 == 0) && !h->thermal && h->storage != ST_FP64;
+    return h->variant != 1 && (h->nx % 2 == 0) && !h->thermal && h->storage != ST_FP64;
 }
 
+int kernel_kind(const lbm2d_solver* h) {
+    if (!use_pair(h)) return KERNEL_SCALAR;
+    if (h->variant == 0 && !h->in_batch && rows_eligible(h->storage, h->nx, h->ny, h->thermal)) return KERNEL_ROWS;
+    return KERNEL_PAIR;
+}
+
+// Per-warp force slots of the kernel that will run.  Scalar / paired
+// kernels: one table entry per launch block (blocks without a force node get
+// -1).  Row pipeline: one entry per persistent CTA, marking the CTAs whose
+// tiles (tile t goes to CTA t mod grid) hold a force node.
 int ensure_slots(lbm2d_solver* h) {
-    const int pair = use_pair(h) ? 1 : 0;
-    if (h->slot_bx == h->bx && h->slot_by == h->by && h->slot_pair == pair && h->d_block_slot) return LBM2D_OK;
+    const int kind = kernel_kind(h);
+    int grid = 0;
+    if (kind == KERNEL_ROWS) {
+        grid = rows_grid(h->storage, h->nx, h->ny, h->device);
+        if (grid <= 0) return fail(h, LBM2D_ERR_CUDA, "row pipeline: no launch configuration");
+    }
+    if (h->slot_kind == kind && h->d_block_slot &&
+        (kind == KERNEL_ROWS ? h->slot_grid == grid : (h->slot_bx == h->bx && h->slot_by == h->by)))
+        return LBM2D_OK;
     std::vector<int> slots;
-    h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx * (pair ? 2 : 1), h->by, h->bx * h->by,
-                                  slots);  // per-warp slots
+    if (kind == KERNEL_ROWS) {
+        const int tw = rows_tile_width(), tpr = (h->nx + tw - 1) / tw, warps = rows_warps_per_block();
+        slots.assign((size_t)grid, -1);
+        for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
+            if (!h->geo.rec_force[r]) continue;
+            const int id = h->geo.rec_node[r];
+            const long long t = (long long)(id / h->nx) * tpr + (id % h->nx) / tw;
+            slots[(size_t)(t % grid)] = 0;
+        }
+        int k = 0;
+        for (auto& s : slots)
+            if (s == 0) {
+                s = k;
+                k += warps;
+            }
+        h->nslots = k;
+    } else {
+        h->nslots = force_block_slots(h->geo, h->nx, h->ny, h->bx * (kind == KERNEL_PAIR ? 2 : 1), h->by,
+                                      h->bx * h->by, slots);  // per-warp slots
+    }
     dfree(h, &h->d_block_slot);
     dfree(h, &h->d_partials);
     int rc;
@@ -271,7 +308,8 @@ int ensure_slots(lbm2d_solver* h) {
     CK(cudaStreamSynchronize(h->stream), "slots");
     h->slot_bx = h->bx;
     h->slot_by = h->by;
-    h->slot_pair = pair;
+    h->slot_kind = kind;
+    h->slot_grid = grid;
     return LBM2D_OK;
 }
 
@@ -327,6 +365,10 @@ int prologue(lbm2d_solver* h, const CollideParams& c) {
     apply_collide(p, c);
     p.fout = h->P[h->cur];
     p.gout = h->G[h->cur];
+    // rounding-noise seed of the prologue; the steps after it continue from
+    // seed_host + 1 (written to the seed word of the current buffer)
+    p.seed_host = (uint32_t)h->steps_done ^ 0xA511E9B3u;
+    p.seed_out = h->d_seed + h->cur;
     int e = launch_prologue(h->storage, p, h->d_stage_f, h->thermal ? h->d_stage_g : nullptr, h->stream);
     ++h->launches;
     if (e) return cuda_fail(h, (cudaError_t)e, "prologue");
@@ -367,6 +409,8 @@ int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p) {
     p.fout = h->P[h->cur ^ 1];
     p.gin = h->G[h->cur];
     p.gout = h->G[h->cur ^ 1];
+    p.seed_in = h->d_seed + h->cur;
+    p.seed_out = h->d_seed + (h->cur ^ 1);
     p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
     return LBM2D_OK;
 }
@@ -423,6 +467,14 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
     h->mask.assign(h->N, 0);
     cudaError_t e = cudaSetDevice(h->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        // keep freed solver memory in the device's pool for the next solver
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, h->device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     int rc = LBM2D_OK;
     if (e != cudaSuccess) {
         g_global_err = std::string("stream: ") + cudaGetErrorString(e);
@@ -430,6 +482,7 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
         return LBM2D_ERR_CUDA;
     }
     if (!rc) rc = dalloc(h, &h->d_nan, 16);
+    if (!rc) rc = dalloc(h, &h->d_seed, 16);
     if (!rc) rc = dalloc(h, &h->d_counter, 16);
     if (!rc) rc = dalloc(h, &h->d_last, 16);
     if (!rc) rc = dalloc(h, &h->d_hist, (size_t)h->hist_cap * 2 * sizeof(double));
@@ -437,6 +490,7 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
     if (!rc) rc = ensure_populations(h);
     if (!rc) {
         cudaMemsetAsync(h->d_nan, 0, 16, h->stream);
+        cudaMemsetAsync(h->d_seed, 0, 16, h->stream);
         cudaMemsetAsync(h->d_counter, 0, 16, h->stream);
         cudaMemsetAsync(h->d_last, 0, 16, h->stream);
         if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = LBM2D_ERR_CUDA;
@@ -456,10 +510,11 @@ int lbm2d_destroy(lbm2d_solver* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
                     h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
-                    h->d_counter, h->d_last, h->d_nan, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
+                    h->d_counter, h->d_last, h->d_nan, h->d_seed, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
                     h->d_diag, h->d_prev_uv};
     for (void* b : bufs)
-        if (b) cudaFree(b);
+        if (b) cudaFreeAsync(b, h->stream);
+    if (h->stream) cudaStreamSynchronize(h->stream);
     for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -631,6 +686,8 @@ int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
         p.fout = h->P[h->cur ^ 1];
         p.gin = h->G[h->cur];
         p.gout = h->G[h->cur ^ 1];
+        p.seed_in = h->d_seed + h->cur;
+        p.seed_out = h->d_seed + (h->cur ^ 1);
         p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (h->profiling) {
@@ -645,7 +702,8 @@ int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
             e1 = h->ev_pool[h->ev_used++];
             CK(cudaEventRecord(e0, h->stream), "event");
         }
-        int e = launch_step(h->storage, p, h->bx, h->by, h->stream);
+        int e = h->slot_kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
+                                            : launch_step(h->storage, p, h->bx, h->by, h->stream);
         if (e1) CK(cudaEventRecord(e1, h->stream), "event");
         ++h->launches;
         if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
@@ -671,6 +729,7 @@ int lbm2d_synchronize(lbm2d_solver* h) {
     CK(cudaMemcpy(&flag, h->d_nan, sizeof(flag), cudaMemcpyDeviceToHost), "nan flag");
     if (flag) {
         cudaMemset(h->d_nan, 0, sizeof(flag));
+        if (flag & 2u) return fail(h, LBM2D_ERR_TIMEOUT, "a step kernel's pipeline wait exceeded its limit");
         return fail(h, LBM2D_ERR_NAN, "a non-finite or zero density was produced");
     }
     return LBM2D_OK;
@@ -792,9 +851,9 @@ int lbm2d_download_macros(lbm2d_solver* h, double* rho, double* u, double* v, do
     double* outs[4] = {rho, u, v, (h->thermal ? T : nullptr)};
     for (int k = 0; k < 4; ++k) {
         if (!outs[k]) continue;
-        if (cudaMalloc(&bufs[k], h->N * sizeof(double)) != cudaSuccess) {
+        if (cudaMallocAsync(&bufs[k], h->N * sizeof(double), h->stream) != cudaSuccess) {
             for (int j = 0; j < k; ++j)
-                if (bufs[j]) cudaFree(bufs[j]);
+                if (bufs[j]) cudaFreeAsync(bufs[j], h->stream);
             return fail(h, LBM2D_ERR_OOM, "macros buffer");
         }
     }
@@ -815,9 +874,9 @@ int lbm2d_download_macros(lbm2d_solver* h, double* rho, double* u, double* v, do
                                              h->stream);
             if (ce != cudaSuccess) ret = cuda_fail(h, ce, "D2H macros");
         }
-    cudaStreamSynchronize(h->stream);
     for (int k = 0; k < 4; ++k)
-        if (bufs[k]) cudaFree(bufs[k]);
+        if (bufs[k]) cudaFreeAsync(bufs[k], h->stream);
+    cudaStreamSynchronize(h->stream);
     return ret;
 }
 
@@ -868,6 +927,7 @@ int lbm2d_get_info(lbm2d_solver* h, lbm2d_info* info) {
     info->steps_done = h->steps_done;
     info->block_x = h->bx;
     info->block_y = h->by;
+    info->kernel = kernel_kind(h);
     return LBM2D_OK;
 }
 
@@ -911,7 +971,7 @@ int lbm2d_profile(lbm2d_solver* h, double* ms, long long* n) {
 int lbm2d_set_kernel_variant(lbm2d_solver* h, int variant) {
     int rc;
     if ((rc = check_handle(h))) return rc;
-    if (variant < 0 || variant > 1) return fail(h, LBM2D_ERR_INVALID, "unknown kernel variant");
+    if (variant < 0 || variant > 2) return fail(h, LBM2D_ERR_INVALID, "unknown kernel variant");
     if (variant == h->variant) return LBM2D_OK;
     if ((rc = before_setting_change(h))) return rc;  // the stored state stays valid; rebuild for safety
     h->variant = variant;

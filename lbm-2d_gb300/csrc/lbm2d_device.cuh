@@ -1,0 +1,692 @@
+// lbm2d_device.cuh -- device functions shared by the step kernels: storage
+// formats, lattice math, the pull + rebuild of the reference's post-stream
+// state, the MRT/BGK/LES/thermal collision (one node, and two nodes at once
+// in packed FP32x2 arithmetic) and the per-block step bodies.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "lbm2d_internal.h"
+
+namespace lbm2d {
+namespace {
+
+// D2Q9 lattice, direction order of src/lbm_types.hpp:41-55.
+__host__ __device__ constexpr int CXf(int i) { return (i == 1 || i == 5 || i == 8) ? 1 : ((i == 3 || i == 6 || i == 7) ? -1 : 0); }
+__host__ __device__ constexpr int CYf(int i) { return (i == 2 || i == 5 || i == 6) ? 1 : ((i == 4 || i == 7 || i == 8) ? -1 : 0); }
+__host__ __device__ constexpr int BBf(int i) { return i == 0 ? 0 : (i < 5 ? ((i + 1) % 4 + 1) : ((i - 5 + 2) % 4 + 5)); }
+static_assert(BBf(1) == 3 && BBf(2) == 4 && BBf(3) == 1 && BBf(4) == 2, "bounce-back map");
+static_assert(BBf(5) == 7 && BBf(6) == 8 && BBf(7) == 5 && BBf(8) == 6, "bounce-back map");
+__host__ __device__ constexpr double wgt(int i) { return i == 0 ? 4.0 / 9.0 : (i < 5 ? 1.0 / 9.0 : 1.0 / 36.0); }
+
+// ----------------------------------------------------------------- storage formats
+// FP16/BF16 hold shifted deviations d = f - w_i*rho0 (g - w_i*T_ref); FP16
+// stores d * 2^12 so that small deviations stay clear of the FP16 subnormal
+// range (|d| < 16 fits).  Both are written with STOCHASTIC rounding
+// (Blackwell cvt.rs, one 32-bit random word per two values): round-to-nearest
+// makes the same rounding error at every node of a near-uniform flow on
+// every step, which drifts the conserved moments linearly in time; rounding
+// up with probability equal to the discarded fraction leaves the stored
+// value unbiased, so the errors stay a zero-mean random walk.
+constexpr float kF16Scale = 4096.0f;
+constexpr float kF16InvScale = 1.0f / 4096.0f;
+
+// Two FP32 values -> packed FP16x2 / BF16x2 (lo = a, hi = b), rounded
+// stochastically with the random bits rb.
+__device__ __forceinline__ uint32_t cvt_rs_f16x2(float a, float b, uint32_t rb) {
+    uint32_t d;
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(b), "f"(a), "r"(rb));
+    return d;
+}
+__device__ __forceinline__ uint32_t cvt_rs_bf16x2(float a, float b, uint32_t rb) {
+    uint32_t d;
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(b), "f"(a), "r"(rb));
+    return d;
+}
+
+template <class T>
+struct Pop;
+template <>
+struct Pop<float> {
+    using R = float;
+    static constexpr bool kRounds = false;
+    static __device__ __forceinline__ R ld(const float* __restrict__ p, size_t i, float) { return __ldg(p + i); }
+    static __device__ __forceinline__ void st(float* __restrict__ p, size_t i, R v, float, uint32_t) { p[i] = v; }
+};
+template <>
+struct Pop<double> {
+    using R = double;
+    static constexpr bool kRounds = false;
+    static __device__ __forceinline__ R ld(const double* __restrict__ p, size_t i, float) { return __ldg(p + i); }
+    static __device__ __forceinline__ void st(double* __restrict__ p, size_t i, R v, float, uint32_t) { p[i] = v; }
+};
+template <>
+struct Pop<__half> {
+    using R = float;
+    static constexpr bool kRounds = true;
+    static __device__ __forceinline__ R ld(const __half* __restrict__ p, size_t i, float sh) {
+        return fmaf(__half2float(__ldg(p + i)), kF16InvScale, sh);
+    }
+    static __device__ __forceinline__ void st(__half* __restrict__ p, size_t i, R v, float sh, uint32_t rb) {
+        const float d = fmaf(v, kF16Scale, -sh * kF16Scale);
+        p[i] = __ushort_as_half((unsigned short)(cvt_rs_f16x2(d, d, rb) & 0xFFFFu));
+    }
+};
+template <>
+struct Pop<__nv_bfloat16> {
+    using R = float;
+    static constexpr bool kRounds = true;
+    static __device__ __forceinline__ R ld(const __nv_bfloat16* __restrict__ p, size_t i, float sh) {
+        return __bfloat162float(__ldg(p + i)) + sh;
+    }
+    static __device__ __forceinline__ void st(__nv_bfloat16* __restrict__ p, size_t i, R v, float sh, uint32_t rb) {
+        const float d = v - sh;
+        p[i] = __ushort_as_bfloat16((unsigned short)(cvt_rs_bf16x2(d, d, rb) & 0xFFFFu));
+    }
+};
+
+// ----------------------------------------------------------------- rounding noise
+// Random words for stochastic rounding: the lowbias32 integer hash (C.
+// Wellons, 2018) of a per-node key; nine words come from three hashes
+// combined by XOR and rotation (each word is uniform, which is all unbiased
+// rounding needs).  The key is node + seed * golden-ratio constant, the seed
+// advancing by one per step through the solver's seed words (see seed_of).
+__device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ void rand9(uint32_t key, uint32_t r[9]) {
+    const uint32_t a = lowbias32(key), b = lowbias32(key ^ 0x9E3779B9u), c = lowbias32(key + 0x7F4A7C15u);
+    r[0] = a;
+    r[1] = b;
+    r[2] = c;
+    r[3] = a ^ b;
+    r[4] = b ^ c;
+    r[5] = a ^ c;
+    r[6] = a ^ b ^ c;
+    r[7] = __funnelshift_l(a, a, 16) ^ b;
+    r[8] = __funnelshift_l(b, b, 16) ^ c;
+}
+
+// Seed of this launch's rounding noise, and the hand-over to the next launch:
+// a step kernel reads seed_in and its first thread writes seed_in + 1 to
+// seed_out (the solver's two seed words swap roles every step like the
+// population buffers, so no launch reads a word that it writes).  A
+// prologue has no seed_in and uses seed_host.
+__device__ __forceinline__ uint32_t seed_of(const KParams& p) {
+    return p.seed_in ? __ldg(p.seed_in) : p.seed_host;
+}
+__device__ __forceinline__ void pass_seed(const KParams& p, uint32_t s, bool first_thread) {
+    if (first_thread && p.seed_out) *p.seed_out = s + 1u;
+}
+__device__ __forceinline__ uint32_t seed_key(uint32_t s) { return s * 0x9E3779B1u; }
+
+// Parameters in the compute precision.
+template <class R>
+__device__ __forceinline__ const Phys<R>& phys(const KParams& p);
+template <>
+__device__ __forceinline__ const Phys<float>& phys<float>(const KParams& p) { return p.pf; }
+template <>
+__device__ __forceinline__ const Phys<double>& phys<double>(const KParams& p) { return p.pd; }
+
+// Reciprocal / square root / exponential: hardware approximations (a few
+// ulp) in the FP32 path, IEEE in the FP64 path.
+template <class R>
+struct Fm;
+template <>
+struct Fm<float> {
+    static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
+    static __device__ __forceinline__ float sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+    static __device__ __forceinline__ float exp(float x) { return __expf(x); }
+};
+template <>
+struct Fm<double> {
+    static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+};
+
+// ----------------------------------------------------------------- lattice math
+// compute_equilibrium, src/lbm_types.hpp:269-273
+template <class R>
+__device__ __forceinline__ R feq(int i, R rho, R u, R v) {
+    R ed = R(CXf(i)) * u + R(CYf(i)) * v;
+    R usq = u * u + v * v;
+    return R(wgt(i)) * rho * (R(1) + R(3) * ed + R(4.5) * ed * ed - R(1.5) * usq);
+}
+
+// compute_macros, src/lbm_types.hpp:278-288
+template <class R>
+__device__ __forceinline__ void macros(const R f[9], R& rho, R& u, R& v) {
+    rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
+    R mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    R my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    const R inv = Fm<R>::rcp(rho);
+    u = mx * inv;
+    v = my * inv;
+}
+
+template <class R>
+__device__ __forceinline__ R clamp_rate(R s) { return s < R(0.5) ? R(0.5) : (s > R(1.99) ? R(1.99) : s); }
+
+// ----------------------------------------------------------------- pull + rebuild
+template <class T>
+__device__ __forceinline__ void pull(const KParams& p, const T* __restrict__ P, const float* sh, int x, int y,
+                                     typename Pop<T>::R f[9]) {
+    const unsigned nx = (unsigned)p.nx, ny = (unsigned)p.ny;
+    const size_t N = (size_t)p.N;
+    const unsigned ux = (unsigned)x, uy = (unsigned)y;
+    const unsigned xm = ux == 0 ? nx - 1 : ux - 1, xp = ux == nx - 1 ? 0 : ux + 1;
+    const unsigned ym = uy == 0 ? ny - 1 : uy - 1, yp = uy == ny - 1 ? 0 : uy + 1;
+    const unsigned r0 = uy * nx, rm = ym * nx, rp = yp * nx;  // nx*ny < 2^32 (checked at create)
+    // slot j pulls from (x - cx_j, y - cy_j), wrapped; records override the
+    // slots whose source is solid or outside the domain.
+    f[0] = Pop<T>::ld(P, r0 + ux, sh[0]);
+    f[1] = Pop<T>::ld(P + N, r0 + xm, sh[1]);
+    f[2] = Pop<T>::ld(P + 2 * N, rm + ux, sh[2]);
+    f[3] = Pop<T>::ld(P + 3 * N, r0 + xp, sh[3]);
+    f[4] = Pop<T>::ld(P + 4 * N, rp + ux, sh[4]);
+    f[5] = Pop<T>::ld(P + 5 * N, rm + xm, sh[5]);
+    f[6] = Pop<T>::ld(P + 6 * N, rm + xp, sh[6]);
+    f[7] = Pop<T>::ld(P + 7 * N, rp + xp, sh[7]);
+    f[8] = Pop<T>::ld(P + 8 * N, rp + xm, sh[8]);
+}
+
+// Rebuild the non-regular f slots of a boundary node from its record
+// (streaming bounce-back src/lbm.hpp:418-428, :449-452, :470-480 and
+// apply_bouzidi_bb :226-288).
+template <class T>
+__device__ __forceinline__ void fix_f(const KParams& p, const T* __restrict__ P, int x, int y, uint32_t rec,
+                                   typename Pop<T>::R f[9]) {
+    using R = typename Pop<T>::R;
+    const uint32_t types = p.rec_info[rec] & 0x3FFFFu;
+    if (types == 0) return;
+    const size_t N = (size_t)p.N;
+    const size_t n = (size_t)y * p.nx + x;
+    R own[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) own[j] = Pop<T>::ld(P + j * N, n, p.shf[j]);
+    R rho, u, v;
+    macros(own, rho, u, v);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const uint32_t t = (types >> (2 * j)) & 3u;
+        if (t == SLOT_SIMPLE_BB) {
+            f[j] = own[BBf(j)];
+        } else if (t == SLOT_ZERO) {
+            f[j] = R(0);
+        } else if (t == SLOT_INTERP) {
+            const int i = BBf(j);  // the reference's link direction (node -> solid)
+            const R q = R(p.rec_q[(size_t)rec * 9 + j]);
+            R uwx = R(0), uwy = R(0);
+            if (p.moving_wall) {
+                uwx = R(p.rec_uw[((size_t)rec * 9 + j) * 2]);
+                uwy = R(p.rec_uw[((size_t)rec * 9 + j) * 2 + 1]);
+            }
+            const R ed = R(CXf(i)) * uwx + R(CYf(i)) * uwy;
+            R fbb;
+            if (!p.interp_classic) {
+                // Mei (1999) / Filippova-Hanel (1998), src/lbm.hpp:234-256
+                fbb = q * feq<R>(i, rho, uwx, uwy) + (R(1) - q) * own[i] +
+                      (R(2) * q - R(1)) * R(wgt(i)) * rho * ed * R(3);
+            } else {
+                // classic Bouzidi (2001), src/lbm.hpp:257-273, + Ladd :276-285
+                if (q < R(0.5)) {
+                    const int sx = x - CXf(i), sy = y - CYf(i);
+                    R fsrc = own[i];
+                    if (sx >= 0 && sx < p.nx && sy >= 0 && sy < p.ny)
+                        fsrc = Pop<T>::ld(P + i * N, (size_t)sy * p.nx + sx, p.shf[i]);
+                    fbb = R(2) * q * own[i] + (R(1) - R(2) * q) * fsrc;
+                } else {
+                    const R inv2q = R(1) / (R(2) * q);
+                    fbb = inv2q * own[i] + (R(1) - inv2q) * own[j];
+                }
+                if (p.moving_wall) fbb -= R(2) * R(wgt(i)) * rho * ed * R(3);
+            }
+            f[j] = fbb;
+        }
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void fix_g(const KParams& p, const T* __restrict__ G, int x, int y, uint32_t rec,
+                                   typename Pop<T>::R g[9]) {
+    using R = typename Pop<T>::R;
+    const uint32_t m = (p.rec_info[rec] >> REC_GBB_SHIFT) & 0x1FFu;
+    if (m == 0) return;
+    const size_t N = (size_t)p.N;
+    const size_t n = (size_t)y * p.nx + x;
+    R own[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) own[j] = Pop<T>::ld(G + j * N, n, p.shg[j]);
+#pragma unroll
+    for (int j = 0; j < 9; ++j)
+        if (m & (1u << j)) g[j] = own[BBf(j)];  // adiabatic bounce-back, src/lbm.hpp:512-520
+}
+
+// Zou/He velocity inlet on one node, src/lbm.hpp:21-34 / :40-58
+template <class R>
+__device__ __forceinline__ void zou_he(R f[9], R uin) {
+    R rho = (f[0] + f[2] + f[4] + R(2) * (f[3] + f[6] + f[7])) / (R(1) - uin);
+    f[1] = f[3] + R(2.0 / 3.0) * rho * uin;
+    f[5] = f[7] + R(1.0 / 6.0) * rho * uin;
+    f[8] = f[6] + R(1.0 / 6.0) * rho * uin;
+}
+
+// Boundary conditions of execute_time_step on node (x, y) after streaming,
+// src/lbm.hpp:531-540.
+template <class R>
+__device__ __forceinline__ void apply_bc(const KParams& p, int x, int y, uint32_t fl, R f[9]) {
+    if (p.bc_kind == BC_LID) {
+        if (y == p.ny - 1) {  // enforce_lid :110-120 (corner nodes included)
+            R rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
+            const R ul = phys<R>(p).u_bc;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) f[i] = feq<R>(i, rho, ul, R(0));
+        }
+    } else if (p.bc_kind == BC_INFLOW) {
+        if (x == 0) zou_he<R>(f, phys<R>(p).u_bc);
+    } else if (p.bc_kind == BC_STEP) {
+        const int hs = p.ny / 3;
+        if (x == 0 && y >= hs && !(fl & FLAG_SOLID)) {
+            const R yy = R(y - hs), h = R(p.ny - 1 - hs);
+            zou_he<R>(f, phys<R>(p).u_bc * R(4) * yy * (h - yy) / (h * h));
+        }
+    }
+}
+
+// The reference's state after streaming, boundary conditions and (optionally)
+// a driver thermal pass, for node (x, y).  f/g hold it on return.
+template <class T, bool TH>
+__device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint32_t fl, typename Pop<T>::R f[9],
+                                            typename Pop<T>::R g[9]) {
+    using R = typename Pop<T>::R;
+    const T* __restrict__ Pf = static_cast<const T*>(p.fin);
+    const bool outflow_col = (p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x == p.nx - 1;
+    // zero-gradient outlet: column NX-1 takes NX-2's post-stream state (src/lbm.hpp:63-73)
+    const int sx = outflow_col ? x - 1 : x;
+    const uint32_t sfl = outflow_col ? __ldg(p.flags + (size_t)y * p.nx + sx) : fl;
+    if (sfl & FLAG_SOLID) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) f[j] = R(0);
+    } else {
+        pull<T>(p, Pf, p.shf, sx, y, f);
+        if (sfl & FLAG_BOUNDARY) fix_f<T>(p, Pf, sx, y, sfl >> 2, f);
+    }
+    if (TH) {
+        const T* __restrict__ Pg = static_cast<const T*>(p.gin);
+        if (fl & FLAG_SOLID) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) g[j] = R(0);
+        } else {
+            pull<T>(p, Pg, p.shg, x, y, g);
+            if (fl & FLAG_BOUNDARY) fix_g<T>(p, Pg, x, y, fl >> 2, g);
+        }
+    }
+    apply_bc<R>(p, x, y, fl, f);
+    if (TH && p.hook_kind == 1) {
+        // src/thermal_cavity.cpp:168-204: Dirichlet columns, then adiabatic rows
+        if ((x == 1 || x == p.nx - 2) && y >= 1 && y <= p.ny - 2) {
+            const R Tw = x == p.nx - 2 ? phys<R>(p).hook_b : phys<R>(p).hook_a;
+            R rho, u, v;
+            macros(f, rho, u, v);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = feq<R>(i, Tw, u, v);
+        }
+        if ((y == 1 || y == p.ny - 2) && x >= 1 && x <= p.nx - 2) {
+            g[1] = g[3];
+            g[2] = g[4];
+            g[5] = g[7];
+            g[6] = g[8];
+        }
+    } else if (TH && p.hook_kind == 2) {
+        if (fl & FLAG_SOLID) {  // src/heated_cylinder.cpp:156-164
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = R(wgt(i)) * phys<R>(p).hook_a;
+        }
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R wall_distance(const KParams& p, uint32_t fl) {
+    if (fl & FLAG_BOUNDARY) return R(p.rec_wd[fl >> 2]);
+    const uint32_t d = fl >> 2;
+    if (d == WD_UNREACHED) return R(1e9);
+    if (d < (1u << 23)) return R(__uint_as_float(0x4B000000u | d) - 8388608.0f);  // exact integer
+    return R(d);
+}
+
+// Collision of one fluid node: src/lbm.hpp:300-354 (mrt_collide :128-218,
+// LES :158-182 with y+ :317-325, body force :327-331) and the thermal
+// collision with Boussinesq/Guo forcing :357-397 (src/thermal.hpp:25-52).
+template <class R, bool TH>
+__device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R g[9]) {
+    const Phys<R>& q = phys<R>(p);
+    R rho, u, v;
+    macros(f, rho, u, v);
+    if (!(rho == rho) || rho == R(0)) atomicOr(p.nan_flag, 1u);
+    if (p.collision == 0) {
+        const R f0 = f[0], f1 = f[1], f2 = f[2], f3 = f[3], f4 = f[4];
+        const R f5 = f[5], f6 = f[6], f7 = f[7], f8 = f[8];
+        const R sd = f5 + f6 + f7 + f8, sa = f1 + f2 + f3 + f4;
+        R me = R(-4) * f0 - sa + R(2) * sd;
+        R meps = R(4) * f0 - R(2) * sa + sd;
+        R mpxx = f1 - f2 + f3 - f4;
+        R mpxy = f5 - f6 + f7 - f8;
+        const R jx = rho * u, jy = rho * v;
+        const R usq = u * u + v * v;
+        const R e_eq = R(-2) * rho + R(3) * rho * usq;
+        const R eps_eq = rho - R(3) * rho * usq;
+        const R pxx_eq = rho * (u * u - v * v);
+        const R pxy_eq = rho * u * v;
+        R s_eff = q.s_shear;
+        if (p.les) {
+            // Smagorinsky with Van Driest damping (src/lbm.hpp:158-182, y+ :317-325);
+            // the damped branch always applies when y+ > 0
+            R csq = q.cs_sq;
+            if (q.nu > R(0)) {
+                const R wd = wall_distance<R>(p, fl);
+                const R yp = wd * Fm<R>::sqrt(usq + R(1e-12)) * q.inv_nu;
+                if (yp > R(0)) {
+                    const R cd = q.cs * (R(1) - Fm<R>::exp(-yp * R(1.0 / 26.0)));
+                    csq = cd * cd;
+                }
+            }
+            const R a = mpxx - pxx_eq, b = mpxy - pxy_eq;
+            const R Q = Fm<R>::sqrt(R(2) * (a * a + b * b));
+            const R A = R(4.5) * csq * Q * Fm<R>::rcp(rho);
+            const R te2 = q.tau + Fm<R>::sqrt(q.tau * q.tau + R(4) * A);  // 2 * tau_eff
+            s_eff = clamp_rate<R>(R(2) * Fm<R>::rcp(te2));
+        }
+        me -= q.s_bulk * (me - e_eq);
+        meps -= q.s_bulk * (meps - eps_eq);
+        // MRTParams::from_tau fixes s_normal = 1 (src/lbm_types.hpp:75): the
+        // energy-flux moments relax exactly to their equilibrium -j
+        const R mqx = -jx, mqy = -jy;
+        mpxx -= s_eff * (mpxx - pxx_eq);
+        mpxy -= s_eff * (mpxy - pxy_eq);
+        // closed-form inverse transform (src/lbm.hpp:193-217), common terms shared
+        const R a0 = R(1.0 / 9.0) * rho;
+        const R ax = a0 - R(1.0 / 36.0) * me - R(1.0 / 18.0) * meps;  // axial base
+        const R ad = a0 + R(1.0 / 18.0) * me + R(1.0 / 36.0) * meps;  // diagonal base
+        const R hx = R(1.0 / 6.0) * (jx - mqx);
+        const R hy = R(1.0 / 6.0) * (jy - mqy);
+        const R dx = R(1.0 / 6.0) * jx + R(1.0 / 12.0) * mqx;
+        const R dy = R(1.0 / 6.0) * jy + R(1.0 / 12.0) * mqy;
+        const R px = R(0.25) * mpxx, py = R(0.25) * mpxy;
+        f[0] = a0 - R(1.0 / 9.0) * me + R(1.0 / 9.0) * meps;
+        f[1] = ax + hx + px;
+        f[2] = ax + hy - px;
+        f[3] = ax - hx + px;
+        f[4] = ax - hy - px;
+        f[5] = ad + dx + dy + py;
+        f[6] = ad - dx + dy - py;
+        f[7] = ad - dx - dy + py;
+        f[8] = ad + dx - dy - py;
+    } else {
+        const R it = q.inv_tau;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f[i] -= it * (f[i] - feq<R>(i, rho, u, v));
+    }
+    if (q.Fscale != R(0)) {
+        const R F = q.Fscale;
+        const R fa = R(1.0 / 9.0) * F, fd = R(1.0 / 36.0) * F;
+        f[1] += fa;
+        f[3] -= fa;
+        f[5] += fd;
+        f[6] -= fd;
+        f[7] -= fd;
+        f[8] += fd;
+    }
+    if (TH) {
+        R rho2, u2, v2;
+        macros(f, rho2, u2, v2);
+        const R T = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8];
+        const R om = q.omega_k;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) g[i] -= om * (g[i] - feq<R>(i, T, u2, v2));
+        if (q.beta > R(0) && q.g_buoy != R(0)) {
+            const R fyb = -q.beta * (T - q.T_ref) * q.g_buoy;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const R eu = R(CXf(i)) * u2 + R(CYf(i)) * v2;
+                const R Fd = R(CYf(i)) * fyb;
+                f[i] += R(wgt(i)) * (R(3) * Fd + R(9) * eu * Fd);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void block_reduce2(double& a, double& b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    __shared__ double sa[32], sb[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    if ((tid & 31) == 0) {
+        sa[tid >> 5] = a;
+        sb[tid >> 5] = b;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        a = tid < nw ? sa[tid] : 0.0;
+        b = tid < nw ? sb[tid] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+    }
+}
+
+// ----------------------------------------------------------------- kernels
+// One step of the block (bxi, byi) of an instance whose block grid is gx wide.
+template <class T, bool TH>
+__device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, int gx) {
+    using R = typename Pop<T>::R;
+    const int x = bxi * blockDim.x + threadIdx.x;
+    const int y = byi * blockDim.y + threadIdx.y;
+    uint32_t skey = 0;
+    if constexpr (Pop<T>::kRounds) {
+        const uint32_t s = seed_of(p);
+        skey = seed_key(s);
+        pass_seed(p, s, bxi == 0 && byi == 0 && threadIdx.x == 0 && threadIdx.y == 0);
+    }
+    R fxs = R(0), fys = R(0);
+    if (x < p.nx && y < p.ny) {
+        const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
+        const uint32_t fl = __ldg(p.flags + n);
+        R f[9], g[9];
+        build_state<T, TH>(p, x, y, fl, f, g);
+        if (!(fl & FLAG_SOLID)) {
+            if (fl & FLAG_BOUNDARY) {
+                // momentum exchange of this node's links (src/lbm.hpp:565-577)
+                const uint32_t fm = p.rec_force[fl >> 2];
+#pragma unroll
+                for (int j = 1; j < 9; ++j)
+                    if (fm & (1u << j)) {
+                        fxs -= R(CXf(j)) * R(2) * f[j];
+                        fys -= R(CYf(j)) * R(2) * f[j];
+                    }
+            }
+            collide<R, TH>(p, fl, f, g);
+        }
+        T* __restrict__ Fo = static_cast<T*>(p.fout);
+        const size_t N = (size_t)p.N;
+        if (!((fl & FLAG_SOLID) && p.skip_settled_solids && x > 0 && x < p.nx - 1 && y < p.ny - 1)) {
+            uint32_t rb[9] = {};
+            if constexpr (Pop<T>::kRounds) rand9(skey + n, rb);
+#pragma unroll
+            for (int j = 0; j < 9; ++j) Pop<T>::st(Fo + j * N, n, f[j], p.shf[j], rb[j]);
+            if (TH) {
+                T* __restrict__ Go = static_cast<T*>(p.gout);
+                if constexpr (Pop<T>::kRounds) rand9((skey + n) ^ 0x6A09E667u, rb);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) Pop<T>::st(Go + j * N, n, g[j], p.shg[j], rb[j]);
+            }
+        }
+    }
+    if (p.block_slot) {
+        const int base = p.block_slot[byi * gx + bxi];
+        if (base >= 0) {  // uniform per block; no barrier: one slot per warp
+            // Warp sum in the compute precision (FP32 per-node terms carry FP32
+            // rounding already; the FP64 variant stays FP64), only in warps that
+            // hold a force node; the cross-warp sum is FP64.
+            R a = fxs, b = fys;
+            if (__any_sync(0xffffffffu, a != R(0) || b != R(0))) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    a += __shfl_down_sync(0xffffffffu, a, o);
+                    b += __shfl_down_sync(0xffffffffu, b, o);
+                }
+            }
+            const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+            if ((tid & 31) == 0) {
+                const int slot = base + (tid >> 5);
+                p.partials[2 * slot] = double(a);
+                p.partials[2 * slot + 1] = double(b);
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------- paired nodes
+// A thread owns two x-neighbours (x0, x0+1) with x0 even (nx even).  The
+// reference state of each node is rebuilt with the same per-node functions
+// as above; the collision runs on both nodes at once with Blackwell's packed
+// FP32x2 arithmetic (one FFMA2/FADD2/FMUL2 per operation pair) and the
+// populations are written as 8-byte (FP32) or 4-byte (FP16/BF16) pairs.
+struct F2 {
+    float2 v;
+};
+__device__ __forceinline__ F2 mk2(float a, float b) { return {make_float2(a, b)}; }
+__device__ __forceinline__ F2 sp2(float s) { return {make_float2(s, s)}; }
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return {__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return {__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return {__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ F2 rcp2(F2 a) { return mk2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y)); }
+__device__ __forceinline__ F2 sqrt2(F2 a) { return mk2(Fm<float>::sqrt(a.v.x), Fm<float>::sqrt(a.v.y)); }
+
+// Same operator as collide<float, false> on two nodes; lane k is collided
+// only when fluid_k (a solid lane keeps its value).
+__device__ __forceinline__ void collide_pair(const KParams& p, uint32_t fla, uint32_t flb, bool fa_ok, bool fb_ok,
+                                             F2 f[9]) {
+    const Phys<float>& q = p.pf;
+    const F2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    const F2 mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    const F2 my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    const F2 inv = rcp2(rho);
+    const F2 u = mx * inv, v = my * inv;
+    if ((fa_ok && (!(rho.v.x == rho.v.x) || rho.v.x == 0.0f)) || (fb_ok && (!(rho.v.y == rho.v.y) || rho.v.y == 0.0f)))
+        atomicOr(p.nan_flag, 1u);
+    F2 o[9];
+    if (p.collision == 0) {
+        const F2 sd = (f[5] + f[6]) + (f[7] + f[8]), sa = (f[1] + f[2]) + (f[3] + f[4]);
+        F2 me = fma2(sp2(2.0f), sd, fma2(sp2(-4.0f), f[0], sp2(0.0f) - sa));
+        F2 meps = fma2(sp2(4.0f), f[0], sd - sp2(2.0f) * sa);
+        F2 mpxx = (f[1] - f[2]) + (f[3] - f[4]);
+        F2 mpxy = (f[5] - f[6]) + (f[7] - f[8]);
+        const F2 jx = rho * u, jy = rho * v;
+        const F2 usq = fma2(u, u, v * v);
+        const F2 r3u = sp2(3.0f) * rho * usq;
+        const F2 e_eq = fma2(sp2(-2.0f), rho, r3u);
+        const F2 eps_eq = rho - r3u;
+        const F2 pxx_eq = rho * (u * u - v * v);
+        const F2 pxy_eq = jx * v;
+        F2 s_eff = sp2(q.s_shear);
+        if (p.les) {
+            F2 csq = sp2(q.cs_sq);
+            if (q.nu > 0.0f) {
+                const F2 wd = mk2(wall_distance<float>(p, fla), wall_distance<float>(p, flb));
+                const F2 yp = wd * sqrt2(usq + sp2(1e-12f)) * sp2(q.inv_nu);
+                const float dxa = yp.v.x > 0.0f ? q.cs * (1.0f - __expf(-yp.v.x * (1.0f / 26.0f))) : 0.0f;
+                const float dxb = yp.v.y > 0.0f ? q.cs * (1.0f - __expf(-yp.v.y * (1.0f / 26.0f))) : 0.0f;
+                csq = mk2(yp.v.x > 0.0f ? dxa * dxa : q.cs_sq, yp.v.y > 0.0f ? dxb * dxb : q.cs_sq);
+            }
+            const F2 a = mpxx - pxx_eq, b = mpxy - pxy_eq;
+            const F2 Q = sqrt2(sp2(2.0f) * fma2(a, a, b * b));
+            const F2 A = sp2(4.5f) * csq * Q * inv;
+            const F2 te2 = sp2(q.tau) + sqrt2(fma2(sp2(q.tau), sp2(q.tau), sp2(4.0f) * A));
+            const F2 s2 = sp2(2.0f) * rcp2(te2);
+            s_eff = mk2(clamp_rate<float>(s2.v.x), clamp_rate<float>(s2.v.y));
+        }
+        const F2 sb = sp2(q.s_bulk);
+        me = me - sb * (me - e_eq);
+        meps = meps - sb * (meps - eps_eq);
+        mpxx = mpxx - s_eff * (mpxx - pxx_eq);
+        mpxy = mpxy - s_eff * (mpxy - pxy_eq);
+        // s_normal = 1: the energy-flux moments relax to -j (see collide)
+        const F2 a0 = sp2(1.0f / 9.0f) * rho;
+        const F2 ax = a0 - sp2(1.0f / 36.0f) * me - sp2(1.0f / 18.0f) * meps;
+        const F2 ad = fma2(sp2(1.0f / 18.0f), me, fma2(sp2(1.0f / 36.0f), meps, a0));
+        const F2 hx = sp2(1.0f / 3.0f) * jx, hy = sp2(1.0f / 3.0f) * jy;  // (j - q)/6 with q = -j
+        const F2 dx = sp2(1.0f / 12.0f) * jx, dy = sp2(1.0f / 12.0f) * jy;  // j/6 + q/12 with q = -j
+        const F2 px = sp2(0.25f) * mpxx, py = sp2(0.25f) * mpxy;
+        o[0] = a0 - sp2(1.0f / 9.0f) * (me - meps);
+        o[1] = ax + hx + px;
+        o[2] = ax + hy - px;
+        o[3] = ax - hx + px;
+        o[4] = ax - hy - px;
+        o[5] = ad + dx + dy + py;
+        o[6] = ad - dx + dy - py;
+        o[7] = ad - dx - dy + py;
+        o[8] = ad + dx - dy - py;
+    } else {
+        const F2 it = sp2(q.inv_tau), usq = fma2(u, u, v * v);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const F2 ed = sp2(float(CXf(i))) * u + sp2(float(CYf(i))) * v;
+            const F2 poly = fma2(sp2(4.5f) * ed, ed, fma2(sp2(3.0f), ed, sp2(1.0f))) - sp2(1.5f) * usq;
+            const F2 fe = sp2(float(wgt(i))) * rho * poly;
+            o[i] = f[i] - it * (f[i] - fe);
+        }
+    }
+    if (q.Fscale != 0.0f) {
+        const F2 fa = sp2((1.0f / 9.0f) * q.Fscale), fd = sp2((1.0f / 36.0f) * q.Fscale);
+        o[1] = o[1] + fa;
+        o[3] = o[3] - fa;
+        o[5] = o[5] + fd;
+        o[6] = o[6] - fd;
+        o[7] = o[7] - fd;
+        o[8] = o[8] + fd;
+    }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) f[j] = mk2(fa_ok ? o[j].v.x : f[j].v.x, fb_ok ? o[j].v.y : f[j].v.y);
+}
+
+template <class T>
+struct PairStore;
+template <>
+struct PairStore<float> {
+    static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, float, uint32_t) {
+        *reinterpret_cast<float2*>(p + i) = make_float2(a, b);
+    }
+};
+template <>
+struct PairStore<__half> {
+    static __device__ __forceinline__ void st(__half* p, size_t i, float a, float b, float sh, uint32_t rb) {
+        const float o = -sh * kF16Scale;
+        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_f16x2(fmaf(a, kF16Scale, o), fmaf(b, kF16Scale, o), rb);
+    }
+};
+template <>
+struct PairStore<__nv_bfloat16> {
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, size_t i, float a, float b, float sh, uint32_t rb) {
+        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_bf16x2(a - sh, b - sh, rb);
+    }
+};
+
+}  // namespace
+}  // namespace lbm2d

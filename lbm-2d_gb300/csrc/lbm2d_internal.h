@@ -90,6 +90,12 @@ struct KParams {
     int skip_settled_solids;
     int gx;    // width of the instance's block grid (batched launches)
     int pair;  // 1: two x-neighbours per thread (nx even, non-thermal, not FP64)
+    // stochastic-rounding seed of FP16/BF16 stores: a step reads *seed_in and
+    // hands seed + 1 to the next step through *seed_out; a prologue (seed_in
+    // null) uses seed_host
+    const uint32_t* seed_in;
+    uint32_t* seed_out;
+    uint32_t seed_host;
 };
 
 // Readback outputs (any may be null).
@@ -126,5 +132,14 @@ int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, dou
                             void* stream);
 int launch_force_reduce(const double* partials, int nslots, double* hist, int hist_cap,
                         unsigned long long* counter, double* last, void* stream);
+
+// Row-pipelined step (lbm2d_rows.cu): persistent grid of `grid` CTAs, each
+// walking row tiles of rows_tile_width() nodes; p.block_slot has one entry
+// per CTA (first of rows_warps_per_block() per-warp force slots, or -1).
+bool rows_eligible(int storage, int nx, int ny, bool thermal);
+int rows_tile_width();
+int rows_warps_per_block();
+int rows_grid(int storage, int nx, int ny, int device);  // 0 on error
+int launch_rows(int storage, const KParams& p, int grid, void* stream);
 
 }  // namespace lbm2d

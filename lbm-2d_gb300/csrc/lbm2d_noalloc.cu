@@ -60,8 +60,9 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
     // same tau and settings has uploaded the geometry, collided the state and
     // built the force-slot table for the current launch shape.
     const CollideParams c = collide_params(h, tau);
-    if (h->staged || h->geom_dirty || !(c == h->cp_of_P) || h->slot_bx != h->bx || h->slot_by != h->by ||
-        h->slot_pair != (use_pair(h) ? 1 : 0) || !h->d_block_slot)
+    const int kind = kernel_kind(h);
+    if (h->staged || h->geom_dirty || !(c == h->cp_of_P) || h->slot_kind != kind || !h->d_block_slot ||
+        (kind != KERNEL_ROWS && (h->slot_bx != h->bx || h->slot_by != h->by)))
         return fail(h, LBM2D_ERR_STATE,
                     "lbm2d_step_noalloc needs a solver prepared by lbm2d_step with the same tau and settings");
     if (h->nslots > kNoAllocMaxSlots)
@@ -84,8 +85,11 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
         p.fout = h->P[h->cur ^ 1];
         p.gin = h->G[h->cur];
         p.gout = h->G[h->cur ^ 1];
+        p.seed_in = h->d_seed + h->cur;
+        p.seed_out = h->d_seed + (h->cur ^ 1);
         p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
-        int e = launch_step(h->storage, p, h->bx, h->by, h->stream);
+        int e = kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
+                                    : launch_step(h->storage, p, h->bx, h->by, h->stream);
         ++h->launches;
         if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
         if (h->nslots > 0) {

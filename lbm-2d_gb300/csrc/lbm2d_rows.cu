@@ -1,0 +1,420 @@
+// lbm2d_rows.cu -- the row-pipelined step kernel (sm_103a).
+//
+// The same step as step_pair_kernel (pull, rebuild, force, packed FP32x2
+// collision, store), with the pulls served from shared memory that the
+// Blackwell bulk-copy engine fills ahead of the computation:
+//
+//   * work unit = a row tile: W = 512 consecutive nodes of one lattice row
+//     (nx a multiple of 8).  The 9 source rows of a tile (direction j reads
+//     row y - cy_j, x range [x0 - PAD, x0 + W + PAD)) and the tile's flags
+//     are brought in by 10 cp.async.bulk copies (plus 16-byte copies for the
+//     periodic x wrap at the row ends), completing on an mbarrier;
+//   * a persistent grid (a multiple of the SM count) walks the tiles; each
+//     CTA keeps S tiles in flight in a ring of shared-memory stages;
+//   * warp 8 is the producer (one elected lane issues the copies), warps 0-7
+//     consume: each lane owns two x-neighbours of the tile.
+// The copies move the source bytes with no load instructions, so the
+// consumer warps spend their issue slots on the collision and the stores,
+// and the bytes in flight per SM no longer depend on how many warps happen
+// to be waiting on loads.
+//
+// Every wait is bounded: after kWaitCycles SM cycles a waiting thread sets
+// bit 1 of the solver's status word (the host reports a pipeline timeout)
+// and leaves its loop; the producer waits, again bounded, for the copies it
+// issued before it exits.  No wait can time out in a correct launch: the
+// copies of a tile complete in microseconds.
+#include <algorithm>
+#include <atomic>
+
+#include "lbm2d_device.cuh"
+
+namespace lbm2d {
+namespace {
+
+constexpr int kConsumerWarps = 8;
+constexpr int kThreads = 32 * (kConsumerWarps + 1);
+constexpr int kTileW = 2 * 32 * kConsumerWarps;  // nodes per row tile
+constexpr long long kWaitCycles = 2000000000LL;  // about one second at 2 GHz
+
+template <class T>
+struct RowsCfg {
+    static constexpr int ES = (int)sizeof(T);
+    static constexpr int PAD = 16 / ES;  // halo rounded to the 16-byte copy granule
+    static constexpr int SW = kTileW + 2 * PAD;  // elements per staged row
+    static constexpr int ROW_BYTES = SW * ES;
+    static constexpr int FLAGS_OFF = 9 * ROW_BYTES;
+    static constexpr int STAGE_BYTES = ((FLAGS_OFF + kTileW * 4) + 127) / 128 * 128;
+    static constexpr int STAGES = ES == 4 ? 4 : 6;
+    static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
+    static constexpr int SMEM = BAR_OFF + 2 * STAGES * 8;
+    static_assert(ROW_BYTES % 16 == 0 && FLAGS_OFF % 16 == 0, "bulk-copy alignment");
+};
+
+// ----------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of parity `parity` to complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+
+// Global -> shared bulk copy completing `bytes` on the mbarrier (16-byte
+// aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+// ----------------------------------------------------------------- producer
+// Bytes the copies of the tile starting at x0 complete on its mbarrier.
+template <class T>
+__device__ __forceinline__ uint32_t tile_bytes(const KParams& p, int x0) {
+    using C = RowsCfg<T>;
+    const int xs = max(x0 - C::PAD, 0), xe = min(x0 + kTileW + C::PAD, p.nx);
+    uint32_t b = 9u * (uint32_t)((xe - xs) * C::ES);
+    if (x0 == 0) b += 3u * 16u;                  // x = -1 of the three cx = +1 rows
+    if (x0 + kTileW >= p.nx) b += 3u * 16u;      // x = nx of the three cx = -1 rows
+    b += (uint32_t)((min(x0 + kTileW, p.nx) - x0) * 4);  // flags
+    return b;
+}
+
+// Issue the copies of the tile (x0, y) into the stage at shared address st.
+template <class T>
+__device__ __forceinline__ void issue_tile(const KParams& p, int x0, int y, uint32_t st, uint32_t bar) {
+    using C = RowsCfg<T>;
+    const T* __restrict__ P = static_cast<const T*>(p.fin);
+    const size_t N = (size_t)p.N;
+    const int nx = p.nx, ny = p.ny;
+    const int xs = max(x0 - C::PAD, 0), xe = min(x0 + kTileW + C::PAD, nx);
+    const uint32_t dst_off = (uint32_t)((xs - (x0 - C::PAD)) * C::ES);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        int ys = y - CYf(j);
+        ys = ys < 0 ? ys + ny : (ys >= ny ? ys - ny : ys);
+        const T* row = P + j * N + (size_t)ys * nx;
+        const uint32_t rdst = st + (uint32_t)(j * C::ROW_BYTES);
+        bulk_g2s(rdst + dst_off, row + xs, (uint32_t)((xe - xs) * C::ES), bar);
+        if (CXf(j) == 1 && x0 == 0)  // periodic x: x = -1 is x = nx - 1
+            bulk_g2s(rdst, row + (nx - C::PAD), 16u, bar);
+        if (CXf(j) == -1 && x0 + kTileW >= nx)  // x = nx is x = 0
+            bulk_g2s(rdst + (uint32_t)((nx - x0 + C::PAD) * C::ES), row, 16u, bar);
+    }
+    const int fe = min(x0 + kTileW, nx);
+    bulk_g2s(st + C::FLAGS_OFF, p.flags + (size_t)y * nx + x0, (uint32_t)((fe - x0) * 4), bar);
+}
+
+// ----------------------------------------------------------------- consumer
+template <class T>
+struct SmemPair;
+template <>
+struct SmemPair<float> {
+    // elements e, e+1 of a staged row (FP32 is stored unshifted)
+    static __device__ __forceinline__ void aligned(const float* r, int e, float, float& a, float& b) {
+        const float2 v = *reinterpret_cast<const float2*>(r + e);
+        a = v.x;
+        b = v.y;
+    }
+    static __device__ __forceinline__ void any(const float* r, int e, float, float& a, float& b) {
+        a = r[e];
+        b = r[e + 1];
+    }
+};
+template <>
+struct SmemPair<__half> {
+    static __device__ __forceinline__ void aligned(const __half* r, int e, float sh, float& a, float& b) {
+        const float2 v = __half22float2(*reinterpret_cast<const __half2*>(r + e));
+        a = fmaf(v.x, kF16InvScale, sh);
+        b = fmaf(v.y, kF16InvScale, sh);
+    }
+    static __device__ __forceinline__ void any(const __half* r, int e, float sh, float& a, float& b) {
+        a = fmaf(__half2float(r[e]), kF16InvScale, sh);
+        b = fmaf(__half2float(r[e + 1]), kF16InvScale, sh);
+    }
+};
+template <>
+struct SmemPair<__nv_bfloat16> {
+    static __device__ __forceinline__ void aligned(const __nv_bfloat16* r, int e, float sh, float& a, float& b) {
+        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(r + e));
+        a = v.x + sh;
+        b = v.y + sh;
+    }
+    static __device__ __forceinline__ void any(const __nv_bfloat16* r, int e, float sh, float& a, float& b) {
+        a = __bfloat162float(r[e]) + sh;
+        b = __bfloat162float(r[e + 1]) + sh;
+    }
+};
+
+// Nodes (x, x+1) of the tile staged at `stage` (x0 its first node): the
+// reference's post-stream state (pull, bounce-back records, outflow column,
+// boundary conditions), the momentum-exchange force, the collision and the
+// stores -- the body of step_pair_block with shared-memory pulls.
+template <class T>
+__device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
+                                             uint32_t skey, float& fxs, float& fys) {
+    using C = RowsCfg<T>;
+    const uint2 fl = *reinterpret_cast<const uint2*>(stage + C::FLAGS_OFF + (x - x0) * 4);
+    const int e0 = (x - x0) + C::PAD;
+    float fa[9], fb[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const T* r = reinterpret_cast<const T*>(stage + j * C::ROW_BYTES);
+        if (CXf(j) == 0)
+            SmemPair<T>::aligned(r, e0, p.shf[j], fa[j], fb[j]);
+        else
+            SmemPair<T>::any(r, e0 - CXf(j), p.shf[j], fa[j], fb[j]);
+    }
+    const T* __restrict__ Pf = static_cast<const T*>(p.fin);
+    if (fl.x & FLAG_SOLID) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) fa[j] = 0.0f;
+    } else if (fl.x & FLAG_BOUNDARY) {
+        fix_f<T>(p, Pf, x, y, fl.x >> 2, fa);
+    }
+    // zero-gradient outlet: column NX-1 takes NX-2's post-stream state
+    // (src/lbm.hpp:63-73); x + 1 == nx - 1 means x == nx - 2
+    if ((p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x + 1 == p.nx - 1) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) fb[j] = fa[j];
+    } else if (fl.y & FLAG_SOLID) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) fb[j] = 0.0f;
+    } else if (fl.y & FLAG_BOUNDARY) {
+        fix_f<T>(p, Pf, x + 1, y, fl.y >> 2, fb);
+    }
+    apply_bc<float>(p, x, y, fl.x, fa);
+    apply_bc<float>(p, x + 1, y, fl.y, fb);
+    const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
+    if ((fl.x | fl.y) & FLAG_BOUNDARY) {
+        // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
+        const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
+        const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+#pragma unroll
+        for (int j = 1; j < 9; ++j) {
+            if (ma & (1u << j)) {
+                fxs -= float(CXf(j)) * 2.0f * fa[j];
+                fys -= float(CYf(j)) * 2.0f * fa[j];
+            }
+            if (mb & (1u << j)) {
+                fxs -= float(CXf(j)) * 2.0f * fb[j];
+                fys -= float(CYf(j)) * 2.0f * fb[j];
+            }
+        }
+    }
+    if (oka || okb) {
+        F2 f[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
+        collide_pair(p, fl.x, fl.y, oka, okb, f);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            fa[j] = f[j].v.x;
+            fb[j] = f[j].v.y;
+        }
+    }
+    const bool settled = p.skip_settled_solids && y < p.ny - 1;
+    const bool skip_a = !oka && settled && x > 0;
+    const bool skip_b = !okb && settled && x + 1 < p.nx - 1;
+    if (!(skip_a && skip_b)) {
+        T* __restrict__ Fo = static_cast<T*>(p.fout);
+        const size_t N = (size_t)p.N;
+        const size_t n0 = (size_t)y * p.nx + x;
+        uint32_t rb[9] = {};
+        if constexpr (Pop<T>::kRounds) rand9(skey + (uint32_t)n0, rb);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], p.shf[j], rb[j]);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads, 2) step_rows_kernel(const KParams p) {
+    using C = RowsCfg<T>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const uint32_t sbase = smem_u32(smem);
+    const uint32_t full0 = sbase + C::BAR_OFF, empty0 = full0 + 8 * C::STAGES;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tpr = (p.nx + kTileW - 1) / kTileW;
+    const int total = tpr * p.ny;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C::STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, kConsumerWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == kConsumerWarps) {  // producer
+        if (lane != 0) return;
+        int k = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, ++k) {
+            const int s = k % C::STAGES, n = k / C::STAGES;
+            if (n > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1))) {
+                ok = false;
+                break;
+            }
+            const int y = t / tpr, x0 = (t - y * tpr) * kTileW;
+            const uint32_t bar = full0 + 8 * s;
+            mbar_expect_tx(bar, tile_bytes<T>(p, x0));
+            issue_tile<T>(p, x0, y, sbase + (uint32_t)(s * C::STAGE_BYTES), bar);
+        }
+        // every issued copy completes before the CTA may exit
+        bool drained = true;
+        for (int i = max(k - C::STAGES, 0); i < k; ++i)
+            drained = mbar_wait(full0 + 8 * (i % C::STAGES), (uint32_t)((i / C::STAGES) & 1)) && drained;
+        if (!ok || !drained) atomicOr(p.nan_flag, 2u);
+        return;
+    }
+
+    // consumers
+    uint32_t skey = 0;
+    if constexpr (Pop<T>::kRounds) {
+        const uint32_t s = seed_of(p);
+        skey = seed_key(s);
+        pass_seed(p, s, blockIdx.x == 0 && threadIdx.x == 0);
+    }
+    float fxs = 0.0f, fys = 0.0f;
+    double accx = 0.0, accy = 0.0;
+    const bool force = p.block_slot != nullptr;
+    int k = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++k) {
+        const int s = k % C::STAGES, n = k / C::STAGES;
+        if (!mbar_wait(full0 + 8 * s, (uint32_t)(n & 1))) {
+            atomicOr(p.nan_flag, 2u);
+            break;
+        }
+        const int y = t / tpr, x0 = (t - y * tpr) * kTileW;
+        const int x = x0 + 2 * (warp * 32 + lane);
+        const unsigned char* stage = smem + s * C::STAGE_BYTES;
+        if (x < p.nx) consume_pair<T>(p, stage, x0, x, y, skey, fxs, fys);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8 * s);
+        if (force && __any_sync(0xffffffffu, fxs != 0.0f || fys != 0.0f)) {
+            // per tile: FP32 warp sum of the tile's link terms, FP64 across tiles
+            float a = fxs, b = fys;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_down_sync(0xffffffffu, a, o);
+                b += __shfl_down_sync(0xffffffffu, b, o);
+            }
+            accx += double(a);
+            accy += double(b);
+            fxs = fys = 0.0f;
+        }
+    }
+    if (force) {
+        const int base = p.block_slot[blockIdx.x];
+        if (base >= 0 && lane == 0) {
+            p.partials[2 * (base + warp)] = accx;
+            p.partials[2 * (base + warp) + 1] = accy;
+        }
+    }
+}
+
+template <class T>
+int rows_blocks_per_sm() {
+    static int cached = -1;
+    if (cached < 0) {
+        int b = 0;
+        if (cudaFuncSetAttribute(step_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, RowsCfg<T>::SMEM) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, step_rows_kernel<T>, kThreads, RowsCfg<T>::SMEM) !=
+                cudaSuccess)
+            return 0;
+        cached = b;
+    }
+    return cached;
+}
+
+template <class T>
+int rows_grid_t(int nx, int ny, int device) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    const int per = rows_blocks_per_sm<T>();
+    if (per <= 0) return 0;
+    const long long tiles = (long long)((nx + kTileW - 1) / kTileW) * ny;
+    return (int)std::min<long long>(tiles, (long long)sms * per);
+}
+
+template <class T>
+int launch_rows_t(const KParams& p, int grid, cudaStream_t s) {
+    if (grid <= 0) return (int)cudaErrorInvalidConfiguration;
+    // the shared-memory opt-in is per device: set it once for each
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(done.load() & bit)) {
+        e = cudaFuncSetAttribute(step_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, RowsCfg<T>::SMEM);
+        if (e != cudaSuccess) return (int)e;
+        done.fetch_or(bit);
+    }
+    step_rows_kernel<T><<<grid, kThreads, RowsCfg<T>::SMEM, s>>>(p);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+bool rows_eligible(int storage, int nx, int ny, bool thermal) {
+    return !thermal && (storage == ST_FP32 || storage == ST_FP16 || storage == ST_BF16) && nx % 8 == 0 && nx >= 16 &&
+           ny >= 2;
+}
+
+int rows_tile_width() { return kTileW; }
+
+int rows_warps_per_block() { return kConsumerWarps; }
+
+int rows_grid(int storage, int nx, int ny, int device) {
+    switch (storage) {
+        case ST_FP32: return rows_grid_t<float>(nx, ny, device);
+        case ST_FP16: return rows_grid_t<__half>(nx, ny, device);
+        case ST_BF16: return rows_grid_t<__nv_bfloat16>(nx, ny, device);
+    }
+    return 0;
+}
+
+int launch_rows(int storage, const KParams& p, int grid, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_rows_t<float>(p, grid, s);
+        case ST_FP16: return launch_rows_t<__half>(p, grid, s);
+        case ST_BF16: return launch_rows_t<__nv_bfloat16>(p, grid, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace lbm2d

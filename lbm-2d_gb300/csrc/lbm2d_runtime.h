@@ -72,12 +72,13 @@ struct lbm2d_solver {
     double* d_rec_uw = nullptr;
     double* d_partials = nullptr;
     int* d_block_slot = nullptr;
-    int nslots = 0, slot_bx = 0, slot_by = 0, slot_pair = -1;
+    int nslots = 0, slot_bx = 0, slot_by = 0, slot_kind = -1, slot_grid = 0;
     double* d_hist = nullptr;
     int hist_cap = 1 << 18;
     unsigned long long* d_counter = nullptr;
     double* d_last = nullptr;
     unsigned int* d_nan = nullptr;
+    uint32_t* d_seed = nullptr;  // rounding-noise seed words, one per population buffer
     double* d_stage_f = nullptr;
     double* d_stage_g = nullptr;
     double* d_fx = nullptr;
@@ -97,7 +98,10 @@ struct lbm2d_solver {
     long long steps_done = 0;
     long long launches = 0;
     int bx = 128, by = 2;
-    int variant = 0;  // 0: paired kernel where possible, 1: one node per thread
+    // 0: fastest kernel the configuration allows (row pipeline, else paired,
+    // else one node per thread), 1: one node per thread, 2: paired nodes
+    int variant = 0;
+    bool in_batch = false;  // a batch member is stepped by the batched kernels
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;  // even/odd = start/stop
     size_t ev_used = 0;
@@ -127,6 +131,10 @@ int check_handle(lbm2d_solver* h);
 // Two x-neighbours per thread (packed FP32x2 collision) when nx is even and
 // the step is non-thermal FP32/FP16/BF16.
 bool use_pair(const lbm2d_solver* h);
+// Step kernel of the next lbm2d_step: KERNEL_SCALAR, KERNEL_PAIR or
+// KERNEL_ROWS (the bulk-copy row pipeline; single solves only).
+enum KernelKind : int { KERNEL_SCALAR = 0, KERNEL_PAIR = 1, KERNEL_ROWS = 2 };
+int kernel_kind(const lbm2d_solver* h);
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
 // kernel parameters of the next step (fin = current buffer); returns status.
 int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p);

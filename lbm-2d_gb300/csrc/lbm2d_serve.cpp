@@ -1,19 +1,21 @@
 // lbm2d_serve.cpp -- a serving loop for many concurrent solves on one GPU.
 //
 // Requests (grid, geometry, Reynolds number, step budget, storage) arrive at
-// any time through lbm2d_server_submit.  A worker thread
-//   * admits queued requests in arrival order while the device-memory
-//     footprint of the active solves stays within the budget and a slot is
-//     free: it builds the case the way the reference's drivers do (mask,
-//     bounce-back geometry, tau from Re, LES when tau < 0.55, thermal set-up)
-//     and initialises the state on the device;
-//   * advances every active solve together: one lbm2d_batch_step per tick
+// any time through lbm2d_server_submit.
+//   * Set-up threads admit queued requests in arrival order while the
+//     device-memory footprint of the live solves stays within the budget and
+//     a slot is free, and build each case the way the reference's drivers do
+//     (mask, bounce-back geometry and its records, tau from Re, LES when
+//     tau < 0.55, thermal set-up, initial state on the device).  Several
+//     requests are set up at once, on the host cores, while the GPU steps
+//     the others.
+//   * The stepping thread adds the solves that are ready to the batch and
+//     advances every active solve together: one lbm2d_batch_step per tick
 //     (one packed launch per step per storage group, CUDA-graph replay), the
 //     tick being the smallest remaining budget capped at steps_per_tick, so
 //     every solve stops exactly at its budget;
-//   * retires finished solves (drag/lift read back, memory freed) and
-//     records arrival, admission and completion times.
-// New requests are admitted while the GPU works on the current tick.
+//   * it then retires finished solves (non-finite check, drag/lift read back,
+//     memory freed) and records arrival, admission and completion times.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -47,6 +49,7 @@ struct Active {
     long long left = 0;
     double t_submit = 0, t_admit = 0;
     size_t footprint = 0;
+    double tau = 0.0, u_bc = 0.0;
 };
 
 size_t footprint_bytes(const lbm2d_request& r) {
@@ -66,17 +69,24 @@ struct lbm2d_server {
     int steps_per_tick = 0;
     lbm2d_batch* batch = nullptr;
     std::thread worker;
+    std::vector<std::thread> setup_threads;
+    // guarded by mu: queue, ready, results, used, live, counters, stop
     std::mutex mu;
-    std::condition_variable cv;
+    std::condition_variable cv;        // results, ready solves, stop
+    std::condition_variable cv_setup;  // queued requests, freed memory, stop
     std::deque<Pending> queue;
+    std::deque<Active> ready;          // set up, waiting to join the batch
     std::vector<lbm2d_result> results;
-    std::vector<Active> active;
     size_t used = 0;
+    int live = 0;  // being set up + ready + active
     long long next_id = 0, submitted = 0, finished = 0;
-    bool stop = false, running = false;
+    bool stop = false;
+    double setup_s = 0.0;
+    // stepping thread only
+    std::vector<Active> active;
     double busy_s = 0.0;
     long long lattice_updates = 0;
-    std::string err;
+    long long ticks = 0, member_ticks = 0;
 };
 
 namespace {
@@ -161,7 +171,12 @@ int setup_request(lbm2d_server* s, Active& a) {
         u_init = u;  // uniform inflow initial state
     }
     if ((rc = lbm2d_init_equilibrium(a.h, 1.0, u_init, 0.0, 1.0))) return rc;
-    return lbm2d_batch_add(s->batch, a.h, tau, u_bc);
+    lbm2d_info info;  // builds and uploads the geometry here, off the stepping thread
+    if ((rc = lbm2d_get_info(a.h, &info))) return rc;
+    if ((rc = lbm2d_synchronize(a.h))) return rc;
+    a.tau = tau;
+    a.u_bc = u_bc;
+    return LBM2D_OK;
 }
 
 void record(lbm2d_server* s, const Active& a, int status) {
@@ -184,61 +199,106 @@ void record(lbm2d_server* s, const Active& a, int status) {
     s->cv.notify_all();
 }
 
+// Free a solve that is in no batch and give its memory back to admission.
+void release(lbm2d_server* s, const Active& a, int status) {
+    record(s, a, status);
+    if (a.h) lbm2d_destroy(a.h);
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->used -= a.footprint;
+    --s->live;
+    s->cv_setup.notify_all();
+}
+
 void retire(lbm2d_server* s, size_t k, int status) {
     Active a = s->active[k];
     if (a.h) lbm2d_batch_remove(s->batch, a.h);
-    record(s, a, status);
-    if (a.h) lbm2d_destroy(a.h);
-    s->used -= a.footprint;
     s->active.erase(s->active.begin() + k);
+    release(s, a, status);
 }
 
-// Admit queued requests while the budget allows (arrival order).
-void admit(lbm2d_server* s) {
+// Set-up thread: take queued requests in arrival order while the budget
+// allows, build them, hand them to the stepping thread.
+void setup_loop(lbm2d_server* s) {
+    cudaSetDevice(s->device);
     for (;;) {
-        Pending p;
-        {
-            std::lock_guard<std::mutex> lock(s->mu);
-            if (s->queue.empty()) return;
-            const size_t fp = footprint_bytes(s->queue.front().req);
-            if ((int)s->active.size() >= s->max_active) return;
-            if (s->used + fp > s->budget && !s->active.empty()) return;
-            p = s->queue.front();
-            s->queue.pop_front();
-        }
         Active a;
-        a.id = p.id;
-        a.req = p.req;
-        a.left = p.req.steps;
-        a.t_submit = p.t_submit;
-        a.t_admit = now_s();
-        a.footprint = footprint_bytes(p.req);
-        s->used += a.footprint;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv_setup.wait(lock, [&] {
+                if (s->stop) return true;
+                if (s->queue.empty() || s->live >= s->max_active) return false;
+                const size_t fp = footprint_bytes(s->queue.front().req);
+                return s->used + fp <= s->budget || s->live == 0;  // one solve always fits
+            });
+            if (s->stop) return;
+            const Pending p = s->queue.front();
+            s->queue.pop_front();
+            a.id = p.id;
+            a.req = p.req;
+            a.left = p.req.steps;
+            a.t_submit = p.t_submit;
+            a.t_admit = now_s();
+            a.footprint = footprint_bytes(p.req);
+            s->used += a.footprint;
+            ++s->live;
+        }
+        const double t0 = now_s();
         const int rc = setup_request(s, a);
+        const double dt = now_s() - t0;
+        if (rc) {
+            release(s, a, rc);
+            std::lock_guard<std::mutex> lock(s->mu);
+            s->setup_s += dt;
+            continue;
+        }
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->setup_s += dt;
+        s->ready.push_back(a);
+        s->cv.notify_all();
+    }
+}
+
+// Move the solves that are set up into the batch (stepping thread).
+void join_ready(lbm2d_server* s) {
+    std::deque<Active> r;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        r.swap(s->ready);
+    }
+    for (auto& a : r) {
+        const int rc = lbm2d_batch_add(s->batch, a.h, a.tau, a.u_bc);
+        if (rc) {
+            release(s, a, rc);
+            continue;
+        }
         s->active.push_back(a);
-        if (rc) retire(s, s->active.size() - 1, rc);
     }
 }
 
 void worker_loop(lbm2d_server* s) {
     cudaSetDevice(s->device);
     for (;;) {
-        admit(s);
+        join_ready(s);
         if (s->active.empty()) {
             std::unique_lock<std::mutex> lock(s->mu);
             if (s->stop) return;
-            s->cv.wait(lock, [&] { return s->stop || !s->queue.empty(); });
-            if (s->stop && s->queue.empty()) return;
+            s->cv.wait(lock, [&] { return s->stop || !s->ready.empty(); });
+            if (s->stop) return;
             continue;
         }
         long long k = s->steps_per_tick;
         for (auto& a : s->active) k = std::min(k, a.left);
-        // the members of this tick; arrivals admitted below join the next one
+        // the members of this tick; solves joining below wait for the next one
         const size_t n_tick = s->active.size();
         const double t0 = now_s();
         int rc = lbm2d_batch_step(s->batch, (int)k);
-        admit(s);  // host set-up of new arrivals overlaps the GPU work
-        if (!rc) rc = lbm2d_batch_synchronize(s->batch);
+        join_ready(s);  // adding members only edits the host-side member list
+        // wait for the tick only: a diverged solve must not fail the others;
+        // each solve's own non-finite flag is read when it retires
+        if (!rc && cudaStreamSynchronize(static_cast<cudaStream_t>(lbm2d_batch_stream(s->batch))) != cudaSuccess)
+            rc = LBM2D_ERR_CUDA;
+        ++s->ticks;
+        s->member_ticks += (long long)n_tick;
         s->busy_s += now_s() - t0;
         for (size_t i = 0; i < n_tick; ++i) {
             Active& a = s->active[i];
@@ -253,8 +313,6 @@ void worker_loop(lbm2d_server* s) {
                 retire(s, i, st);
             }
         }
-        std::lock_guard<std::mutex> lock(s->mu);
-        if (s->stop && s->queue.empty() && s->active.empty()) return;
     }
 }
 
@@ -274,8 +332,10 @@ int lbm2d_server_create(int device, double budget_bytes, int max_active, int ste
         delete s;
         return rc;
     }
-    s->running = true;
     s->worker = std::thread(worker_loop, s);
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int n_setup = (int)std::max(1u, std::min(hw > 2 ? hw - 2 : 1u, 6u));
+    for (int k = 0; k < n_setup; ++k) s->setup_threads.emplace_back(setup_loop, s);
     *out = s;
     return LBM2D_OK;
 }
@@ -288,7 +348,7 @@ int lbm2d_server_submit(lbm2d_server* s, const lbm2d_request* r, long long* id) 
     s->queue.push_back(p);
     ++s->submitted;
     if (id) *id = p.id;
-    s->cv.notify_all();
+    s->cv_setup.notify_all();
     return LBM2D_OK;
 }
 
@@ -315,10 +375,13 @@ int lbm2d_server_stats(lbm2d_server* s, lbm2d_server_stats_t* st) {
     st->submitted = s->submitted;
     st->finished = s->finished;
     st->queued = (long long)s->queue.size();
-    st->active = (long long)s->active.size();
+    st->active = (long long)s->live;
+    st->setup_s = s->setup_s;
     st->busy_s = s->busy_s;
     st->lattice_updates = s->lattice_updates;
     st->device_bytes_in_use = (double)s->used;
+    st->ticks = s->ticks;
+    st->member_ticks = s->member_ticks;
     return LBM2D_OK;
 }
 
@@ -329,8 +392,13 @@ int lbm2d_server_destroy(lbm2d_server* s) {
         s->stop = true;
         s->queue.clear();
         s->cv.notify_all();
+        s->cv_setup.notify_all();
     }
     if (s->worker.joinable()) s->worker.join();
+    for (auto& t : s->setup_threads)
+        if (t.joinable()) t.join();
+    for (size_t k = s->active.size(); k-- > 0;) retire(s, k, LBM2D_ERR_STATE);
+    join_ready(s);  // set up but never stepped
     for (size_t k = s->active.size(); k-- > 0;) retire(s, k, LBM2D_ERR_STATE);
     lbm2d_batch_destroy(s->batch);
     delete s;

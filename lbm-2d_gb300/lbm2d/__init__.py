@@ -24,6 +24,7 @@ MRT, BGK = 0, 1
 STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2, "fp64": 3}
 BYTES_PER_POP = {"fp32": 4, "fp16": 2, "bf16": 2, "fp64": 8}
 HOOK_NONE, HOOK_HEATED_CAVITY, HOOK_HEATED_SOLIDS = 0, 1, 2
+KERNEL_SCALAR, KERNEL_PAIR, KERNEL_ROWS = 0, 1, 2
 
 ERRORS = {1: "invalid argument", 2: "out of device memory", 3: "CUDA error", 4: "non-finite density",
           5: "call out of order", 6: "no CUDA device", 7: "device wait timed out"}
@@ -43,7 +44,7 @@ class Config(C.Structure):
 class Info(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("storage", C.c_int), ("bytes_per_update", C.c_double),
                 ("device_bytes", C.c_size_t), ("n_boundary_nodes", C.c_int), ("n_force_nodes", C.c_int),
-                ("steps_done", C.c_longlong), ("block_x", C.c_int), ("block_y", C.c_int)]
+                ("steps_done", C.c_longlong), ("block_x", C.c_int), ("block_y", C.c_int), ("kernel", C.c_int)]
 
 
 class BBGeometry(C.Structure):
@@ -66,7 +67,8 @@ class Result(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("finished", C.c_longlong), ("queued", C.c_longlong),
                 ("active", C.c_longlong), ("busy_s", C.c_double), ("lattice_updates", C.c_longlong),
-                ("device_bytes_in_use", C.c_double)]
+                ("device_bytes_in_use", C.c_double), ("ticks", C.c_longlong), ("member_ticks", C.c_longlong),
+                ("setup_s", C.c_double)]
 
 
 class ForceStats(C.Structure):
@@ -375,7 +377,10 @@ class Solver:
         self._ck(self.L.lbm2d_set_block(self.h, int(bx), int(by)))
 
     def set_kernel_variant(self, variant: int):
-        """0: paired nodes per thread where possible (default), 1: one node per thread."""
+        """0 (default): fastest kernel the configuration allows (row pipeline,
+        else paired nodes, else one node per thread); 1: one node per thread;
+        2: paired nodes per thread.  `info().kernel` reports the kernel in use
+        (KERNEL_SCALAR / KERNEL_PAIR / KERNEL_ROWS)."""
         self._ck(self.L.lbm2d_set_kernel_variant(self.h, int(variant)))
 
     # -- state

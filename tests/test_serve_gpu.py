@@ -1,10 +1,16 @@
 """Serving loop: requests of different sizes, geometries and budgets are
-admitted, stepped together and retired exactly at their budgets; every
-served result matches the same request solved alone with the plain
-per-solve API -- drag/lift within 1e-6 relative, and 1e-4 for the closed
-heated cavity, whose net wall force is a small difference of large wall
-terms that amplifies rounding differences between the batched and the
-single-solve kernels -- and admission respects the device-memory budget."""
+admitted, stepped together and retired exactly at their budgets.
+
+* Co-scheduling invariance: a request served in the mix gives bit-for-bit
+  the drag/lift it gives when it is the only request of a serving loop.
+* Against the plain per-solve API (a separately compiled kernel), drag/lift
+  agree within 1e-6 relative, except for the closed heated cavity, whose net
+  wall force is a small difference of large wall terms: 1e-4 in FP32 and
+  2e-3 in FP16.  FP16 is stored with stochastic rounding, which carries an
+  ulp-level FP32 difference between two kernels forward as a random walk
+  (round-to-nearest would mostly absorb it), so two FP16 runs differ by up
+  to the storage precision.
+* Admission respects the device-memory budget."""
 import time
 
 import numpy as np
@@ -49,8 +55,30 @@ def test_served_results_match_alone(product, storage):
             continue  # the cavity has no momentum-exchange pass
         fx, fy = _alone(product, r, storage)
         scale = max(abs(fx), abs(fy), 1e-12)
-        tol = 1e-4 if r["geometry"] == 4 else 1e-6
+        tol = (1e-4 if storage == "fp32" else 2e-3) if r["geometry"] == 4 else 1e-6
         assert abs(x["fx"] - fx) <= tol * scale and abs(x["fy"] - fy) <= tol * scale, (r, x, fx, fy)
+
+
+def _serve(product, reqs, storage, tick):
+    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=tick)
+    ids = [srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"]) for r in reqs]
+    assert srv.wait(len(reqs), 120)
+    res = {x["id"]: x for x in srv.results()}
+    srv.close()
+    return [res[i] for i in ids]
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_mix_equals_alone_bit_for_bit(product, storage):
+    """Every request alone in a serving loop and the same request among the
+    others (different tick boundaries, other solves in the same launches)
+    end with identical drag/lift."""
+    mixed = _serve(product, REQS, storage, 64)
+    for r, x in zip(REQS, mixed):
+        (a,) = _serve(product, [r], storage, 64)
+        assert x["status"] == 0 and a["status"] == 0
+        assert x["steps"] == a["steps"] == r["steps"]
+        assert x["fx"] == a["fx"] and x["fy"] == a["fy"], (r, x, a)
 
 
 def test_admission_respects_memory_budget(product):
