@@ -125,7 +125,7 @@ KParams base_params(const lbm2d_solver* h) {
     p.pair = use_pair(h) ? 1 : 0;
     const int nbw = h->bx * (p.pair ? 2 : 1);  // node width of a block
     p.gx = (h->nx + nbw - 1) / nbw;
-    const bool shifted = h->storage == ST_FP16 || h->storage == ST_BF16;
+    const bool shifted = h->storage != ST_FP64;  // FP32/FP16/BF16 store deviations
     for (int j = 0; j < 9; ++j) {
         p.shf[j] = shifted ? float(W[j]) : 0.0f;
         p.shg[j] = shifted ? float(W[j] * h->T_ref) : 0.0f;

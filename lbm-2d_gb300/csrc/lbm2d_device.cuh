@@ -23,9 +23,9 @@ static_assert(BBf(5) == 7 && BBf(6) == 8 && BBf(7) == 5 && BBf(8) == 6, "bounce-
 __host__ __device__ constexpr double wgt(int i) { return i == 0 ? 4.0 / 9.0 : (i < 5 ? 1.0 / 9.0 : 1.0 / 36.0); }
 
 // ----------------------------------------------------------------- storage formats
-// FP16/BF16 hold shifted deviations d = f - w_i*rho0 (g - w_i*T_ref); FP16
-// stores d * 2^12 so that small deviations stay clear of the FP16 subnormal
-// range (|d| < 16 fits).  Both are written with STOCHASTIC rounding
+// FP32/FP16/BF16 hold shifted deviations d = f - w_i*rho0 (g - w_i*T_ref),
+// FP64 holds f itself.  FP16 stores d * 2^12 so that small deviations stay
+// clear of the FP16 subnormal range (|d| < 16 fits).  Both are written with STOCHASTIC rounding
 // (Blackwell cvt.rs, one 32-bit random word per two values): round-to-nearest
 // makes the same rounding error at every node of a near-uniform flow on
 // every step, which drifts the conserved moments linearly in time; rounding
@@ -47,14 +47,21 @@ __device__ __forceinline__ uint32_t cvt_rs_bf16x2(float a, float b, uint32_t rb)
     return d;
 }
 
+// ldd/std move the stored DEVIATION (the FP32 compute path works on
+// deviations); ld/st move the full population f = deviation + sh (FP64
+// stores f itself, sh = 0).
 template <class T>
 struct Pop;
 template <>
 struct Pop<float> {
     using R = float;
     static constexpr bool kRounds = false;
-    static __device__ __forceinline__ R ld(const float* __restrict__ p, size_t i, float) { return __ldg(p + i); }
-    static __device__ __forceinline__ void st(float* __restrict__ p, size_t i, R v, float, uint32_t) { p[i] = v; }
+    static __device__ __forceinline__ float ldd(const float* __restrict__ p, size_t i) { return __ldg(p + i); }
+    static __device__ __forceinline__ void std_(float* __restrict__ p, size_t i, float d, uint32_t) { p[i] = d; }
+    static __device__ __forceinline__ R ld(const float* __restrict__ p, size_t i, float sh) { return __ldg(p + i) + sh; }
+    static __device__ __forceinline__ void st(float* __restrict__ p, size_t i, R v, float sh, uint32_t) {
+        p[i] = v - sh;
+    }
 };
 template <>
 struct Pop<double> {
@@ -67,24 +74,35 @@ template <>
 struct Pop<__half> {
     using R = float;
     static constexpr bool kRounds = true;
+    static __device__ __forceinline__ float ldd(const __half* __restrict__ p, size_t i) {
+        return __half2float(__ldg(p + i)) * kF16InvScale;
+    }
+    static __device__ __forceinline__ void std_(__half* __restrict__ p, size_t i, float d, uint32_t rb) {
+        const float x = d * kF16Scale;
+        p[i] = __ushort_as_half((unsigned short)(cvt_rs_f16x2(x, x, rb) & 0xFFFFu));
+    }
     static __device__ __forceinline__ R ld(const __half* __restrict__ p, size_t i, float sh) {
         return fmaf(__half2float(__ldg(p + i)), kF16InvScale, sh);
     }
     static __device__ __forceinline__ void st(__half* __restrict__ p, size_t i, R v, float sh, uint32_t rb) {
-        const float d = fmaf(v, kF16Scale, -sh * kF16Scale);
-        p[i] = __ushort_as_half((unsigned short)(cvt_rs_f16x2(d, d, rb) & 0xFFFFu));
+        std_(p, i, v - sh, rb);
     }
 };
 template <>
 struct Pop<__nv_bfloat16> {
     using R = float;
     static constexpr bool kRounds = true;
+    static __device__ __forceinline__ float ldd(const __nv_bfloat16* __restrict__ p, size_t i) {
+        return __bfloat162float(__ldg(p + i));
+    }
+    static __device__ __forceinline__ void std_(__nv_bfloat16* __restrict__ p, size_t i, float d, uint32_t rb) {
+        p[i] = __ushort_as_bfloat16((unsigned short)(cvt_rs_bf16x2(d, d, rb) & 0xFFFFu));
+    }
     static __device__ __forceinline__ R ld(const __nv_bfloat16* __restrict__ p, size_t i, float sh) {
         return __bfloat162float(__ldg(p + i)) + sh;
     }
     static __device__ __forceinline__ void st(__nv_bfloat16* __restrict__ p, size_t i, R v, float sh, uint32_t rb) {
-        const float d = v - sh;
-        p[i] = __ushort_as_bfloat16((unsigned short)(cvt_rs_bf16x2(d, d, rb) & 0xFFFFu));
+        std_(p, i, v - sh, rb);
     }
 };
 
@@ -465,6 +483,181 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
     }
 }
 
+// ----------------------------------------------------------------- deviation form
+// The FP32 compute path (FP32/FP16/BF16 storage) keeps every population as
+// its deviation d_i = f_i - w_i (g: e_i = g_i - w_i*T_ref) in registers.  A
+// deviation is ~10x smaller than f_i, so its FP32 rounding is ~10x finer;
+// the density enters as drho = sum d_i, the momentum as the exact moment
+// sum c_i d_i (never rebuilt as rho * (m / rho) through an approximate
+// reciprocal, which would break momentum conservation by ~1e-7 per step),
+// and the body force is folded into the momentum terms of the inverse
+// transform before the final rounding instead of being added to the rounded
+// populations, where an increment below half an ulp of f_i vanishes.  In
+// exact arithmetic every step below equals the full-population step.
+//
+// Nodes whose post-stream state is more than the plain pull (solid,
+// boundary record, a boundary-condition row or column, a thermal hook) are
+// rebuilt through build_state on full populations and converted back.
+template <bool TH>
+__device__ __forceinline__ bool special_node(const KParams& p, int x, int y, uint32_t fl) {
+    if (fl & (FLAG_SOLID | FLAG_BOUNDARY)) return true;
+    if (p.bc_kind == BC_LID) {
+        if (y == p.ny - 1) return true;
+    } else if (p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) {
+        if (x == 0 || x == p.nx - 1) return true;
+    }
+    if (TH && p.hook_kind == 1 && (x == 1 || x == p.nx - 2 || y == 1 || y == p.ny - 2)) return true;
+    return false;
+}
+
+template <class T>
+__device__ __forceinline__ void pull_dev(const KParams& p, const T* __restrict__ P, int x, int y, float d[9]) {
+    const unsigned nx = (unsigned)p.nx, ny = (unsigned)p.ny;
+    const size_t N = (size_t)p.N;
+    const unsigned ux = (unsigned)x, uy = (unsigned)y;
+    const unsigned xm = ux == 0 ? nx - 1 : ux - 1, xp = ux == nx - 1 ? 0 : ux + 1;
+    const unsigned ym = uy == 0 ? ny - 1 : uy - 1, yp = uy == ny - 1 ? 0 : uy + 1;
+    const unsigned r0 = uy * nx, rm = ym * nx, rp = yp * nx;
+    d[0] = Pop<T>::ldd(P, r0 + ux);
+    d[1] = Pop<T>::ldd(P + N, r0 + xm);
+    d[2] = Pop<T>::ldd(P + 2 * N, rm + ux);
+    d[3] = Pop<T>::ldd(P + 3 * N, r0 + xp);
+    d[4] = Pop<T>::ldd(P + 4 * N, rp + ux);
+    d[5] = Pop<T>::ldd(P + 5 * N, rm + xm);
+    d[6] = Pop<T>::ldd(P + 6 * N, rm + xp);
+    d[7] = Pop<T>::ldd(P + 7 * N, rp + xp);
+    d[8] = Pop<T>::ldd(P + 8 * N, rp + xm);
+}
+
+// Post-stream state of node (x, y) as deviations; returns true for a special
+// node (built on full populations).
+template <class T, bool TH>
+__device__ __forceinline__ bool build_dev(const KParams& p, int x, int y, uint32_t fl, float d[9], float e[9]) {
+    if (!special_node<TH>(p, x, y, fl)) {
+        pull_dev<T>(p, static_cast<const T*>(p.fin), x, y, d);
+        if (TH) pull_dev<T>(p, static_cast<const T*>(p.gin), x, y, e);
+        return false;
+    }
+    float f[9], g[9];
+    build_state<T, TH>(p, x, y, fl, f, g);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) d[j] = f[j] - p.shf[j];
+    if (TH) {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) e[j] = g[j] - p.shg[j];
+    }
+    return true;
+}
+
+// Collision of one fluid node on deviations (same operator as collide<R, TH>).
+template <bool TH>
+__device__ __forceinline__ void collide_dev(const KParams& p, uint32_t fl, float d[9], float e[9]) {
+    const Phys<float>& q = p.pf;
+    const float drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+    const float mx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
+    const float my = (d[2] - d[4]) + (d[5] + d[6]) - (d[7] + d[8]);
+    const float rho = 1.0f + drho;
+    if (!(rho == rho) || rho == 0.0f) atomicOr(p.nan_flag, 1u);
+    const float inv = Fm<float>::rcp(rho);
+    const float u = mx * inv, v = my * inv;
+    const float F = q.Fscale;
+    if (p.collision == 0) {
+        const float sd = (d[5] + d[6]) + (d[7] + d[8]), sa = (d[1] + d[2]) + (d[3] + d[4]);
+        float me = fmaf(2.0f, sd, fmaf(-4.0f, d[0], -sa));   // e + 2
+        float meps = fmaf(4.0f, d[0], fmaf(-2.0f, sa, sd));  // eps - 1
+        float mpxx = (d[1] - d[2]) + (d[3] - d[4]);
+        float mpxy = (d[5] - d[6]) + (d[7] - d[8]);
+        const float r3u = 3.0f * fmaf(mx, u, my * v);  // 3 rho |u|^2
+        const float e_eq = fmaf(-2.0f, drho, r3u);     // e_eq + 2
+        const float eps_eq = drho - r3u;               // eps_eq - 1
+        const float pxx_eq = fmaf(mx, u, -(my * v));   // rho (u^2 - v^2)
+        const float pxy_eq = mx * v;                   // rho u v
+        float s_eff = q.s_shear;
+        if (p.les) {
+            float csq = q.cs_sq;
+            if (q.nu > 0.0f) {
+                const float wd = wall_distance<float>(p, fl);
+                const float yp = wd * Fm<float>::sqrt(fmaf(u, u, v * v) + 1e-12f) * q.inv_nu;
+                if (yp > 0.0f) {
+                    const float cd = q.cs * (1.0f - Fm<float>::exp(-yp * (1.0f / 26.0f)));
+                    csq = cd * cd;
+                }
+            }
+            const float a = mpxx - pxx_eq, b = mpxy - pxy_eq;
+            const float Q = Fm<float>::sqrt(2.0f * fmaf(a, a, b * b));
+            const float A = 4.5f * csq * Q * inv;
+            const float te2 = q.tau + Fm<float>::sqrt(fmaf(q.tau, q.tau, 4.0f * A));
+            s_eff = clamp_rate<float>(2.0f * Fm<float>::rcp(te2));
+        }
+        me -= q.s_bulk * (me - e_eq);
+        meps -= q.s_bulk * (meps - eps_eq);
+        mpxx -= s_eff * (mpxx - pxx_eq);
+        mpxy -= s_eff * (mpxy - pxy_eq);
+        // inverse transform with s_normal = 1 (q = -j) and the body force
+        // w_i c_xi F folded into the x momentum terms
+        const float a0 = (1.0f / 9.0f) * drho;
+        const float ax = a0 - (1.0f / 36.0f) * me - (1.0f / 18.0f) * meps;
+        const float ad = fmaf(1.0f / 18.0f, me, fmaf(1.0f / 36.0f, meps, a0));
+        const float hx = fmaf(1.0f / 3.0f, mx, (1.0f / 9.0f) * F), hy = (1.0f / 3.0f) * my;
+        const float dx = fmaf(1.0f / 12.0f, mx, (1.0f / 36.0f) * F), dy = (1.0f / 12.0f) * my;
+        const float px = 0.25f * mpxx, py = 0.25f * mpxy;
+        d[0] = a0 - (1.0f / 9.0f) * (me - meps);
+        d[1] = ax + hx + px;
+        d[2] = ax + hy - px;
+        d[3] = ax - hx + px;
+        d[4] = ax - hy - px;
+        d[5] = ad + dx + dy + py;
+        d[6] = ad - dx + dy - py;
+        d[7] = ad - dx - dy + py;
+        d[8] = ad + dx - dy - py;
+    } else {
+        // BGK: f_eq - w = w (drho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 |u|^2))
+        const float it = q.inv_tau, usq = fmaf(u, u, v * v);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const float cj = float(CXf(i)) * mx + float(CYf(i)) * my;
+            const float ed = float(CXf(i)) * u + float(CYf(i)) * v;
+            const float fe = float(wgt(i)) * (fmaf(3.0f, cj, drho) + rho * fmaf(4.5f * ed, ed, -1.5f * usq));
+            d[i] -= it * (d[i] - fe);
+        }
+        if (F != 0.0f) {
+            const float fa = (1.0f / 9.0f) * F, fd = (1.0f / 36.0f) * F;
+            d[1] += fa;
+            d[3] -= fa;
+            d[5] += fd;
+            d[6] -= fd;
+            d[7] -= fd;
+            d[8] += fd;
+        }
+    }
+    if (TH) {
+        // thermal DDF on deviations: T = T_ref + dT, u from the post-collision f
+        const float drho2 = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+        const float mx2 = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
+        const float my2 = (d[2] - d[4]) + (d[5] + d[6]) - (d[7] + d[8]);
+        const float inv2 = Fm<float>::rcp(1.0f + drho2);
+        const float u2 = mx2 * inv2, v2 = my2 * inv2, usq2 = fmaf(u2, u2, v2 * v2);
+        const float dT = ((e[0] + e[1]) + (e[2] + e[3])) + ((e[4] + e[5]) + (e[6] + e[7])) + e[8];
+        const float T = q.T_ref + dT;
+        const float om = q.omega_k;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const float ed = float(CXf(i)) * u2 + float(CYf(i)) * v2;
+            const float ge = float(wgt(i)) * fmaf(T, fmaf(4.5f * ed, ed, fmaf(3.0f, ed, -1.5f * usq2)), dT);
+            e[i] -= om * (e[i] - ge);
+        }
+        if (q.beta > 0.0f && q.g_buoy != 0.0f) {
+            const float fyb = -q.beta * dT * q.g_buoy;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const float eu = float(CXf(i)) * u2 + float(CYf(i)) * v2;
+                const float Fd = float(CYf(i)) * fyb;
+                d[i] += float(wgt(i)) * (3.0f * Fd + 9.0f * eu * Fd);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ void block_reduce2(double& a, double& b) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -507,8 +700,11 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
     if (x < p.nx && y < p.ny) {
         const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
         const uint32_t fl = __ldg(p.flags + n);
-        R f[9], g[9];
-        build_state<T, TH>(p, x, y, fl, f, g);
+        R f[9], g[9];  // FP64: populations; FP32 compute: deviations
+        if constexpr (std::is_same<T, double>::value)
+            build_state<T, TH>(p, x, y, fl, f, g);
+        else
+            build_dev<T, TH>(p, x, y, fl, f, g);
         if (!(fl & FLAG_SOLID)) {
             if (fl & FLAG_BOUNDARY) {
                 // momentum exchange of this node's links (src/lbm.hpp:565-577)
@@ -516,24 +712,38 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
 #pragma unroll
                 for (int j = 1; j < 9; ++j)
                     if (fm & (1u << j)) {
-                        fxs -= R(CXf(j)) * R(2) * f[j];
-                        fys -= R(CYf(j)) * R(2) * f[j];
+                        const R fj = f[j] + R(p.shf[j]);
+                        fxs -= R(CXf(j)) * R(2) * fj;
+                        fys -= R(CYf(j)) * R(2) * fj;
                     }
             }
-            collide<R, TH>(p, fl, f, g);
+            if constexpr (std::is_same<T, double>::value)
+                collide<R, TH>(p, fl, f, g);
+            else
+                collide_dev<TH>(p, fl, f, g);
         }
         T* __restrict__ Fo = static_cast<T*>(p.fout);
         const size_t N = (size_t)p.N;
         if (!((fl & FLAG_SOLID) && p.skip_settled_solids && x > 0 && x < p.nx - 1 && y < p.ny - 1)) {
-            uint32_t rb[9] = {};
-            if constexpr (Pop<T>::kRounds) rand9(skey + n, rb);
+            if constexpr (std::is_same<T, double>::value) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) Pop<T>::st(Fo + j * N, n, f[j], p.shf[j], rb[j]);
-            if (TH) {
-                T* __restrict__ Go = static_cast<T*>(p.gout);
-                if constexpr (Pop<T>::kRounds) rand9((skey + n) ^ 0x6A09E667u, rb);
+                for (int j = 0; j < 9; ++j) Fo[j * N + n] = f[j];
+                if (TH) {
+                    T* __restrict__ Go = static_cast<T*>(p.gout);
 #pragma unroll
-                for (int j = 0; j < 9; ++j) Pop<T>::st(Go + j * N, n, g[j], p.shg[j], rb[j]);
+                    for (int j = 0; j < 9; ++j) Go[j * N + n] = g[j];
+                }
+            } else {
+                uint32_t rb[9] = {};
+                if constexpr (Pop<T>::kRounds) rand9(skey + n, rb);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) Pop<T>::std_(Fo + j * N, n, f[j], rb[j]);
+                if (TH) {
+                    T* __restrict__ Go = static_cast<T*>(p.gout);
+                    if constexpr (Pop<T>::kRounds) rand9((skey + n) ^ 0x6A09E667u, rb);
+#pragma unroll
+                    for (int j = 0; j < 9; ++j) Pop<T>::std_(Go + j * N, n, g[j], rb[j]);
+                }
             }
         }
     }
@@ -579,38 +789,38 @@ __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return {__ffma2_rn(a.v, b
 __device__ __forceinline__ F2 rcp2(F2 a) { return mk2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y)); }
 __device__ __forceinline__ F2 sqrt2(F2 a) { return mk2(Fm<float>::sqrt(a.v.x), Fm<float>::sqrt(a.v.y)); }
 
-// Same operator as collide<float, false> on two nodes; lane k is collided
-// only when fluid_k (a solid lane keeps its value).
-__device__ __forceinline__ void collide_pair(const KParams& p, uint32_t fla, uint32_t flb, bool fa_ok, bool fb_ok,
-                                             F2 f[9]) {
+// collide_dev<false> on two nodes at once (FP32x2); lane k is collided only
+// when ok_k (a solid lane keeps its value).
+__device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla, uint32_t flb, bool fa_ok,
+                                                 bool fb_ok, F2 d[9]) {
     const Phys<float>& q = p.pf;
-    const F2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
-    const F2 mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
-    const F2 my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    const F2 drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+    const F2 mx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
+    const F2 my = (d[2] - d[4]) + (d[5] + d[6]) - (d[7] + d[8]);
+    const F2 rho = sp2(1.0f) + drho;
     const F2 inv = rcp2(rho);
     const F2 u = mx * inv, v = my * inv;
     if ((fa_ok && (!(rho.v.x == rho.v.x) || rho.v.x == 0.0f)) || (fb_ok && (!(rho.v.y == rho.v.y) || rho.v.y == 0.0f)))
         atomicOr(p.nan_flag, 1u);
+    const float F = q.Fscale;
     F2 o[9];
     if (p.collision == 0) {
-        const F2 sd = (f[5] + f[6]) + (f[7] + f[8]), sa = (f[1] + f[2]) + (f[3] + f[4]);
-        F2 me = fma2(sp2(2.0f), sd, fma2(sp2(-4.0f), f[0], sp2(0.0f) - sa));
-        F2 meps = fma2(sp2(4.0f), f[0], sd - sp2(2.0f) * sa);
-        F2 mpxx = (f[1] - f[2]) + (f[3] - f[4]);
-        F2 mpxy = (f[5] - f[6]) + (f[7] - f[8]);
-        const F2 jx = rho * u, jy = rho * v;
-        const F2 usq = fma2(u, u, v * v);
-        const F2 r3u = sp2(3.0f) * rho * usq;
-        const F2 e_eq = fma2(sp2(-2.0f), rho, r3u);
-        const F2 eps_eq = rho - r3u;
-        const F2 pxx_eq = rho * (u * u - v * v);
-        const F2 pxy_eq = jx * v;
+        const F2 sd = (d[5] + d[6]) + (d[7] + d[8]), sa = (d[1] + d[2]) + (d[3] + d[4]);
+        F2 me = fma2(sp2(2.0f), sd, fma2(sp2(-4.0f), d[0], sp2(0.0f) - sa));  // e + 2
+        F2 meps = fma2(sp2(4.0f), d[0], fma2(sp2(-2.0f), sa, sd));            // eps - 1
+        F2 mpxx = (d[1] - d[2]) + (d[3] - d[4]);
+        F2 mpxy = (d[5] - d[6]) + (d[7] - d[8]);
+        const F2 r3u = sp2(3.0f) * fma2(mx, u, my * v);
+        const F2 e_eq = fma2(sp2(-2.0f), drho, r3u);
+        const F2 eps_eq = drho - r3u;
+        const F2 pxx_eq = fma2(mx, u, sp2(0.0f) - my * v);
+        const F2 pxy_eq = mx * v;
         F2 s_eff = sp2(q.s_shear);
         if (p.les) {
             F2 csq = sp2(q.cs_sq);
             if (q.nu > 0.0f) {
                 const F2 wd = mk2(wall_distance<float>(p, fla), wall_distance<float>(p, flb));
-                const F2 yp = wd * sqrt2(usq + sp2(1e-12f)) * sp2(q.inv_nu);
+                const F2 yp = wd * sqrt2(fma2(u, u, v * v) + sp2(1e-12f)) * sp2(q.inv_nu);
                 const float dxa = yp.v.x > 0.0f ? q.cs * (1.0f - __expf(-yp.v.x * (1.0f / 26.0f))) : 0.0f;
                 const float dxb = yp.v.y > 0.0f ? q.cs * (1.0f - __expf(-yp.v.y * (1.0f / 26.0f))) : 0.0f;
                 csq = mk2(yp.v.x > 0.0f ? dxa * dxa : q.cs_sq, yp.v.y > 0.0f ? dxb * dxb : q.cs_sq);
@@ -627,12 +837,11 @@ __device__ __forceinline__ void collide_pair(const KParams& p, uint32_t fla, uin
         meps = meps - sb * (meps - eps_eq);
         mpxx = mpxx - s_eff * (mpxx - pxx_eq);
         mpxy = mpxy - s_eff * (mpxy - pxy_eq);
-        // s_normal = 1: the energy-flux moments relax to -j (see collide)
-        const F2 a0 = sp2(1.0f / 9.0f) * rho;
+        const F2 a0 = sp2(1.0f / 9.0f) * drho;
         const F2 ax = a0 - sp2(1.0f / 36.0f) * me - sp2(1.0f / 18.0f) * meps;
         const F2 ad = fma2(sp2(1.0f / 18.0f), me, fma2(sp2(1.0f / 36.0f), meps, a0));
-        const F2 hx = sp2(1.0f / 3.0f) * jx, hy = sp2(1.0f / 3.0f) * jy;  // (j - q)/6 with q = -j
-        const F2 dx = sp2(1.0f / 12.0f) * jx, dy = sp2(1.0f / 12.0f) * jy;  // j/6 + q/12 with q = -j
+        const F2 hx = fma2(sp2(1.0f / 3.0f), mx, sp2((1.0f / 9.0f) * F)), hy = sp2(1.0f / 3.0f) * my;
+        const F2 dx = fma2(sp2(1.0f / 12.0f), mx, sp2((1.0f / 36.0f) * F)), dy = sp2(1.0f / 12.0f) * my;
         const F2 px = sp2(0.25f) * mpxx, py = sp2(0.25f) * mpxy;
         o[0] = a0 - sp2(1.0f / 9.0f) * (me - meps);
         o[1] = ax + hx + px;
@@ -647,44 +856,45 @@ __device__ __forceinline__ void collide_pair(const KParams& p, uint32_t fla, uin
         const F2 it = sp2(q.inv_tau), usq = fma2(u, u, v * v);
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
+            const F2 cj = sp2(float(CXf(i))) * mx + sp2(float(CYf(i))) * my;
             const F2 ed = sp2(float(CXf(i))) * u + sp2(float(CYf(i))) * v;
-            const F2 poly = fma2(sp2(4.5f) * ed, ed, fma2(sp2(3.0f), ed, sp2(1.0f))) - sp2(1.5f) * usq;
-            const F2 fe = sp2(float(wgt(i))) * rho * poly;
-            o[i] = f[i] - it * (f[i] - fe);
+            const F2 fe = sp2(float(wgt(i))) * (fma2(sp2(3.0f), cj, drho) +
+                                                 rho * fma2(sp2(4.5f) * ed, ed, sp2(-1.5f) * usq));
+            o[i] = d[i] - it * (d[i] - fe);
+        }
+        if (F != 0.0f) {
+            const F2 fa = sp2((1.0f / 9.0f) * F), fd = sp2((1.0f / 36.0f) * F);
+            o[1] = o[1] + fa;
+            o[3] = o[3] - fa;
+            o[5] = o[5] + fd;
+            o[6] = o[6] - fd;
+            o[7] = o[7] - fd;
+            o[8] = o[8] + fd;
         }
     }
-    if (q.Fscale != 0.0f) {
-        const F2 fa = sp2((1.0f / 9.0f) * q.Fscale), fd = sp2((1.0f / 36.0f) * q.Fscale);
-        o[1] = o[1] + fa;
-        o[3] = o[3] - fa;
-        o[5] = o[5] + fd;
-        o[6] = o[6] - fd;
-        o[7] = o[7] - fd;
-        o[8] = o[8] + fd;
-    }
 #pragma unroll
-    for (int j = 0; j < 9; ++j) f[j] = mk2(fa_ok ? o[j].v.x : f[j].v.x, fb_ok ? o[j].v.y : f[j].v.y);
+    for (int j = 0; j < 9; ++j) d[j] = mk2(fa_ok ? o[j].v.x : d[j].v.x, fb_ok ? o[j].v.y : d[j].v.y);
 }
 
 template <class T>
 struct PairStore;
+// Deviations of two x-neighbours (index i even) as one 8-byte / 4-byte store.
 template <>
 struct PairStore<float> {
-    static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, float, uint32_t) {
+    static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, uint32_t) {
         *reinterpret_cast<float2*>(p + i) = make_float2(a, b);
     }
 };
 template <>
 struct PairStore<__half> {
-    static __device__ __forceinline__ void st(__half* p, size_t i, float a, float b, float sh, uint32_t rb) {
-        const float o = -sh * kF16Scale;
-        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_f16x2(fmaf(a, kF16Scale, o), fmaf(b, kF16Scale, o), rb);
+    static __device__ __forceinline__ void st(__half* p, size_t i, float a, float b, uint32_t rb) {
+        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_f16x2(a * kF16Scale, b * kF16Scale, rb);
     }
 };
 template <>
 struct PairStore<__nv_bfloat16> {
-    static __device__ __forceinline__ void st(__nv_bfloat16* p, size_t i, float a, float b, float sh, uint32_t rb) {
-        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_bf16x2(a - sh, b - sh, rb);
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, size_t i, float a, float b, uint32_t rb) {
+        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_bf16x2(a, b, rb);
     }
 };
 

@@ -42,9 +42,9 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
     if (x0 < p.nx && y < p.ny) {
         const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
         const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
-        float fa[9], fb[9], ga[9], gb[9];
-        build_state<T, false>(p, x0, y, fl.x, fa, ga);
-        build_state<T, false>(p, x0 + 1, y, fl.y, fb, gb);
+        float fa[9], fb[9], ga[9], gb[9];  // deviations
+        build_dev<T, false>(p, x0, y, fl.x, fa, ga);
+        build_dev<T, false>(p, x0 + 1, y, fl.y, fb, gb);
         const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
         if ((fl.x | fl.y) & FLAG_BOUNDARY) {
             // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
@@ -53,12 +53,12 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
 #pragma unroll
             for (int j = 1; j < 9; ++j) {
                 if (ma & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * fa[j];
-                    fys -= float(CYf(j)) * 2.0f * fa[j];
+                    fxs -= float(CXf(j)) * 2.0f * (fa[j] + p.shf[j]);
+                    fys -= float(CYf(j)) * 2.0f * (fa[j] + p.shf[j]);
                 }
                 if (mb & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * fb[j];
-                    fys -= float(CYf(j)) * 2.0f * fb[j];
+                    fxs -= float(CXf(j)) * 2.0f * (fb[j] + p.shf[j]);
+                    fys -= float(CYf(j)) * 2.0f * (fb[j] + p.shf[j]);
                 }
             }
         }
@@ -66,7 +66,7 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
             F2 f[9];
 #pragma unroll
             for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
-            collide_pair(p, fl.x, fl.y, oka, okb, f);
+            collide_pair_dev(p, fl.x, fl.y, oka, okb, f);
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
                 fa[j] = f[j].v.x;
@@ -82,7 +82,7 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
             uint32_t rb[9] = {};
             if constexpr (Pop<T>::kRounds) rand9(skey + n0, rb);
 #pragma unroll
-            for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], p.shf[j], rb[j]);
+            for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
         }
     }
     if (p.block_slot) {
@@ -183,23 +183,39 @@ __global__ void __launch_bounds__(512) batch_step_pair_kernel(const KParams* __r
     step_pair_block<T>(sp, local % sp.gx, local / sp.gx, sp.gx);
 }
 
+// Post-stream state of node (x, y) in FP64: stored deviations are widened
+// before the shift is added back, so the FP64 value is exact.
+template <class T, bool TH>
+__device__ __forceinline__ void state_fp64(const KParams& p, int x, int y, uint32_t fl, double f[9], double g[9]) {
+    if constexpr (std::is_same<T, double>::value) {
+        build_state<T, TH>(p, x, y, fl, f, g);
+    } else {
+        float d[9], e[9];
+        build_dev<T, TH>(p, x, y, fl, d, e);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) f[j] = double(d[j]) + double(p.shf[j]);
+        if (TH) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) g[j] = double(e[j]) + double(p.shg[j]);
+        }
+    }
+}
+
 template <class T, bool TH>
 __global__ void readback_kernel(const KParams p, const ROut o) {
-    using R = typename Pop<T>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= p.nx || y >= p.ny) return;
     const size_t n = (size_t)y * p.nx + x;
     const uint32_t fl = p.flags[n];
-    R f[9], g[9];
-    build_state<T, TH>(p, x, y, fl, f, g);
+    double f[9], g[9];  // the reference's post-stream state in FP64
+    state_fp64<T, TH>(p, x, y, fl, f, g);
     if (o.f_aos)
-        for (int j = 0; j < 9; ++j) o.f_aos[n * 9 + j] = double(f[j]);
+        for (int j = 0; j < 9; ++j) o.f_aos[n * 9 + j] = f[j];
     if (TH && o.g_aos)
-        for (int j = 0; j < 9; ++j) o.g_aos[n * 9 + j] = double(g[j]);
+        for (int j = 0; j < 9; ++j) o.g_aos[n * 9 + j] = g[j];
     if (o.rho || o.u || o.v) {
-        double fd[9];
-        for (int j = 0; j < 9; ++j) fd[j] = double(f[j]);
+        const double* fd = f;
         double rho, u, v;
         macros(fd, rho, u, v);
         if (o.rho) o.rho[n] = rho;
@@ -236,21 +252,32 @@ __global__ void prologue_kernel(const KParams p, const double* __restrict__ fa, 
     if (x >= p.nx || y >= p.ny) return;
     const size_t n = (size_t)y * p.nx + x;
     const uint32_t fl = p.flags[n];
-    R f[9], g[9];
-    for (int j = 0; j < 9; ++j) f[j] = R(fa[n * 9 + j]);
-    if (TH)
-        for (int j = 0; j < 9; ++j) g[j] = R(ga[n * 9 + j]);
-    if (!(fl & FLAG_SOLID)) collide<R, TH>(p, fl, f, g);
     T* Fo = static_cast<T*>(p.fout);
+    T* Go = static_cast<T*>(p.gout);
     const size_t N = (size_t)p.N;
-    uint32_t rb[9] = {};
-    const uint32_t skey = seed_key(p.seed_host);
-    if constexpr (Pop<T>::kRounds) rand9(skey + (uint32_t)n, rb);
-    for (int j = 0; j < 9; ++j) Pop<T>::st(Fo + j * N, n, f[j], p.shf[j], rb[j]);
-    if (TH) {
-        T* Go = static_cast<T*>(p.gout);
-        if constexpr (Pop<T>::kRounds) rand9((skey + (uint32_t)n) ^ 0x6A09E667u, rb);
-        for (int j = 0; j < 9; ++j) Pop<T>::st(Go + j * N, n, g[j], p.shg[j], rb[j]);
+    R f[9], g[9];
+    if constexpr (std::is_same<T, double>::value) {
+        for (int j = 0; j < 9; ++j) f[j] = fa[n * 9 + j];
+        if (TH)
+            for (int j = 0; j < 9; ++j) g[j] = ga[n * 9 + j];
+        if (!(fl & FLAG_SOLID)) collide<R, TH>(p, fl, f, g);
+        for (int j = 0; j < 9; ++j) Fo[j * N + n] = f[j];
+        if (TH)
+            for (int j = 0; j < 9; ++j) Go[j * N + n] = g[j];
+    } else {
+        // deviations taken in FP64, then collided in the FP32 deviation form
+        for (int j = 0; j < 9; ++j) f[j] = float(fa[n * 9 + j] - double(p.shf[j]));
+        if (TH)
+            for (int j = 0; j < 9; ++j) g[j] = float(ga[n * 9 + j] - double(p.shg[j]));
+        if (!(fl & FLAG_SOLID)) collide_dev<TH>(p, fl, f, g);
+        uint32_t rb[9] = {};
+        const uint32_t skey = seed_key(p.seed_host);
+        if constexpr (Pop<T>::kRounds) rand9(skey + (uint32_t)n, rb);
+        for (int j = 0; j < 9; ++j) Pop<T>::std_(Fo + j * N, n, f[j], rb[j]);
+        if (TH) {
+            if constexpr (Pop<T>::kRounds) rand9((skey + (uint32_t)n) ^ 0x6A09E667u, rb);
+            for (int j = 0; j < 9; ++j) Pop<T>::std_(Go + j * N, n, g[j], rb[j]);
+        }
     }
     pass_seed(p, p.seed_host, x == 0 && y == 0);
 }
@@ -277,7 +304,6 @@ __global__ void fill_equilibrium_kernel(double* __restrict__ fa, double* __restr
 template <class T, bool TH>
 __global__ void diagnostics_kernel(const KParams p, double* __restrict__ acc, float* __restrict__ prev_uv,
                                    int have_prev) {
-    using R = typename Pop<T>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     double m = 0.0, jx = 0.0, jy = 0.0, du2 = 0.0, u2 = 0.0;
@@ -285,8 +311,8 @@ __global__ void diagnostics_kernel(const KParams p, double* __restrict__ acc, fl
         const size_t n = (size_t)y * p.nx + x;
         const uint32_t fl = p.flags[n];
         if (!(fl & FLAG_SOLID)) {
-            R f[9], g[9];
-            build_state<T, TH>(p, x, y, fl, f, g);
+            double f[9], g[9];
+            state_fp64<T, TH>(p, x, y, fl, f, g);
             double rho = 0.0, mx = 0.0, my = 0.0;
             for (int j = 0; j < 9; ++j) {
                 rho += double(f[j]);
@@ -335,13 +361,14 @@ __global__ void prologue_pair_kernel(const KParams p, const double* __restrict__
     const uint32_t fla = p.flags[n0], flb = p.flags[n0 + 1];
     const bool oka = !(fla & FLAG_SOLID), okb = !(flb & FLAG_SOLID);
     F2 f[9];
-    for (int j = 0; j < 9; ++j) f[j] = mk2(float(fa[n0 * 9 + j]), float(fa[(n0 + 1) * 9 + j]));
-    if (oka || okb) collide_pair(p, fla, flb, oka, okb, f);
+    for (int j = 0; j < 9; ++j)
+        f[j] = mk2(float(fa[n0 * 9 + j] - double(p.shf[j])), float(fa[(n0 + 1) * 9 + j] - double(p.shf[j])));
+    if (oka || okb) collide_pair_dev(p, fla, flb, oka, okb, f);
     T* Fo = static_cast<T*>(p.fout);
     const size_t N = (size_t)p.N;
     uint32_t rb[9] = {};
     if constexpr (Pop<T>::kRounds) rand9(seed_key(p.seed_host) + (uint32_t)n0, rb);
-    for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, f[j].v.x, f[j].v.y, p.shf[j], rb[j]);
+    for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, f[j].v.x, f[j].v.y, rb[j]);
     pass_seed(p, p.seed_host, x0 == 0 && y == 0);
 }
 

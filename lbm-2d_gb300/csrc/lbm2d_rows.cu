@@ -137,111 +137,131 @@ __device__ __forceinline__ void issue_tile(const KParams& p, int x0, int y, uint
 }
 
 // ----------------------------------------------------------------- consumer
+// Deviations of elements e, e+1 of a staged row.
 template <class T>
 struct SmemPair;
 template <>
 struct SmemPair<float> {
-    // elements e, e+1 of a staged row (FP32 is stored unshifted)
-    static __device__ __forceinline__ void aligned(const float* r, int e, float, float& a, float& b) {
+    static __device__ __forceinline__ void aligned(const float* r, int e, float& a, float& b) {
         const float2 v = *reinterpret_cast<const float2*>(r + e);
         a = v.x;
         b = v.y;
     }
-    static __device__ __forceinline__ void any(const float* r, int e, float, float& a, float& b) {
+    static __device__ __forceinline__ void any(const float* r, int e, float& a, float& b) {
         a = r[e];
         b = r[e + 1];
     }
 };
 template <>
 struct SmemPair<__half> {
-    static __device__ __forceinline__ void aligned(const __half* r, int e, float sh, float& a, float& b) {
+    static __device__ __forceinline__ void aligned(const __half* r, int e, float& a, float& b) {
         const float2 v = __half22float2(*reinterpret_cast<const __half2*>(r + e));
-        a = fmaf(v.x, kF16InvScale, sh);
-        b = fmaf(v.y, kF16InvScale, sh);
+        a = v.x * kF16InvScale;
+        b = v.y * kF16InvScale;
     }
-    static __device__ __forceinline__ void any(const __half* r, int e, float sh, float& a, float& b) {
-        a = fmaf(__half2float(r[e]), kF16InvScale, sh);
-        b = fmaf(__half2float(r[e + 1]), kF16InvScale, sh);
+    static __device__ __forceinline__ void any(const __half* r, int e, float& a, float& b) {
+        a = __half2float(r[e]) * kF16InvScale;
+        b = __half2float(r[e + 1]) * kF16InvScale;
     }
 };
 template <>
 struct SmemPair<__nv_bfloat16> {
-    static __device__ __forceinline__ void aligned(const __nv_bfloat16* r, int e, float sh, float& a, float& b) {
+    static __device__ __forceinline__ void aligned(const __nv_bfloat16* r, int e, float& a, float& b) {
         const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(r + e));
-        a = v.x + sh;
-        b = v.y + sh;
+        a = v.x;
+        b = v.y;
     }
-    static __device__ __forceinline__ void any(const __nv_bfloat16* r, int e, float sh, float& a, float& b) {
-        a = __bfloat162float(r[e]) + sh;
-        b = __bfloat162float(r[e + 1]) + sh;
+    static __device__ __forceinline__ void any(const __nv_bfloat16* r, int e, float& a, float& b) {
+        a = __bfloat162float(r[e]);
+        b = __bfloat162float(r[e + 1]);
     }
 };
 
 // Nodes (x, x+1) of the tile staged at `stage` (x0 its first node): the
 // reference's post-stream state (pull, bounce-back records, outflow column,
 // boundary conditions), the momentum-exchange force, the collision and the
-// stores -- the body of step_pair_block with shared-memory pulls.
+// stores -- the body of step_pair_block with shared-memory pulls, on
+// deviations.
 template <class T>
 __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
                                              uint32_t skey, float& fxs, float& fys) {
     using C = RowsCfg<T>;
     const uint2 fl = *reinterpret_cast<const uint2*>(stage + C::FLAGS_OFF + (x - x0) * 4);
     const int e0 = (x - x0) + C::PAD;
-    float fa[9], fb[9];
+    float da[9], db[9];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
         const T* r = reinterpret_cast<const T*>(stage + j * C::ROW_BYTES);
         if (CXf(j) == 0)
-            SmemPair<T>::aligned(r, e0, p.shf[j], fa[j], fb[j]);
+            SmemPair<T>::aligned(r, e0, da[j], db[j]);
         else
-            SmemPair<T>::any(r, e0 - CXf(j), p.shf[j], fa[j], fb[j]);
+            SmemPair<T>::any(r, e0 - CXf(j), da[j], db[j]);
     }
-    const T* __restrict__ Pf = static_cast<const T*>(p.fin);
-    if (fl.x & FLAG_SOLID) {
-#pragma unroll
-        for (int j = 0; j < 9; ++j) fa[j] = 0.0f;
-    } else if (fl.x & FLAG_BOUNDARY) {
-        fix_f<T>(p, Pf, x, y, fl.x >> 2, fa);
-    }
-    // zero-gradient outlet: column NX-1 takes NX-2's post-stream state
-    // (src/lbm.hpp:63-73); x + 1 == nx - 1 means x == nx - 2
-    if ((p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x + 1 == p.nx - 1) {
-#pragma unroll
-        for (int j = 0; j < 9; ++j) fb[j] = fa[j];
-    } else if (fl.y & FLAG_SOLID) {
-#pragma unroll
-        for (int j = 0; j < 9; ++j) fb[j] = 0.0f;
-    } else if (fl.y & FLAG_BOUNDARY) {
-        fix_f<T>(p, Pf, x + 1, y, fl.y >> 2, fb);
-    }
-    apply_bc<float>(p, x, y, fl.x, fa);
-    apply_bc<float>(p, x + 1, y, fl.y, fb);
     const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
-    if ((fl.x | fl.y) & FLAG_BOUNDARY) {
-        // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
-        const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
-        const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+    const bool sa = special_node<false>(p, x, y, fl.x), sb = special_node<false>(p, x + 1, y, fl.y);
+    if (sa || sb) {
+        // full populations for the special node(s)
+        const T* __restrict__ Pf = static_cast<const T*>(p.fin);
+        float fa[9], fb[9];
 #pragma unroll
-        for (int j = 1; j < 9; ++j) {
-            if (ma & (1u << j)) {
-                fxs -= float(CXf(j)) * 2.0f * fa[j];
-                fys -= float(CYf(j)) * 2.0f * fa[j];
+        for (int j = 0; j < 9; ++j) {
+            fa[j] = da[j] + p.shf[j];
+            fb[j] = db[j] + p.shf[j];
+        }
+        if (fl.x & FLAG_SOLID) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) fa[j] = 0.0f;
+        } else if (fl.x & FLAG_BOUNDARY) {
+            fix_f<T>(p, Pf, x, y, fl.x >> 2, fa);
+        }
+        // zero-gradient outlet: column NX-1 takes NX-2's post-stream state
+        // (src/lbm.hpp:63-73); x + 1 == nx - 1 means x == nx - 2
+        if ((p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x + 1 == p.nx - 1) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) fb[j] = fa[j];
+        } else if (fl.y & FLAG_SOLID) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) fb[j] = 0.0f;
+        } else if (fl.y & FLAG_BOUNDARY) {
+            fix_f<T>(p, Pf, x + 1, y, fl.y >> 2, fb);
+        }
+        apply_bc<float>(p, x, y, fl.x, fa);
+        apply_bc<float>(p, x + 1, y, fl.y, fb);
+        if ((fl.x | fl.y) & FLAG_BOUNDARY) {
+            // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
+            const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
+            const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+#pragma unroll
+            for (int j = 1; j < 9; ++j) {
+                if (ma & (1u << j)) {
+                    fxs -= float(CXf(j)) * 2.0f * fa[j];
+                    fys -= float(CYf(j)) * 2.0f * fa[j];
+                }
+                if (mb & (1u << j)) {
+                    fxs -= float(CXf(j)) * 2.0f * fb[j];
+                    fys -= float(CYf(j)) * 2.0f * fb[j];
+                }
             }
-            if (mb & (1u << j)) {
-                fxs -= float(CXf(j)) * 2.0f * fb[j];
-                fys -= float(CYf(j)) * 2.0f * fb[j];
-            }
+        }
+        // back to deviations; a regular neighbour keeps its exact deviations
+        if (sa) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) da[j] = fa[j] - p.shf[j];
+        }
+        if (sb) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) db[j] = fb[j] - p.shf[j];
         }
     }
     if (oka || okb) {
         F2 f[9];
 #pragma unroll
-        for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
-        collide_pair(p, fl.x, fl.y, oka, okb, f);
+        for (int j = 0; j < 9; ++j) f[j] = mk2(da[j], db[j]);
+        collide_pair_dev(p, fl.x, fl.y, oka, okb, f);
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-            fa[j] = f[j].v.x;
-            fb[j] = f[j].v.y;
+            da[j] = f[j].v.x;
+            db[j] = f[j].v.y;
         }
     }
     const bool settled = p.skip_settled_solids && y < p.ny - 1;
@@ -254,7 +274,7 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
         uint32_t rb[9] = {};
         if constexpr (Pop<T>::kRounds) rand9(skey + (uint32_t)n0, rb);
 #pragma unroll
-        for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], p.shf[j], rb[j]);
+        for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, da[j], db[j], rb[j]);
     }
 }
 
