@@ -72,7 +72,9 @@ def peaks():
 
 
 def traffic_record():
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes per step-kernel launch from one ncu capture of this workload
+    (profiles/step_rows_kernel_4096x4096_dram.json, with the command that made it)."""
+    p = os.path.join(ROOT, "profiles", "step_rows_kernel_4096x4096_dram.json")
     if os.path.exists(p):
         try:
             return json.load(open(p))
@@ -627,8 +629,9 @@ def main():
     achieved = alg_bytes / (r0["kernel_ms"] * 1e-3) / 1e9
     tr = traffic_record()
     traffic = None
-    if tr and tr.get("storage") == main_st and tr.get("nodes"):
-        traffic = float(tr["dram_bytes_per_launch"]) * nodes / float(tr["nodes"])
+    if tr and main_st in tr and tr.get("nodes") and KERNEL_NAMES[r0["kernel"]][0] == tr.get("kernel"):
+        # bytes per launch scale with the nodes of the launch
+        traffic = float(tr[main_st]["dram_bytes_per_launch"]) * nodes / float(tr["nodes"])
     prec = {}
     for label, st, les in runs[1:]:
         r = results[label]

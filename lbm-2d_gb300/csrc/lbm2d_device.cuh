@@ -56,6 +56,8 @@ template <>
 struct Pop<float> {
     using R = float;
     static constexpr bool kRounds = false;
+    static constexpr float kS = 1.0f, kInvS = 1.0f;  // stored value = deviation * kS
+    static __device__ __forceinline__ float ldr(const float* __restrict__ p, size_t i) { return __ldg(p + i); }
     static __device__ __forceinline__ float ldd(const float* __restrict__ p, size_t i) { return __ldg(p + i); }
     static __device__ __forceinline__ void std_(float* __restrict__ p, size_t i, float d, uint32_t) { p[i] = d; }
     static __device__ __forceinline__ R ld(const float* __restrict__ p, size_t i, float sh) { return __ldg(p + i) + sh; }
@@ -74,6 +76,10 @@ template <>
 struct Pop<__half> {
     using R = float;
     static constexpr bool kRounds = true;
+    static constexpr float kS = kF16Scale, kInvS = kF16InvScale;
+    static __device__ __forceinline__ float ldr(const __half* __restrict__ p, size_t i) {
+        return __half2float(__ldg(p + i));
+    }
     static __device__ __forceinline__ float ldd(const __half* __restrict__ p, size_t i) {
         return __half2float(__ldg(p + i)) * kF16InvScale;
     }
@@ -92,6 +98,10 @@ template <>
 struct Pop<__nv_bfloat16> {
     using R = float;
     static constexpr bool kRounds = true;
+    static constexpr float kS = 1.0f, kInvS = 1.0f;
+    static __device__ __forceinline__ float ldr(const __nv_bfloat16* __restrict__ p, size_t i) {
+        return __bfloat162float(__ldg(p + i));
+    }
     static __device__ __forceinline__ float ldd(const __nv_bfloat16* __restrict__ p, size_t i) {
         return __bfloat162float(__ldg(p + i));
     }
@@ -549,6 +559,42 @@ __device__ __forceinline__ bool build_dev(const KParams& p, int x, int y, uint32
     return true;
 }
 
+// The paired kernels work in STORAGE units, deviation * kS (FP16: 2^12), so
+// loads and stores need no scaling; the scale enters once per node through
+// rho and u.
+template <class T>
+__device__ __forceinline__ void pull_raw(const KParams& p, const T* __restrict__ P, int x, int y, float d[9]) {
+    const unsigned nx = (unsigned)p.nx, ny = (unsigned)p.ny;
+    const size_t N = (size_t)p.N;
+    const unsigned ux = (unsigned)x, uy = (unsigned)y;
+    const unsigned xm = ux == 0 ? nx - 1 : ux - 1, xp = ux == nx - 1 ? 0 : ux + 1;
+    const unsigned ym = uy == 0 ? ny - 1 : uy - 1, yp = uy == ny - 1 ? 0 : uy + 1;
+    const unsigned r0 = uy * nx, rm = ym * nx, rp = yp * nx;
+    d[0] = Pop<T>::ldr(P, r0 + ux);
+    d[1] = Pop<T>::ldr(P + N, r0 + xm);
+    d[2] = Pop<T>::ldr(P + 2 * N, rm + ux);
+    d[3] = Pop<T>::ldr(P + 3 * N, r0 + xp);
+    d[4] = Pop<T>::ldr(P + 4 * N, rp + ux);
+    d[5] = Pop<T>::ldr(P + 5 * N, rm + xm);
+    d[6] = Pop<T>::ldr(P + 6 * N, rm + xp);
+    d[7] = Pop<T>::ldr(P + 7 * N, rp + xp);
+    d[8] = Pop<T>::ldr(P + 8 * N, rp + xm);
+}
+
+// build_dev<T, false> in storage units.
+template <class T>
+__device__ __forceinline__ bool build_dev_s(const KParams& p, int x, int y, uint32_t fl, float d[9]) {
+    if (!special_node<false>(p, x, y, fl)) {
+        pull_raw<T>(p, static_cast<const T*>(p.fin), x, y, d);
+        return false;
+    }
+    float f[9], g[9];
+    build_state<T, false>(p, x, y, fl, f, g);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) d[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
+    return true;
+}
+
 // Collision of one fluid node on deviations (same operator as collide<R, TH>).
 template <bool TH>
 __device__ __forceinline__ void collide_dev(const KParams& p, uint32_t fl, float d[9], float e[9]) {
@@ -788,26 +834,36 @@ __device__ __forceinline__ F2 operator-(F2 a, F2 b) { return {__ffma2_rn(b.v, ma
 __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
 __device__ __forceinline__ F2 rcp2(F2 a) { return mk2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y)); }
 __device__ __forceinline__ F2 sqrt2(F2 a) { return mk2(Fm<float>::sqrt(a.v.x), Fm<float>::sqrt(a.v.y)); }
+// square root of a strictly positive argument (no zero guard)
+__device__ __forceinline__ F2 sqrt2_pos(F2 a) { return a * mk2(rsqrtf(a.v.x), rsqrtf(a.v.y)); }
 
-// collide_dev<false> on two nodes at once (FP32x2); lane k is collided only
-// when ok_k (a solid lane keeps its value).
+// collide_dev<false> on two nodes at once (FP32x2), in storage units
+// (deviation * kS); lane k is collided only when ok_k (a solid lane keeps the
+// solid state, f = 0).
+// KC / KL fix the collision (0 MRT, 1 BGK) and LES (0/1) at compile time;
+// -1 reads them from the parameters.
+template <class T, int KC = -1, int KL = -1>
 __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla, uint32_t flb, bool fa_ok,
                                                  bool fb_ok, F2 d[9]) {
+    constexpr float S = Pop<T>::kS, iS = Pop<T>::kInvS;
+    const bool mrt = KC >= 0 ? KC == 0 : p.collision == 0;
+    const bool les = KL >= 0 ? KL == 1 : p.les != 0;
     const Phys<float>& q = p.pf;
     const F2 drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
     const F2 mx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
     const F2 my = (d[2] - d[4]) + (d[5] + d[6]) - (d[7] + d[8]);
-    const F2 rho = sp2(1.0f) + drho;
+    const F2 rho = fma2(drho, sp2(iS), sp2(1.0f));
     const F2 inv = rcp2(rho);
-    const F2 u = mx * inv, v = my * inv;
+    const F2 k = S == 1.0f ? inv : inv * sp2(iS);  // 1 / (rho * S)
+    const F2 u = mx * k, v = my * k;
     if ((fa_ok && (!(rho.v.x == rho.v.x) || rho.v.x == 0.0f)) || (fb_ok && (!(rho.v.y == rho.v.y) || rho.v.y == 0.0f)))
         atomicOr(p.nan_flag, 1u);
-    const float F = q.Fscale;
+    const float F = q.Fscale * S;
     F2 o[9];
-    if (p.collision == 0) {
+    if (mrt) {
         const F2 sd = (d[5] + d[6]) + (d[7] + d[8]), sa = (d[1] + d[2]) + (d[3] + d[4]);
-        F2 me = fma2(sp2(2.0f), sd, fma2(sp2(-4.0f), d[0], sp2(0.0f) - sa));  // e + 2
-        F2 meps = fma2(sp2(4.0f), d[0], fma2(sp2(-2.0f), sa, sd));            // eps - 1
+        F2 me = fma2(sp2(2.0f), sd, fma2(sp2(-4.0f), d[0], sp2(0.0f) - sa));  // (e + 2) S
+        F2 meps = fma2(sp2(4.0f), d[0], fma2(sp2(-2.0f), sa, sd));            // (eps - 1) S
         F2 mpxx = (d[1] - d[2]) + (d[3] - d[4]);
         F2 mpxy = (d[5] - d[6]) + (d[7] - d[8]);
         const F2 r3u = sp2(3.0f) * fma2(mx, u, my * v);
@@ -816,19 +872,20 @@ __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla,
         const F2 pxx_eq = fma2(mx, u, sp2(0.0f) - my * v);
         const F2 pxy_eq = mx * v;
         F2 s_eff = sp2(q.s_shear);
-        if (p.les) {
+        if (les) {
             F2 csq = sp2(q.cs_sq);
             if (q.nu > 0.0f) {
+                // y+ > 0 at every collided node (its wall distance is >= 1),
+                // so the Van Driest branch always applies
                 const F2 wd = mk2(wall_distance<float>(p, fla), wall_distance<float>(p, flb));
-                const F2 yp = wd * sqrt2(fma2(u, u, v * v) + sp2(1e-12f)) * sp2(q.inv_nu);
-                const float dxa = yp.v.x > 0.0f ? q.cs * (1.0f - __expf(-yp.v.x * (1.0f / 26.0f))) : 0.0f;
-                const float dxb = yp.v.y > 0.0f ? q.cs * (1.0f - __expf(-yp.v.y * (1.0f / 26.0f))) : 0.0f;
-                csq = mk2(yp.v.x > 0.0f ? dxa * dxa : q.cs_sq, yp.v.y > 0.0f ? dxb * dxb : q.cs_sq);
+                const F2 yp = wd * sqrt2_pos(fma2(u, u, v * v) + sp2(1e-12f)) * sp2(q.inv_nu);
+                const F2 cd = sp2(q.cs) - sp2(q.cs) * mk2(__expf(yp.v.x * (-1.0f / 26.0f)), __expf(yp.v.y * (-1.0f / 26.0f)));
+                csq = cd * cd;
             }
             const F2 a = mpxx - pxx_eq, b = mpxy - pxy_eq;
-            const F2 Q = sqrt2(sp2(2.0f) * fma2(a, a, b * b));
-            const F2 A = sp2(4.5f) * csq * Q * inv;
-            const F2 te2 = sp2(q.tau) + sqrt2(fma2(sp2(q.tau), sp2(q.tau), sp2(4.0f) * A));
+            const F2 Q = sqrt2(sp2(2.0f) * fma2(a, a, b * b));  // Q * S
+            const F2 A = sp2(4.5f) * csq * Q * k;
+            const F2 te2 = sp2(q.tau) + sqrt2_pos(fma2(sp2(q.tau), sp2(q.tau), sp2(4.0f) * A));
             const F2 s2 = sp2(2.0f) * rcp2(te2);
             s_eff = mk2(clamp_rate<float>(s2.v.x), clamp_rate<float>(s2.v.y));
         }
@@ -854,12 +911,13 @@ __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla,
         o[8] = ad + dx - dy - py;
     } else {
         const F2 it = sp2(q.inv_tau), usq = fma2(u, u, v * v);
+        const F2 rhoS = drho + sp2(S);
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
             const F2 cj = sp2(float(CXf(i))) * mx + sp2(float(CYf(i))) * my;
             const F2 ed = sp2(float(CXf(i))) * u + sp2(float(CYf(i))) * v;
             const F2 fe = sp2(float(wgt(i))) * (fma2(sp2(3.0f), cj, drho) +
-                                                 rho * fma2(sp2(4.5f) * ed, ed, sp2(-1.5f) * usq));
+                                                 rhoS * fma2(sp2(4.5f) * ed, ed, sp2(-1.5f) * usq));
             o[i] = d[i] - it * (d[i] - fe);
         }
         if (F != 0.0f) {
@@ -872,13 +930,27 @@ __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla,
             o[8] = o[8] + fd;
         }
     }
+    if constexpr (std::is_same<T, float>::value) {
+        // keep a solid lane's input (measured faster for FP32 than the branch)
 #pragma unroll
-    for (int j = 0; j < 9; ++j) d[j] = mk2(fa_ok ? o[j].v.x : d[j].v.x, fb_ok ? o[j].v.y : d[j].v.y);
+        for (int j = 0; j < 9; ++j) d[j] = mk2(fa_ok ? o[j].v.x : d[j].v.x, fb_ok ? o[j].v.y : d[j].v.y);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) d[j] = o[j];
+        if (!fa_ok) {  // solid lane: f = 0
+#pragma unroll
+            for (int j = 0; j < 9; ++j) d[j].v.x = -p.shf[j] * S;
+        }
+        if (!fb_ok) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) d[j].v.y = -p.shf[j] * S;
+        }
+    }
 }
 
 template <class T>
 struct PairStore;
-// Deviations of two x-neighbours (index i even) as one 8-byte / 4-byte store.
+// Two x-neighbours (index i even) in storage units as one 8-byte / 4-byte store.
 template <>
 struct PairStore<float> {
     static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, uint32_t) {
@@ -888,7 +960,7 @@ struct PairStore<float> {
 template <>
 struct PairStore<__half> {
     static __device__ __forceinline__ void st(__half* p, size_t i, float a, float b, uint32_t rb) {
-        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_f16x2(a * kF16Scale, b * kF16Scale, rb);
+        *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_f16x2(a, b, rb);
     }
 };
 template <>

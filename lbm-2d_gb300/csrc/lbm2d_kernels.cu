@@ -42,9 +42,10 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
     if (x0 < p.nx && y < p.ny) {
         const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
         const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
-        float fa[9], fb[9], ga[9], gb[9];  // deviations
-        build_dev<T, false>(p, x0, y, fl.x, fa, ga);
-        build_dev<T, false>(p, x0 + 1, y, fl.y, fb, gb);
+        constexpr float iS = Pop<T>::kInvS;
+        float fa[9], fb[9];  // deviations in storage units
+        build_dev_s<T>(p, x0, y, fl.x, fa);
+        build_dev_s<T>(p, x0 + 1, y, fl.y, fb);
         const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
         if ((fl.x | fl.y) & FLAG_BOUNDARY) {
             // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
@@ -53,12 +54,14 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
 #pragma unroll
             for (int j = 1; j < 9; ++j) {
                 if (ma & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * (fa[j] + p.shf[j]);
-                    fys -= float(CYf(j)) * 2.0f * (fa[j] + p.shf[j]);
+                    const float f = fmaf(fa[j], iS, p.shf[j]);
+                    fxs -= float(CXf(j)) * 2.0f * f;
+                    fys -= float(CYf(j)) * 2.0f * f;
                 }
                 if (mb & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * (fb[j] + p.shf[j]);
-                    fys -= float(CYf(j)) * 2.0f * (fb[j] + p.shf[j]);
+                    const float f = fmaf(fb[j], iS, p.shf[j]);
+                    fxs -= float(CXf(j)) * 2.0f * f;
+                    fys -= float(CYf(j)) * 2.0f * f;
                 }
             }
         }
@@ -66,7 +69,7 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
             F2 f[9];
 #pragma unroll
             for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
-            collide_pair_dev(p, fl.x, fl.y, oka, okb, f);
+            collide_pair_dev<T>(p, fl.x, fl.y, oka, okb, f);
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
                 fa[j] = f[j].v.x;
@@ -361,9 +364,10 @@ __global__ void prologue_pair_kernel(const KParams p, const double* __restrict__
     const uint32_t fla = p.flags[n0], flb = p.flags[n0 + 1];
     const bool oka = !(fla & FLAG_SOLID), okb = !(flb & FLAG_SOLID);
     F2 f[9];
+    const double S = Pop<T>::kS;
     for (int j = 0; j < 9; ++j)
-        f[j] = mk2(float(fa[n0 * 9 + j] - double(p.shf[j])), float(fa[(n0 + 1) * 9 + j] - double(p.shf[j])));
-    if (oka || okb) collide_pair_dev(p, fla, flb, oka, okb, f);
+        f[j] = mk2(float((fa[n0 * 9 + j] - double(p.shf[j])) * S), float((fa[(n0 + 1) * 9 + j] - double(p.shf[j])) * S));
+    if (oka || okb) collide_pair_dev<T>(p, fla, flb, oka, okb, f);
     T* Fo = static_cast<T*>(p.fout);
     const size_t N = (size_t)p.N;
     uint32_t rb[9] = {};

@@ -44,9 +44,13 @@ struct RowsCfg {
     static constexpr int ROW_BYTES = SW * ES;
     static constexpr int FLAGS_OFF = 9 * ROW_BYTES;
     static constexpr int STAGE_BYTES = ((FLAGS_OFF + kTileW * 4) + 127) / 128 * 128;
-    static constexpr int STAGES = ES == 4 ? 4 : 6;
+    // FP32 moves twice the bytes per node: 2 CTAs per SM with deeper
+    // registers; the 16-bit forms are latency-bound on the arithmetic: 3 CTAs
+    static constexpr int STAGES = 4;
+    static constexpr int MIN_BLOCKS = ES == 4 ? 2 : 3;
     static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
-    static constexpr int SMEM = BAR_OFF + 2 * STAGES * 8;
+    static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;  // FP64 force sums, 2 per consumer warp
+    static constexpr int SMEM = ACC_OFF + 2 * kConsumerWarps * 8;
     static_assert(ROW_BYTES % 16 == 0 && FLAGS_OFF % 16 == 0, "bulk-copy alignment");
 };
 
@@ -137,7 +141,7 @@ __device__ __forceinline__ void issue_tile(const KParams& p, int x0, int y, uint
 }
 
 // ----------------------------------------------------------------- consumer
-// Deviations of elements e, e+1 of a staged row.
+// Elements e, e+1 of a staged row, in storage units (deviation * kS).
 template <class T>
 struct SmemPair;
 template <>
@@ -156,12 +160,12 @@ template <>
 struct SmemPair<__half> {
     static __device__ __forceinline__ void aligned(const __half* r, int e, float& a, float& b) {
         const float2 v = __half22float2(*reinterpret_cast<const __half2*>(r + e));
-        a = v.x * kF16InvScale;
-        b = v.y * kF16InvScale;
+        a = v.x;
+        b = v.y;
     }
     static __device__ __forceinline__ void any(const __half* r, int e, float& a, float& b) {
-        a = __half2float(r[e]) * kF16InvScale;
-        b = __half2float(r[e + 1]) * kF16InvScale;
+        a = __half2float(r[e]);
+        b = __half2float(r[e + 1]);
     }
 };
 template <>
@@ -182,7 +186,7 @@ struct SmemPair<__nv_bfloat16> {
 // boundary conditions), the momentum-exchange force, the collision and the
 // stores -- the body of step_pair_block with shared-memory pulls, on
 // deviations.
-template <class T>
+template <class T, int KC, int KL>
 __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
                                              uint32_t skey, float& fxs, float& fys) {
     using C = RowsCfg<T>;
@@ -202,11 +206,12 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
     if (sa || sb) {
         // full populations for the special node(s)
         const T* __restrict__ Pf = static_cast<const T*>(p.fin);
+        constexpr float S = Pop<T>::kS, iS = Pop<T>::kInvS;
         float fa[9], fb[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-            fa[j] = da[j] + p.shf[j];
-            fb[j] = db[j] + p.shf[j];
+            fa[j] = fmaf(da[j], iS, p.shf[j]);
+            fb[j] = fmaf(db[j], iS, p.shf[j]);
         }
         if (fl.x & FLAG_SOLID) {
 #pragma unroll
@@ -246,18 +251,18 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
         // back to deviations; a regular neighbour keeps its exact deviations
         if (sa) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) da[j] = fa[j] - p.shf[j];
+            for (int j = 0; j < 9; ++j) da[j] = (fa[j] - p.shf[j]) * S;
         }
         if (sb) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) db[j] = fb[j] - p.shf[j];
+            for (int j = 0; j < 9; ++j) db[j] = (fb[j] - p.shf[j]) * S;
         }
     }
     if (oka || okb) {
         F2 f[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) f[j] = mk2(da[j], db[j]);
-        collide_pair_dev(p, fl.x, fl.y, oka, okb, f);
+        collide_pair_dev<T, KC, KL>(p, fl.x, fl.y, oka, okb, f);
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
             da[j] = f[j].v.x;
@@ -278,15 +283,20 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(kThreads, 2) step_rows_kernel(const KParams p) {
+// KC: 0 MRT, 1 BGK; KL: LES on/off (MRT only); -1: read from the parameters.
+template <class T, int KC, int KL>
+__global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_kernel(const KParams p) {
     using C = RowsCfg<T>;
     extern __shared__ __align__(128) unsigned char smem[];
     const uint32_t sbase = smem_u32(smem);
     const uint32_t full0 = sbase + C::BAR_OFF, empty0 = full0 + 8 * C::STAGES;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tpr = (p.nx + kTileW - 1) / kTileW;
-    const int total = tpr * p.ny;
+    // tile t = y * tpr + seg, walked t = blockIdx.x, blockIdx.x + G, ... with
+    // (y, seg) advanced incrementally
+    const int G = (int)gridDim.x, dy = G / tpr, dseg = G - dy * tpr;
+    const int y_first = (int)blockIdx.x / tpr, seg_first = (int)blockIdx.x - y_first * tpr;
+    double* acc = reinterpret_cast<double*>(smem + C::ACC_OFF);
     if (threadIdx.x == 0) {
         for (int s = 0; s < C::STAGES; ++s) {
             mbar_init(full0 + 8 * s, 1);
@@ -294,22 +304,30 @@ __global__ void __launch_bounds__(kThreads, 2) step_rows_kernel(const KParams p)
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (threadIdx.x < 2 * kConsumerWarps) acc[threadIdx.x] = 0.0;
     __syncthreads();
 
     if (warp == kConsumerWarps) {  // producer
         if (lane != 0) return;
-        int k = 0;
+        int k = 0;  // tiles issued
         bool ok = true;
-        for (int t = blockIdx.x; t < total; t += gridDim.x, ++k) {
+        int y = y_first, seg = seg_first;
+        for (; y < p.ny; ++k) {
             const int s = k % C::STAGES, n = k / C::STAGES;
             if (n > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1))) {
                 ok = false;
                 break;
             }
-            const int y = t / tpr, x0 = (t - y * tpr) * kTileW;
+            const int x0 = seg * kTileW;
             const uint32_t bar = full0 + 8 * s;
             mbar_expect_tx(bar, tile_bytes<T>(p, x0));
             issue_tile<T>(p, x0, y, sbase + (uint32_t)(s * C::STAGE_BYTES), bar);
+            seg += dseg;
+            y += dy;
+            if (seg >= tpr) {
+                seg -= tpr;
+                ++y;
+            }
         }
         // every issued copy completes before the CTA may exit
         bool drained = true;
@@ -326,72 +344,92 @@ __global__ void __launch_bounds__(kThreads, 2) step_rows_kernel(const KParams p)
         skey = seed_key(s);
         pass_seed(p, s, blockIdx.x == 0 && threadIdx.x == 0);
     }
-    float fxs = 0.0f, fys = 0.0f;
-    double accx = 0.0, accy = 0.0;
     const bool force = p.block_slot != nullptr;
-    int k = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++k) {
-        const int s = k % C::STAGES, n = k / C::STAGES;
-        if (!mbar_wait(full0 + 8 * s, (uint32_t)(n & 1))) {
+    int y = y_first, seg = seg_first, s = 0;
+    uint32_t phase = 0;
+    while (y < p.ny) {
+        if (!mbar_wait(full0 + 8 * s, phase)) {
             atomicOr(p.nan_flag, 2u);
             break;
         }
-        const int y = t / tpr, x0 = (t - y * tpr) * kTileW;
+        const int x0 = seg * kTileW;
         const int x = x0 + 2 * (warp * 32 + lane);
-        const unsigned char* stage = smem + s * C::STAGE_BYTES;
-        if (x < p.nx) consume_pair<T>(p, stage, x0, x, y, skey, fxs, fys);
+        float fxs = 0.0f, fys = 0.0f;
+        if (x < p.nx) consume_pair<T, KC, KL>(p, smem + s * C::STAGE_BYTES, x0, x, y, skey, fxs, fys);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8 * s);
         if (force && __any_sync(0xffffffffu, fxs != 0.0f || fys != 0.0f)) {
             // per tile: FP32 warp sum of the tile's link terms, FP64 across tiles
-            float a = fxs, b = fys;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_down_sync(0xffffffffu, a, o);
-                b += __shfl_down_sync(0xffffffffu, b, o);
+                fxs += __shfl_down_sync(0xffffffffu, fxs, o);
+                fys += __shfl_down_sync(0xffffffffu, fys, o);
             }
-            accx += double(a);
-            accy += double(b);
-            fxs = fys = 0.0f;
+            if (lane == 0) {
+                acc[2 * warp] += double(fxs);
+                acc[2 * warp + 1] += double(fys);
+            }
+        }
+        if (++s == C::STAGES) {
+            s = 0;
+            phase ^= 1u;
+        }
+        seg += dseg;
+        y += dy;
+        if (seg >= tpr) {
+            seg -= tpr;
+            ++y;
         }
     }
-    if (force) {
+    if (force && lane == 0) {
         const int base = p.block_slot[blockIdx.x];
-        if (base >= 0 && lane == 0) {
-            p.partials[2 * (base + warp)] = accx;
-            p.partials[2 * (base + warp) + 1] = accy;
+        if (base >= 0) {
+            p.partials[2 * (base + warp)] = acc[2 * warp];
+            p.partials[2 * (base + warp) + 1] = acc[2 * warp + 1];
         }
     }
 }
 
-template <class T>
+template <class T, int KC, int KL>
 int rows_blocks_per_sm() {
     static int cached = -1;
     if (cached < 0) {
         int b = 0;
-        if (cudaFuncSetAttribute(step_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, RowsCfg<T>::SMEM) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, step_rows_kernel<T>, kThreads, RowsCfg<T>::SMEM) !=
-                cudaSuccess)
+        if (cudaFuncSetAttribute(step_rows_kernel<T, KC, KL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 RowsCfg<T>::SMEM) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, step_rows_kernel<T, KC, KL>, kThreads,
+                                                          RowsCfg<T>::SMEM) != cudaSuccess)
             return 0;
         cached = b;
     }
     return cached;
 }
 
+// FP32 runs one kernel with the collision mode read at run time; the 16-bit
+// forms, which are bound by their arithmetic, get one kernel per mode
+// (fewer branches and registers in the hot loop).  Both choices were the
+// faster ones measured on the 4096^2 channel.
+template <class T>
+constexpr bool kPerMode = !std::is_same<T, float>::value;
+
+// Smallest resident-CTA count over the kernel's variants, so one grid (and
+// one force-slot table) serves every collision mode.
 template <class T>
 int rows_grid_t(int nx, int ny, int device) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-    const int per = rows_blocks_per_sm<T>();
+    int per = 0;
+    if constexpr (kPerMode<T>)
+        per = std::min({rows_blocks_per_sm<T, 0, 0>(), rows_blocks_per_sm<T, 0, 1>(), rows_blocks_per_sm<T, 1, 0>()});
+    else
+        per = rows_blocks_per_sm<T, -1, -1>();
     if (per <= 0) return 0;
     const long long tiles = (long long)((nx + kTileW - 1) / kTileW) * ny;
     return (int)std::min<long long>(tiles, (long long)sms * per);
 }
 
-template <class T>
-int launch_rows_t(const KParams& p, int grid, cudaStream_t s) {
-    if (grid <= 0) return (int)cudaErrorInvalidConfiguration;
+template <class T, int KC, int KL>
+int launch_rows_v(const KParams& p, int grid, cudaStream_t s) {
     // the shared-memory opt-in is per device: set it once for each
     static std::atomic<unsigned long long> done{0};
     int dev = 0;
@@ -399,12 +437,24 @@ int launch_rows_t(const KParams& p, int grid, cudaStream_t s) {
     if (e != cudaSuccess) return (int)e;
     const unsigned long long bit = 1ull << (dev & 63);
     if (!(done.load() & bit)) {
-        e = cudaFuncSetAttribute(step_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, RowsCfg<T>::SMEM);
+        e = cudaFuncSetAttribute(step_rows_kernel<T, KC, KL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 RowsCfg<T>::SMEM);
         if (e != cudaSuccess) return (int)e;
         done.fetch_or(bit);
     }
-    step_rows_kernel<T><<<grid, kThreads, RowsCfg<T>::SMEM, s>>>(p);
+    step_rows_kernel<T, KC, KL><<<grid, kThreads, RowsCfg<T>::SMEM, s>>>(p);
     return (int)cudaGetLastError();
+}
+
+template <class T>
+int launch_rows_t(const KParams& p, int grid, cudaStream_t s) {
+    if (grid <= 0) return (int)cudaErrorInvalidConfiguration;
+    if constexpr (!kPerMode<T>) {
+        return launch_rows_v<T, -1, -1>(p, grid, s);
+    } else {
+        if (p.collision != 0) return launch_rows_v<T, 1, 0>(p, grid, s);
+        return p.les ? launch_rows_v<T, 0, 1>(p, grid, s) : launch_rows_v<T, 0, 0>(p, grid, s);
+    }
 }
 
 }  // namespace
