@@ -255,6 +255,13 @@ const char *lbm2d_batch_last_error(const lbm2d_batch *b);
 int lbm2d_batch_add(lbm2d_batch *b, lbm2d_solver *h, double tau, double u_inflow);
 int lbm2d_batch_remove(lbm2d_batch *b, lbm2d_solver *h);
 int lbm2d_batch_set_params(lbm2d_batch *b, lbm2d_solver *h, double tau, double u_inflow);
+/* Step budget of a member: it takes at most `steps` more steps and then sits
+ * out the batch's launches (its state is left after its last step, so
+ * members with different budgets can share one long lbm2d_batch_step call).
+ * -1 (the default) means unlimited. */
+int lbm2d_batch_set_budget(lbm2d_batch *b, lbm2d_solver *h, long long steps);
+/* Remaining budget of a member (-1: unlimited or not a member). */
+long long lbm2d_batch_budget(lbm2d_batch *b, lbm2d_solver *h);
 int lbm2d_batch_size(lbm2d_batch *b);
 /* Step every member nsteps times (asynchronous on the batch stream). */
 int lbm2d_batch_step(lbm2d_batch *b, int nsteps);

@@ -27,6 +27,7 @@ namespace {
 struct Member {
     lbm2d_solver* h;
     double tau, u;
+    long long budget = -1;  // steps the member may still take (-1: unlimited)
 };
 
 struct Group {
@@ -36,7 +37,8 @@ struct Group {
     int njobs = 0;
     KParams* d_params[2] = {nullptr, nullptr};
     int* d_block_start = nullptr;
-    ReduceJob* d_jobs = nullptr;
+    ReduceJob* d_jobs[2] = {nullptr, nullptr};  // per launch parity
+    int* d_left = nullptr;  // step budgets: [0, m) read by parity-0 launches, [m, 2m) by parity 1
     size_t cap_members = 0;
 };
 }  // namespace
@@ -49,9 +51,11 @@ struct lbm2d_batch {
     std::vector<Group> groups;
     bool layout_dirty = true;
     int bx = 128, by = 2;
-    // host staging (pinned) for parameters
+    // host staging (pinned) for parameters and budgets
     KParams* h_params = nullptr;
     size_t h_params_cap = 0;
+    int* h_left = nullptr;
+    size_t h_left_cap = 0;
     // captured step pair
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
@@ -79,7 +83,9 @@ void free_groups(lbm2d_batch* b) {
         cudaFreeAsync(g.d_params[0], b->stream);
         cudaFreeAsync(g.d_params[1], b->stream);
         cudaFreeAsync(g.d_block_start, b->stream);
-        cudaFreeAsync(g.d_jobs, b->stream);
+        cudaFreeAsync(g.d_jobs[0], b->stream);
+        cudaFreeAsync(g.d_jobs[1], b->stream);
+        cudaFreeAsync(g.d_left, b->stream);
     }
     b->groups.clear();
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -118,7 +124,9 @@ int build_layout(lbm2d_batch* b) {
         BCK(cudaMallocAsync(&g.d_params[0], m * sizeof(KParams), b->stream), "batch params");
         BCK(cudaMallocAsync(&g.d_params[1], m * sizeof(KParams), b->stream), "batch params");
         BCK(cudaMallocAsync(&g.d_block_start, (m + 1) * sizeof(int), b->stream), "batch table");
-        BCK(cudaMallocAsync(&g.d_jobs, m * sizeof(ReduceJob), b->stream), "batch jobs");
+        BCK(cudaMallocAsync(&g.d_jobs[0], m * sizeof(ReduceJob), b->stream), "batch jobs");
+        BCK(cudaMallocAsync(&g.d_jobs[1], m * sizeof(ReduceJob), b->stream), "batch jobs");
+        BCK(cudaMallocAsync(&g.d_left, 2 * m * sizeof(int), b->stream), "batch budgets");
         g.cap_members = m;
     }
     b->layout_dirty = false;
@@ -126,11 +134,18 @@ int build_layout(lbm2d_batch* b) {
 }
 
 int ensure_host_params(lbm2d_batch* b, size_t n) {
-    if (n <= b->h_params_cap) return LBM2D_OK;
-    if (b->h_params) cudaFreeHost(b->h_params);
-    b->h_params = nullptr;
-    BCK(cudaMallocHost(&b->h_params, n * sizeof(KParams)), "pinned params");
-    b->h_params_cap = n;
+    if (n > b->h_params_cap) {
+        if (b->h_params) cudaFreeHost(b->h_params);
+        b->h_params = nullptr;
+        BCK(cudaMallocHost(&b->h_params, n * sizeof(KParams)), "pinned params");
+        b->h_params_cap = n;
+    }
+    if (n > b->h_left_cap) {
+        if (b->h_left) cudaFreeHost(b->h_left);
+        b->h_left = nullptr;
+        BCK(cudaMallocHost(&b->h_left, n * sizeof(int)), "pinned budgets");
+        b->h_left_cap = n;
+    }
     return LBM2D_OK;
 }
 
@@ -146,8 +161,9 @@ int prepare(lbm2d_batch* b) {
         const size_t m = g.members.size();
         KParams* p0 = b->h_params + off;
         KParams* p1 = p0 + m;
+        int* left = b->h_left + off;
         std::vector<int> start(m + 1, 0);
-        std::vector<ReduceJob> jobs;
+        std::vector<ReduceJob> jobs[2];
         for (size_t k = 0; k < m; ++k) {
             Member& mem = b->members[g.members[k]];
             lbm2d_solver* h = mem.h;
@@ -159,6 +175,12 @@ int prepare(lbm2d_batch* b) {
             KParams p;
             const long long l0 = h->launches;
             if ((rc = prepare_steps(h, mem.tau, mem.u, p))) return bfail(b, rc, std::string("member: ") + h->err);
+            const bool budgeted = mem.budget >= 0;
+            left[k] = (int)std::min<long long>(std::max(mem.budget, 0LL), 0x7FFFFFFF);
+            if (budgeted) {
+                p.left_in = g.d_left + k;
+                p.left_out = g.d_left + m + k;
+            }
             p0[k] = p;
             p1[k] = p;
             p1[k].fin = p.fout;
@@ -167,6 +189,8 @@ int prepare(lbm2d_batch* b) {
             p1[k].gout = const_cast<void*>(p.gin);
             p1[k].seed_in = p.seed_out;
             p1[k].seed_out = const_cast<uint32_t*>(p.seed_in);
+            p1[k].left_in = p.left_out;
+            p1[k].left_out = const_cast<int*>(p.left_in);
             // order the batch stream after the member's own preparation (a
             // prologue on the member's stream); nothing to order otherwise,
             // the member's stream already waits for the batch's last step
@@ -176,19 +200,26 @@ int prepare(lbm2d_batch* b) {
             }
             const int gy = (h->ny + b->by - 1) / b->by;
             start[k + 1] = start[k] + p.gx * gy;
-            if (h->nslots > 0)
-                jobs.push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last});
+            if (h->nslots > 0) {
+                jobs[0].push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last,
+                                   budgeted ? g.d_left + k : nullptr});
+                jobs[1].push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last,
+                                   budgeted ? g.d_left + m + k : nullptr});
+            }
         }
         g.nblocks = start[m];
-        g.njobs = (int)jobs.size();
+        g.njobs = (int)jobs[0].size();
         BCK(cudaMemcpyAsync(g.d_params[0], p0, m * sizeof(KParams), cudaMemcpyHostToDevice, b->stream), "params");
         BCK(cudaMemcpyAsync(g.d_params[1], p1, m * sizeof(KParams), cudaMemcpyHostToDevice, b->stream), "params");
+        // budgets at the start of the call, read by the first (parity-0) launch
+        BCK(cudaMemcpyAsync(g.d_left, left, m * sizeof(int), cudaMemcpyHostToDevice, b->stream), "budgets");
         BCK(cudaMemcpyAsync(g.d_block_start, start.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice, b->stream),
             "table");
-        if (!jobs.empty())
-            BCK(cudaMemcpyAsync(g.d_jobs, jobs.data(), jobs.size() * sizeof(ReduceJob), cudaMemcpyHostToDevice,
-                                b->stream),
-                "jobs");
+        for (int par = 0; par < 2; ++par)
+            if (!jobs[par].empty())
+                BCK(cudaMemcpyAsync(g.d_jobs[par], jobs[par].data(), jobs[par].size() * sizeof(ReduceJob),
+                                    cudaMemcpyHostToDevice, b->stream),
+                    "jobs");
         off += 2 * m;
     }
     // the staging buffers may be rewritten by the next call: wait for the copies
@@ -203,7 +234,7 @@ int launch_one(lbm2d_batch* b, int parity) {
         ++b->launches;
         if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
         if (g.njobs > 0) {
-            e = launch_batch_force_reduce(g.d_jobs, g.njobs, b->stream);
+            e = launch_batch_force_reduce(g.d_jobs[parity], g.njobs, b->stream);
             ++b->launches;
             if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch reduce: ") + cudaGetErrorString((cudaError_t)e));
         }
@@ -270,6 +301,7 @@ int lbm2d_batch_destroy(lbm2d_batch* b) {
     free_groups(b);
     cudaStreamSynchronize(b->stream);
     if (b->h_params) cudaFreeHost(b->h_params);
+    if (b->h_left) cudaFreeHost(b->h_left);
     cudaEventDestroy(b->ev);
     cudaStreamDestroy(b->stream);
     delete b;
@@ -311,6 +343,21 @@ int lbm2d_batch_set_params(lbm2d_batch* b, lbm2d_solver* h, double tau, double u
     return LBM2D_OK;
 }
 
+int lbm2d_batch_set_budget(lbm2d_batch* b, lbm2d_solver* h, long long steps) {
+    if (!b || !h) return LBM2D_ERR_INVALID;
+    const int k = member_index(b, h);
+    if (k < 0) return bfail(b, LBM2D_ERR_INVALID, "not a member");
+    if (steps > 0x7FFFFFFF) return bfail(b, LBM2D_ERR_INVALID, "budget above 2^31 - 1 steps");
+    b->members[k].budget = steps < 0 ? -1 : steps;
+    return LBM2D_OK;
+}
+
+long long lbm2d_batch_budget(lbm2d_batch* b, lbm2d_solver* h) {
+    if (!b || !h) return -1;
+    const int k = member_index(b, h);
+    return k < 0 ? -1 : b->members[k].budget;
+}
+
 int lbm2d_batch_size(lbm2d_batch* b) { return b ? (int)b->members.size() : 0; }
 
 int lbm2d_batch_step(lbm2d_batch* b, int nsteps) {
@@ -334,10 +381,15 @@ int lbm2d_batch_step(lbm2d_batch* b, int nsteps) {
     }
     for (auto& m : b->members) {
         lbm2d_solver* h = m.h;
-        h->cur ^= (nsteps & 1);
-        h->steps_since_collide += nsteps;
-        h->steps_done += nsteps;
-        h->u_last = m.u;
+        long long taken = nsteps;
+        if (m.budget >= 0) {
+            taken = std::min<long long>(m.budget, nsteps);
+            m.budget -= taken;
+        }
+        h->cur ^= (int)(taken & 1);
+        h->steps_since_collide += taken;
+        h->steps_done += taken;
+        if (taken > 0) h->u_last = m.u;
     }
     BCK(cudaEventRecord(b->ev, b->stream), "event");
     for (auto& m : b->members) BCK(cudaStreamWaitEvent(m.h->stream, b->ev, 0), "member wait");

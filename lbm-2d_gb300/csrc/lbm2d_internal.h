@@ -96,6 +96,10 @@ struct KParams {
     const uint32_t* seed_in;
     uint32_t* seed_out;
     uint32_t seed_host;
+    // batched launches only: remaining step budget of the instance (null:
+    // unlimited); read from left_in, decremented into left_out
+    const int* left_in;
+    int* left_out;
 };
 
 // Readback outputs (any may be null).
@@ -113,6 +117,7 @@ struct ReduceJob {
     double* hist;
     unsigned long long* counter;
     double* last;
+    const int* left;  // the step's budget word (null: unlimited); <= 0 means no step was taken
 };
 
 // Launchers (lbm2d_kernels.cu).  All return a cudaError_t as int.

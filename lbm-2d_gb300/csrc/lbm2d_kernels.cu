@@ -123,12 +123,15 @@ __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
 // instance k owns the launch blocks [block_start[k], block_start[k+1]) and
 // walks its own block grid (gx = p.gx blocks wide).  The block finds its
 // instance by binary search and stages that instance's parameters in shared
-// memory once.
-template <class T, bool TH>
-__global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restrict__ inst,
-                                                         const int* __restrict__ block_start, int ninst) {
-    __shared__ KParams sp;
-    __shared__ int s_inst;
+// memory once.  An instance with a step budget (left_in set) whose budget is
+// spent does nothing; otherwise its first block hands the decremented budget
+// to the next launch through left_out (the two budget words swap roles
+// between launches, so no launch reads a word it writes).  Returns false
+// when the block has nothing to do.
+__device__ __forceinline__ bool batch_block_begin(const KParams* __restrict__ inst,
+                                                  const int* __restrict__ block_start, int ninst, KParams& sp,
+                                                  int& local) {
+    __shared__ int s_inst, s_left;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int b = blockIdx.x;
     if (tid == 0) {
@@ -150,8 +153,23 @@ __global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restri
         const int nw = (int)(sizeof(KParams) / sizeof(int));
         for (int w = tid; w < nw; w += blockDim.x * blockDim.y) dst[w] = src[w];
     }
+    local = b - block_start[k];
+    if (tid == 0) {
+        const int* li = inst[k].left_in;
+        const int L = li ? *li : 1;
+        if (li && local == 0) *inst[k].left_out = L > 0 ? L - 1 : 0;
+        s_left = L;
+    }
     __syncthreads();
-    const int local = b - block_start[k];
+    return s_left > 0;
+}
+
+template <class T, bool TH>
+__global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restrict__ inst,
+                                                         const int* __restrict__ block_start, int ninst) {
+    __shared__ KParams sp;
+    int local;
+    if (!batch_block_begin(inst, block_start, ninst, sp, local)) return;
     step_block<T, TH>(sp, local % sp.gx, local / sp.gx, sp.gx);
 }
 
@@ -159,30 +177,8 @@ template <class T>
 __global__ void __launch_bounds__(512) batch_step_pair_kernel(const KParams* __restrict__ inst,
                                                               const int* __restrict__ block_start, int ninst) {
     __shared__ KParams sp;
-    __shared__ int s_inst;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int b = blockIdx.x;
-    if (tid == 0) {
-        int lo = 0, hi = ninst - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (block_start[mid] <= b)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        s_inst = lo;
-    }
-    __syncthreads();
-    const int k = s_inst;
-    {
-        const int* src = reinterpret_cast<const int*>(inst + k);
-        int* dst = reinterpret_cast<int*>(&sp);
-        const int nw = (int)(sizeof(KParams) / sizeof(int));
-        for (int w = tid; w < nw; w += blockDim.x * blockDim.y) dst[w] = src[w];
-    }
-    __syncthreads();
-    const int local = b - block_start[k];
+    int local;
+    if (!batch_block_begin(inst, block_start, ninst, sp, local)) return;
     step_pair_block<T>(sp, local % sp.gx, local / sp.gx, sp.gx);
 }
 
@@ -401,6 +397,7 @@ __global__ void force_reduce_kernel(const double* __restrict__ part, int nslots,
 // Force reduction of several instances: block b reduces job b.
 __global__ void batch_force_reduce_kernel(const ReduceJob* __restrict__ jobs) {
     const ReduceJob j = jobs[blockIdx.x];
+    if (j.left && *j.left <= 0) return;  // the instance's budget was spent: no step, no history entry
     double a = 0.0, b = 0.0;
     for (int k = threadIdx.x; k < j.nslots; k += blockDim.x) {
         a += j.partials[2 * k];

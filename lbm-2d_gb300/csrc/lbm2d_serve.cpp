@@ -10,10 +10,11 @@
 //     requests are set up at once, on the host cores, while the GPU steps
 //     the others.
 //   * The stepping thread adds the solves that are ready to the batch and
-//     advances every active solve together: one lbm2d_batch_step per tick
-//     (one packed launch per step per storage group, CUDA-graph replay), the
-//     tick being the smallest remaining budget capped at steps_per_tick, so
-//     every solve stops exactly at its budget;
+//     advances every active solve together: one lbm2d_batch_step of
+//     steps_per_tick steps per tick (one packed launch per step per storage
+//     group, CUDA-graph replay); each solve carries its remaining budget into
+//     the batch and sits out the launches after it is spent, so every solve
+//     stops exactly at its budget without shortening the tick;
 //   * it then retires finished solves (non-finite check, drag/lift read back,
 //     memory freed) and records arrival, admission and completion times.
 #include <algorithm>
@@ -266,8 +267,10 @@ void join_ready(lbm2d_server* s) {
         r.swap(s->ready);
     }
     for (auto& a : r) {
-        const int rc = lbm2d_batch_add(s->batch, a.h, a.tau, a.u_bc);
+        int rc = lbm2d_batch_add(s->batch, a.h, a.tau, a.u_bc);
+        if (!rc) rc = lbm2d_batch_set_budget(s->batch, a.h, a.left);
         if (rc) {
+            lbm2d_batch_remove(s->batch, a.h);
             release(s, a, rc);
             continue;
         }
@@ -286,8 +289,11 @@ void worker_loop(lbm2d_server* s) {
             if (s->stop) return;
             continue;
         }
-        long long k = s->steps_per_tick;
-        for (auto& a : s->active) k = std::min(k, a.left);
+        // every solve carries its own budget into the batch, so a tick can be
+        // long: a solve whose budget runs out mid-tick sits out the rest
+        long long k = 0;
+        for (auto& a : s->active) k = std::max(k, a.left);
+        k = std::min<long long>(k, s->steps_per_tick);
         // the members of this tick; solves joining below wait for the next one
         const size_t n_tick = s->active.size();
         const double t0 = now_s();
@@ -302,8 +308,9 @@ void worker_loop(lbm2d_server* s) {
         s->busy_s += now_s() - t0;
         for (size_t i = 0; i < n_tick; ++i) {
             Active& a = s->active[i];
-            a.left -= k;
-            s->lattice_updates += k * (long long)a.req.nx * a.req.ny;
+            const long long taken = std::min(a.left, k);
+            a.left -= taken;
+            s->lattice_updates += taken * (long long)a.req.nx * a.req.ny;
         }
         for (size_t i = n_tick; i-- > 0;) {
             Active& a = s->active[i];

@@ -127,6 +127,8 @@ _SIGS = {
     "lbm2d_batch_remove": ([_P, _P], _I),
     "lbm2d_batch_set_params": ([_P, _P, _D, _D], _I),
     "lbm2d_batch_size": ([_P], _I),
+    "lbm2d_batch_set_budget": ([_P, _P, C.c_longlong], _I),
+    "lbm2d_batch_budget": ([_P, _P], C.c_longlong),
     "lbm2d_batch_step": ([_P, _I], _I),
     "lbm2d_batch_synchronize": ([_P], _I),
     "lbm2d_batch_set_block": ([_P, _I, _I], _I),
@@ -530,6 +532,13 @@ class Batch:
 
     def set_params(self, solver: Solver, tau: float, u_in: float):
         self._ck(self.L.lbm2d_batch_set_params(self.h, solver.h, float(tau), float(u_in)))
+
+    def set_budget(self, solver: Solver, steps: int):
+        """The member takes at most `steps` more steps (-1: unlimited)."""
+        self._ck(self.L.lbm2d_batch_set_budget(self.h, solver.h, int(steps)))
+
+    def budget(self, solver: Solver) -> int:
+        return int(self.L.lbm2d_batch_budget(self.h, solver.h))
 
     def step(self, n: int = 1):
         self._ck(self.L.lbm2d_batch_step(self.h, int(n)))

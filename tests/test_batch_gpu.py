@@ -104,3 +104,43 @@ def test_autotune_preserves_state(product, oracle_lib):
     assert len(fx) == 10 and np.allclose(fx, rfx, rtol=1e-6)
     s.close()
     ref.close()
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_member_budgets(product, oracle_lib, storage):
+    """Members with different step budgets share one long batched call: each
+    stops exactly at its budget (steps taken, force history length) and ends
+    bit-for-bit where a batch stepped for exactly that many steps ends."""
+    cases = [("cylinder_mei", 9), ("step", 16), ("naca_polygon", 3), ("ribs_les", 0), ("cavity_mrt", 25)]
+    b = product.Batch()
+    mem = []
+    for name, budget in cases:
+        spec = CS.CASES[name]
+        s = make(product, oracle_lib, name, storage)
+        b.add(s, spec["tau"], spec["u"])
+        b.set_budget(s, budget)
+        mem.append(s)
+    b.step(12)  # odd / even budgets below and above the call length
+    b.step(12)
+    b.synchronize()
+    for (name, budget), s in zip(cases, mem):
+        spec = CS.CASES[name]
+        assert b.budget(s) == max(budget - 24, 0)
+        taken = min(budget, 24)
+        assert s.info().steps_done == taken, name
+        ref_b = product.Batch()
+        r = make(product, oracle_lib, name, storage)
+        ref_b.add(r, spec["tau"], spec["u"])
+        if taken:
+            ref_b.step(taken)
+        ref_b.synchronize()
+        assert np.array_equal(s.f, r.f), name
+        fx, _ = s.force_history()
+        rx, _ = r.force_history()
+        assert len(fx) == len(rx) == (taken if spec["case"] != CS.CAVITY else 0), name
+        assert np.array_equal(fx, rx), name
+        ref_b.close()
+        r.close()
+    b.close()
+    for s in mem:
+        s.close()
