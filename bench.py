@@ -332,7 +332,9 @@ def run_serve(args):
              "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
              "mean_s": float(lat.mean()), "makespan_s": span, "glups": lu / span / 1e9,
              "busy_glups": st["lattice_updates"] / max(st["busy_s"], 1e-9) / 1e9, "lattice_updates": lu,
-             "setup_s": st["setup_s"]}
+             "setup_s": st["setup_s"], "gpu_s": st["gpu_s"],
+             "stepping_thread_s": {k: st[k] for k in ("call_s", "wait_s", "retire_s", "join_s")},
+             "gpu_glups": st["lattice_updates"] / max(st["gpu_s"], 1e-9) / 1e9}
     # --- sequential plain solves, FIFO, same arrival times:
     #   "dropin": the reference drivers' loop through the per-solve API, one
     #             lbm2d_step call per time step followed by the drag/lift

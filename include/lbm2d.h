@@ -309,6 +309,8 @@ typedef struct lbm2d_server_stats_t {
     long long ticks;        /* batched step calls made */
     long long member_ticks; /* sum over ticks of the solves in the tick */
     double setup_s;         /* host time spent building requests (all set-up threads) */
+    double gpu_s;           /* time from the start to the end of each tick's batched step on the device */
+    double call_s, wait_s, retire_s, join_s; /* stepping thread: step calls, device waits, retirements, joins */
 } lbm2d_server_stats_t;
 
 typedef struct lbm2d_server lbm2d_server;

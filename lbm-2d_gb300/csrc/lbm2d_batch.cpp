@@ -199,7 +199,7 @@ int prepare(lbm2d_batch* b) {
                 BCK(cudaStreamWaitEvent(b->stream, b->ev, 0), "wait");
             }
             const int gy = (h->ny + b->by - 1) / b->by;
-            start[k + 1] = start[k] + p.gx * gy;
+            start[k + 1] = start[k] + (p.gx * gy + kBatchTiles - 1) / kBatchTiles;
             if (h->nslots > 0) {
                 jobs[0].push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last,
                                    budgeted ? g.d_left + k : nullptr});

@@ -127,7 +127,10 @@ int launch_readback(int storage, const KParams& p, const ROut& o, void* stream);
 int launch_prologue(int storage, const KParams& p, const double* f_aos, const double* g_aos, void* stream);
 // Step several instances at once: inst[] holds one KParams per instance and
 // block_start[] (ninst+1 entries, device memory) the first launch block of
-// each instance; nblocks = block_start[ninst].
+// each instance; nblocks = block_start[ninst].  A launch block walks
+// kBatchTiles consecutive blocks (tiles) of its instance's block grid, so an
+// instance with gx*gy tiles owns ceil(gx*gy / kBatchTiles) launch blocks.
+constexpr int kBatchTiles = 4;
 int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
                       int bx, int by, void* stream, int pair);
 int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream);

@@ -170,7 +170,9 @@ __global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restri
     __shared__ KParams sp;
     int local;
     if (!batch_block_begin(inst, block_start, ninst, sp, local)) return;
-    step_block<T, TH>(sp, local % sp.gx, local / sp.gx, sp.gx);
+    const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
+    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+        step_block<T, TH>(sp, t % sp.gx, t / sp.gx, sp.gx);
 }
 
 template <class T>
@@ -179,7 +181,9 @@ __global__ void __launch_bounds__(512) batch_step_pair_kernel(const KParams* __r
     __shared__ KParams sp;
     int local;
     if (!batch_block_begin(inst, block_start, ninst, sp, local)) return;
-    step_pair_block<T>(sp, local % sp.gx, local / sp.gx, sp.gx);
+    const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
+    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+        step_pair_block<T>(sp, t % sp.gx, t / sp.gx, sp.gx);
 }
 
 // Post-stream state of node (x, y) in FP64: stored deviations are widened

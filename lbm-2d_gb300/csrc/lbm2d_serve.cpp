@@ -88,6 +88,11 @@ struct lbm2d_server {
     double busy_s = 0.0;
     long long lattice_updates = 0;
     long long ticks = 0, member_ticks = 0;
+    double gpu_s = 0.0;  // device time of the ticks (CUDA events on the batch stream)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // stepping-thread time split: step call (prepare + enqueue), wait for the
+    // device, retirement, joining ready solves
+    double call_s = 0.0, wait_s = 0.0, retire_s = 0.0, join_s = 0.0;
 };
 
 namespace {
@@ -297,12 +302,22 @@ void worker_loop(lbm2d_server* s) {
         // the members of this tick; solves joining below wait for the next one
         const size_t n_tick = s->active.size();
         const double t0 = now_s();
+        cudaStream_t bs = static_cast<cudaStream_t>(lbm2d_batch_stream(s->batch));
+        if (s->ev0) cudaEventRecord(s->ev0, bs);
         int rc = lbm2d_batch_step(s->batch, (int)k);
+        if (s->ev1) cudaEventRecord(s->ev1, bs);
+        const double t1 = now_s();
         join_ready(s);  // adding members only edits the host-side member list
+        const double t2 = now_s();
         // wait for the tick only: a diverged solve must not fail the others;
         // each solve's own non-finite flag is read when it retires
-        if (!rc && cudaStreamSynchronize(static_cast<cudaStream_t>(lbm2d_batch_stream(s->batch))) != cudaSuccess)
-            rc = LBM2D_ERR_CUDA;
+        if (!rc && cudaStreamSynchronize(bs) != cudaSuccess) rc = LBM2D_ERR_CUDA;
+        const double t3 = now_s();
+        s->call_s += t1 - t0;
+        s->join_s += t2 - t1;
+        s->wait_s += t3 - t2;
+        float ms = 0.0f;
+        if (!rc && s->ev0 && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) s->gpu_s += 1e-3 * ms;
         ++s->ticks;
         s->member_ticks += (long long)n_tick;
         s->busy_s += now_s() - t0;
@@ -312,6 +327,7 @@ void worker_loop(lbm2d_server* s) {
             a.left -= taken;
             s->lattice_updates += taken * (long long)a.req.nx * a.req.ny;
         }
+        const double t4 = now_s();
         for (size_t i = n_tick; i-- > 0;) {
             Active& a = s->active[i];
             if (a.left <= 0 || rc) {
@@ -320,6 +336,7 @@ void worker_loop(lbm2d_server* s) {
                 retire(s, i, st);
             }
         }
+        s->retire_s += now_s() - t4;
     }
 }
 
@@ -339,6 +356,8 @@ int lbm2d_server_create(int device, double budget_bytes, int max_active, int ste
         delete s;
         return rc;
     }
+    cudaSetDevice(device);
+    if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) s->ev0 = s->ev1 = nullptr;
     s->worker = std::thread(worker_loop, s);
     const unsigned hw = std::thread::hardware_concurrency();
     const int n_setup = (int)std::max(1u, std::min(hw > 2 ? hw - 2 : 1u, 6u));
@@ -384,6 +403,11 @@ int lbm2d_server_stats(lbm2d_server* s, lbm2d_server_stats_t* st) {
     st->queued = (long long)s->queue.size();
     st->active = (long long)s->live;
     st->setup_s = s->setup_s;
+    st->gpu_s = s->gpu_s;
+    st->call_s = s->call_s;
+    st->wait_s = s->wait_s;
+    st->retire_s = s->retire_s;
+    st->join_s = s->join_s;
     st->busy_s = s->busy_s;
     st->lattice_updates = s->lattice_updates;
     st->device_bytes_in_use = (double)s->used;
@@ -408,6 +432,8 @@ int lbm2d_server_destroy(lbm2d_server* s) {
     join_ready(s);  // set up but never stepped
     for (size_t k = s->active.size(); k-- > 0;) retire(s, k, LBM2D_ERR_STATE);
     lbm2d_batch_destroy(s->batch);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
     delete s;
     return LBM2D_OK;
 }

@@ -68,7 +68,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("finished", C.c_longlong), ("queued", C.c_longlong),
                 ("active", C.c_longlong), ("busy_s", C.c_double), ("lattice_updates", C.c_longlong),
                 ("device_bytes_in_use", C.c_double), ("ticks", C.c_longlong), ("member_ticks", C.c_longlong),
-                ("setup_s", C.c_double)]
+                ("setup_s", C.c_double), ("gpu_s", C.c_double), ("call_s", C.c_double), ("wait_s", C.c_double),
+                ("retire_s", C.c_double), ("join_s", C.c_double)]
 
 
 class ForceStats(C.Structure):
