@@ -953,8 +953,10 @@ struct PairStore;
 // Two x-neighbours (index i even) in storage units as one 8-byte / 4-byte store.
 template <>
 struct PairStore<float> {
+    // streaming store: the next step reads the populations back from DRAM
+    // anyway (the lattice is far larger than L2); measured +0.5-1.7% for FP32
     static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, uint32_t) {
-        *reinterpret_cast<float2*>(p + i) = make_float2(a, b);
+        __stcs(reinterpret_cast<float2*>(p + i), make_float2(a, b));
     }
 };
 template <>

@@ -45,8 +45,10 @@ struct RowsCfg {
     static constexpr int FLAGS_OFF = 9 * ROW_BYTES;
     static constexpr int STAGE_BYTES = ((FLAGS_OFF + kTileW * 4) + 127) / 128 * 128;
     // FP32 moves twice the bytes per node: 2 CTAs per SM with deeper
-    // registers; the 16-bit forms are latency-bound on the arithmetic: 3 CTAs
-    static constexpr int STAGES = 4;
+    // registers and a 3-tile ring (measured faster than 4 or 5 tiles in
+    // flight); the 16-bit forms are latency-bound on the arithmetic: 3 CTAs
+    // with a 4-tile ring
+    static constexpr int STAGES = ES == 4 ? 3 : 4;
     static constexpr int MIN_BLOCKS = ES == 4 ? 2 : 3;
     static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
     static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;  // FP64 force sums, 2 per consumer warp
