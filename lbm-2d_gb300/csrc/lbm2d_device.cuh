@@ -118,10 +118,11 @@ struct Pop<__nv_bfloat16> {
 
 // ----------------------------------------------------------------- rounding noise
 // Random words for stochastic rounding: the lowbias32 integer hash (C.
-// Wellons, 2018) of a per-node key; nine words come from three hashes
-// combined by XOR and rotation (each word is uniform, which is all unbiased
-// rounding needs).  The key is node + seed * golden-ratio constant, the seed
-// advancing by one per step through the solver's seed words (see seed_of).
+// Wellons, 2018) of a per-node key, times nine distinct odd constants.
+// Multiplication by an odd constant is a bijection of the 32-bit words, so
+// every word is exactly uniform, which is all unbiased rounding needs.  The
+// key is node + seed * golden-ratio constant, the seed advancing by one per
+// step through the solver's seed words (see seed_of).
 __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
     x ^= x >> 16;
     x *= 0x7feb352du;
@@ -132,16 +133,16 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
 }
 
 __device__ __forceinline__ void rand9(uint32_t key, uint32_t r[9]) {
-    const uint32_t a = lowbias32(key), b = lowbias32(key ^ 0x9E3779B9u), c = lowbias32(key + 0x7F4A7C15u);
-    r[0] = a;
-    r[1] = b;
-    r[2] = c;
-    r[3] = a ^ b;
-    r[4] = b ^ c;
-    r[5] = a ^ c;
-    r[6] = a ^ b ^ c;
-    r[7] = __funnelshift_l(a, a, 16) ^ b;
-    r[8] = __funnelshift_l(b, b, 16) ^ c;
+    const uint32_t h = lowbias32(key);
+    r[0] = h;
+    r[1] = h * 0x9E3779B1u;
+    r[2] = h * 0x85EBCA77u;
+    r[3] = h * 0xC2B2AE3Du;
+    r[4] = h * 0x27D4EB2Fu;
+    r[5] = h * 0x165667B1u;
+    r[6] = h * 0xD3A2646Du;
+    r[7] = h * 0xFD7046C5u;
+    r[8] = h * 0xB55A4F09u;
 }
 
 // Seed of this launch's rounding noise, and the hand-over to the next launch:
@@ -508,14 +509,12 @@ __device__ __forceinline__ void collide(const KParams& p, uint32_t fl, R f[9], R
 // Nodes whose post-stream state is more than the plain pull (solid,
 // boundary record, a boundary-condition row or column, a thermal hook) are
 // rebuilt through build_state on full populations and converted back.
+// Boundary-condition rows and columns carry a (possibly empty) boundary
+// record (the geometry builder gives them one), so the flags alone mark
+// every node of a non-thermal step that needs more than the plain pull.
 template <bool TH>
 __device__ __forceinline__ bool special_node(const KParams& p, int x, int y, uint32_t fl) {
     if (fl & (FLAG_SOLID | FLAG_BOUNDARY)) return true;
-    if (p.bc_kind == BC_LID) {
-        if (y == p.ny - 1) return true;
-    } else if (p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) {
-        if (x == 0 || x == p.nx - 1) return true;
-    }
     if (TH && p.hook_kind == 1 && (x == 1 || x == p.nx - 2 || y == 1 || y == p.ny - 2)) return true;
     return false;
 }

@@ -100,6 +100,15 @@ bool build_geometry(const GeometryInput& in, GeometryTables& t, std::string& err
     const BBGeometry& g = *in.bb;
     const bool cavity = in.case_type == CASE_CAVITY;
     const bool periodic = in.case_type == CASE_RIBS || in.case_type == CASE_HILLS;
+    // nodes a boundary condition may rewrite (src/lbm.hpp:531-540): the lid
+    // row of the cavity, the inlet and outlet columns of the open cases.  They
+    // get a record even without bounce-back links, so the step kernels find
+    // every node that needs more than the plain pull from its flags alone.
+    auto bc_node = [&](int x, int y) {
+        if (cavity) return y == ny - 1;
+        if (periodic) return false;
+        return x == 0 || x == nx - 1;
+    };
     const bool interp = g.valid();
     t = GeometryTables();
     t.flags.assign(n, 0u);
@@ -168,7 +177,7 @@ bool build_geometry(const GeometryInput& in, GeometryTables& t, std::string& err
                     }
                 }
             }
-            if (ftypes == 0 && gbb == 0) {
+            if (ftypes == 0 && gbb == 0 && !bc_node(x, y)) {
                 uint32_t wd = 0;
                 if (in.les) {
                     const double d = t.wall_dist[id];
