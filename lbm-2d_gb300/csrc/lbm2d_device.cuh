@@ -384,13 +384,12 @@ __device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint
     }
 }
 
+// LES wall distance of a fluid node: a boundary node's record holds it; any
+// other fluid node's flags are its FP32 bit pattern (bits 0-1 zero).
 template <class R>
 __device__ __forceinline__ R wall_distance(const KParams& p, uint32_t fl) {
     if (fl & FLAG_BOUNDARY) return R(p.rec_wd[fl >> 2]);
-    const uint32_t d = fl >> 2;
-    if (d == WD_UNREACHED) return R(1e9);
-    if (d < (1u << 23)) return R(__uint_as_float(0x4B000000u | d) - 8388608.0f);  // exact integer
-    return R(d);
+    return R(__uint_as_float(fl));
 }
 
 // Collision of one fluid node: src/lbm.hpp:300-354 (mrt_collide :128-218,
@@ -855,8 +854,9 @@ __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla,
     const F2 inv = rcp2(rho);
     const F2 k = S == 1.0f ? inv : inv * sp2(iS);  // 1 / (rho * S)
     const F2 u = mx * k, v = my * k;
-    if ((fa_ok && (!(rho.v.x == rho.v.x) || rho.v.x == 0.0f)) || (fb_ok && (!(rho.v.y == rho.v.y) || rho.v.y == 0.0f)))
-        atomicOr(p.nan_flag, 1u);
+    // a non-finite or zero density in a collided lane: the product of the two
+    // lanes' densities (1 for a solid lane) is NaN or zero
+    if (!(fabsf((fa_ok ? rho.v.x : 1.0f) * (fb_ok ? rho.v.y : 1.0f)) > 0.0f)) atomicOr(p.nan_flag, 1u);
     const float F = q.Fscale * S;
     F2 o[9];
     if (mrt) {

@@ -4,6 +4,7 @@
 #include "lbm2d_geometry.h"
 
 #include <cmath>
+#include <cstring>
 #include <deque>
 
 #include "lbm2d_internal.h"
@@ -178,16 +179,21 @@ bool build_geometry(const GeometryInput& in, GeometryTables& t, std::string& err
                 }
             }
             if (ftypes == 0 && gbb == 0 && !bc_node(x, y)) {
-                uint32_t wd = 0;
+                // the LES wall distance as an FP32 bit pattern: an integer
+                // below 2^21 (or the reference's 1e9 for "no wall") has its
+                // two lowest mantissa bits zero, so bits 0-1 stay free for the
+                // solid / boundary flags and the kernels decode it with a mask
+                uint32_t bits = 0;
                 if (in.les) {
                     const double d = t.wall_dist[id];
-                    wd = d >= 1e9 ? WD_UNREACHED : static_cast<uint32_t>(d);
-                    if (d < 1e9 && d >= static_cast<double>(WD_UNREACHED)) {
-                        err = "wall distance exceeds the flag field";
+                    if (d < 1e9 && d >= static_cast<double>(1u << 21)) {
+                        err = "wall distance exceeds 2^21 nodes";
                         return false;
                     }
+                    const float df = d >= 1e9 ? 1e9f : static_cast<float>(d);
+                    std::memcpy(&bits, &df, sizeof(bits));
                 }
-                t.flags[id] = wd << 2;
+                t.flags[id] = bits;
                 continue;
             }
             const size_t r = t.rec_info.size();

@@ -10,8 +10,10 @@
 //   flags       : one uint32 per node
 //                   bit 0      solid
 //                   bit 1      boundary node (has a boundary record)
-//                   bits 2..31 record index (boundary) or LES wall distance
-//                              (fluid; WD_UNREACHED means "no obstacle")
+//                   boundary node: bits 2..31 = record index
+//                   other fluid node: the LES wall distance as FP32 bits
+//                              (an integer below 2^21, or 1e9 for "no
+//                              obstacle"; its two low mantissa bits are 0)
 //   records     : per boundary node: slot types, thermal bounce mask, force
 //                 mask, wall distance, and per-slot q / wall velocity for
 //                 interpolated links.
@@ -23,7 +25,6 @@ namespace lbm2d {
 
 constexpr uint32_t FLAG_SOLID = 1u;
 constexpr uint32_t FLAG_BOUNDARY = 2u;
-constexpr uint32_t WD_UNREACHED = 0x3FFFFFFFu;  // stands for the reference's 1e9
 constexpr uint32_t MAX_RECORDS = 0x3FFFFFFFu;
 
 // Slot types (2 bits per pull slot j) in rec_info bits 0..17.
