@@ -31,7 +31,9 @@ struct Member {
 };
 
 struct Group {
-    int storage = 0, thermal = 0, pair = 0;
+    int storage = 0, thermal = 0;
+    int kind = 0;  // KERNEL_SCALAR / KERNEL_PAIR (batched launches) or KERNEL_ROWS (solo launches)
+    std::vector<KParams> host;  // KERNEL_ROWS: each member's parameters of the call's first step
     std::vector<int> members;  // indices into lbm2d_batch::members
     int nblocks = 0;
     int njobs = 0;
@@ -106,14 +108,14 @@ int build_layout(lbm2d_batch* b) {
     std::map<std::tuple<int, int, int>, int> gi;
     for (size_t k = 0; k < b->members.size(); ++k) {
         lbm2d_solver* h = b->members[k].h;
-        const auto key = std::make_tuple(h->storage, h->thermal ? 1 : 0, use_pair(h) ? 1 : 0);
+        const auto key = std::make_tuple(h->storage, h->thermal ? 1 : 0, kernel_kind(h));
         auto it = gi.find(key);
         if (it == gi.end()) {
             gi[key] = (int)b->groups.size();
             Group g;
             g.storage = std::get<0>(key);
             g.thermal = std::get<1>(key);
-            g.pair = std::get<2>(key);
+            g.kind = std::get<2>(key);
             b->groups.push_back(g);
             it = gi.find(key);
         }
@@ -207,6 +209,13 @@ int prepare(lbm2d_batch* b) {
                                    budgeted ? g.d_left + m + k : nullptr});
             }
         }
+        if (g.kind == KERNEL_ROWS) {
+            g.host.assign(p0, p0 + m);
+            g.nblocks = 0;
+            g.njobs = 0;
+            off += 2 * m;
+            continue;
+        }
         g.nblocks = start[m];
         g.njobs = (int)jobs[0].size();
         BCK(cudaMemcpyAsync(g.d_params[0], p0, m * sizeof(KParams), cudaMemcpyHostToDevice, b->stream), "params");
@@ -229,8 +238,9 @@ int prepare(lbm2d_batch* b) {
 
 int launch_one(lbm2d_batch* b, int parity) {
     for (auto& g : b->groups) {
+        if (g.kind == KERNEL_ROWS) continue;  // solo members are launched by lbm2d_batch_step
         int e = launch_batch_step(g.storage, g.d_params[parity], g.d_block_start, (int)g.members.size(), g.nblocks,
-                                  g.thermal, b->bx, b->by, b->stream, g.pair);
+                                  g.thermal, b->bx, b->by, b->stream, g.kind == KERNEL_PAIR ? 1 : 0);
         ++b->launches;
         if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
         if (g.njobs > 0) {
@@ -267,7 +277,8 @@ int capture_pair(lbm2d_batch* b) {
 
 long long launches_per_step(const lbm2d_batch* b) {
     long long n = 0;
-    for (auto& g : b->groups) n += 1 + (g.njobs > 0 ? 1 : 0);
+    for (auto& g : b->groups)
+        if (g.kind != KERNEL_ROWS) n += 1 + (g.njobs > 0 ? 1 : 0);
     return n;
 }
 
@@ -368,16 +379,49 @@ int lbm2d_batch_step(lbm2d_batch* b, int nsteps) {
     int rc = prepare(b);
     if (rc) return rc;
     if (relayout) b->graph_valid = false;
-    const int pairs = nsteps / 2;
-    if (pairs > 0) {
-        if ((rc = capture_pair(b))) return rc;
-        for (int k = 0; k < pairs; ++k) {
-            BCK(cudaGraphLaunch(b->graph, b->stream), "graph launch");
-            b->launches += 2 * launches_per_step(b);
+    // solo members (the row pipeline fills the GPU for each of them): their
+    // steps are launched one after another on the batch stream; members are
+    // independent, so they need no ordering against the batched launches
+    for (auto& g : b->groups) {
+        if (g.kind != KERNEL_ROWS) continue;
+        for (size_t k = 0; k < g.members.size(); ++k) {
+            const Member& mem = b->members[g.members[k]];
+            lbm2d_solver* h = mem.h;
+            const long long taken = mem.budget >= 0 ? std::min<long long>(mem.budget, nsteps) : nsteps;
+            KParams p = g.host[k];
+            for (long long st = 0; st < taken; ++st) {
+                const int c = h->cur ^ (int)(st & 1);
+                p.fin = h->P[c];
+                p.fout = h->P[c ^ 1];
+                p.gin = h->G[c];
+                p.gout = h->G[c ^ 1];
+                p.seed_in = h->d_seed + c;
+                p.seed_out = h->d_seed + (c ^ 1);
+                p.skip_settled_solids = (h->steps_since_collide + st >= 2 && h->hook != 1) ? 1 : 0;
+                int e = launch_rows(h->storage, p, h->slot_grid, b->stream);
+                ++b->launches;
+                if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("solo step: ") + cudaGetErrorString((cudaError_t)e));
+                if (h->nslots > 0) {
+                    e = launch_force_reduce(h->d_partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last,
+                                            b->stream);
+                    ++b->launches;
+                    if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("solo reduce: ") + cudaGetErrorString((cudaError_t)e));
+                }
+            }
         }
     }
-    if (nsteps & 1) {
-        if ((rc = launch_one(b, 0))) return rc;
+    if (launches_per_step(b) > 0) {
+        const int pairs = nsteps / 2;
+        if (pairs > 0) {
+            if ((rc = capture_pair(b))) return rc;
+            for (int k = 0; k < pairs; ++k) {
+                BCK(cudaGraphLaunch(b->graph, b->stream), "graph launch");
+                b->launches += 2 * launches_per_step(b);
+            }
+        }
+        if (nsteps & 1) {
+            if ((rc = launch_one(b, 0))) return rc;
+        }
     }
     for (auto& m : b->members) {
         lbm2d_solver* h = m.h;

@@ -259,7 +259,9 @@ bool use_pair(const lbm2d_solver* h) {
 
 int kernel_kind(const lbm2d_solver* h) {
     if (!use_pair(h)) return KERNEL_SCALAR;
-    if (h->variant == 0 && !h->in_batch && rows_eligible(h->storage, h->nx, h->ny, h->thermal)) return KERNEL_ROWS;
+    if (h->variant == 0 && rows_eligible(h->storage, h->nx, h->ny, h->thermal) &&
+        (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
+        return KERNEL_ROWS;
     return KERNEL_PAIR;
 }
 

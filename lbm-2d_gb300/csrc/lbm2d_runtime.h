@@ -131,9 +131,13 @@ int check_handle(lbm2d_solver* h);
 // Two x-neighbours per thread (packed FP32x2 collision) when nx is even and
 // the step is non-thermal FP32/FP16/BF16.
 bool use_pair(const lbm2d_solver* h);
-// Step kernel of the next lbm2d_step: KERNEL_SCALAR, KERNEL_PAIR or
-// KERNEL_ROWS (the bulk-copy row pipeline; single solves only).
+// Step kernel of the next step: KERNEL_SCALAR, KERNEL_PAIR or KERNEL_ROWS
+// (the bulk-copy row pipeline).  Batch members run the batched scalar /
+// paired kernels, except members of at least kBatchSoloNodes nodes that
+// qualify for the row pipeline: those fill the GPU alone and get their own
+// row-pipeline launches inside the batch's step.
 enum KernelKind : int { KERNEL_SCALAR = 0, KERNEL_PAIR = 1, KERNEL_ROWS = 2 };
+constexpr long long kBatchSoloNodes = 1LL << 20;
 int kernel_kind(const lbm2d_solver* h);
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
 // kernel parameters of the next step (fin = current buffer); returns status.

@@ -144,3 +144,36 @@ def test_member_budgets(product, oracle_lib, storage):
     b.close()
     for s in mem:
         s.close()
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_large_member_runs_solo(product, oracle_lib, storage):
+    """A member of at least 2^20 nodes that qualifies for the row pipeline is
+    stepped with its own row-pipeline launches inside the batch call: it
+    reports that kernel, takes exactly its budget, and ends bit-for-bit where
+    the same solve stepped alone ends."""
+    import copy
+    big = copy.deepcopy(CS.CASES["ribs_les"])
+    big["nx"], big["ny"] = 1024, 1024
+    small = CS.CASES["cylinder_mei"]
+    b = product.Batch()
+    s_big = gpu_solver(product, oracle_lib, big, storage)
+    s_small = gpu_solver(product, oracle_lib, small, storage)
+    b.add(s_big, big["tau"], big["u"])
+    b.add(s_small, small["tau"], small["u"])
+    b.set_budget(s_big, 7)
+    assert s_big.info().kernel == product.KERNEL_ROWS
+    assert s_small.info().kernel != product.KERNEL_ROWS
+    b.step(10)
+    b.synchronize()
+    assert s_big.info().steps_done == 7 and s_small.info().steps_done == 10
+    alone = gpu_solver(product, oracle_lib, big, storage)
+    alone.step(big["tau"], big["u"], 7)
+    alone.synchronize()
+    assert np.array_equal(s_big.f, alone.f)
+    fx, fy = s_big.force_history()
+    ax, ay = alone.force_history()
+    assert len(fx) == 7 and np.array_equal(fx, ax) and np.array_equal(fy, ay)
+    for s in (s_big, s_small, alone):
+        s.close()
+    b.close()
