@@ -565,10 +565,12 @@ int lbm2d_batch_autotune(lbm2d_batch* b, int steps, int* best_bx, int* best_by) 
     if (steps < 1) steps = 1;
     cudaSetDevice(b->device);
     std::vector<unsigned long long> counters(b->members.size());
-    std::vector<long long> done(b->members.size());
+    std::vector<long long> done(b->members.size()), budgets(b->members.size());
     int rc;
     for (size_t k = 0; k < b->members.size(); ++k) {
         done[k] = b->members[k].h->steps_done;
+        budgets[k] = b->members[k].budget;
+        b->members[k].budget = -1;  // tuning steps are not the members' own
         if ((rc = save_state(b->members[k].h, counters[k]))) return bfail(b, rc, "autotune save");
     }
     cudaEvent_t e0, e1;
@@ -599,6 +601,7 @@ int lbm2d_batch_autotune(lbm2d_batch* b, int steps, int* best_bx, int* best_by) 
     for (size_t k = 0; k < b->members.size(); ++k) {
         const int r2 = restore_state(b->members[k].h, counters[k], done[k]);
         if (!rc && r2) rc = r2;
+        b->members[k].budget = budgets[k];
     }
     if (rc) return rc;
     if (best_bx) *best_bx = bbx;

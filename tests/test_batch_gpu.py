@@ -177,3 +177,47 @@ def test_large_member_runs_solo(product, oracle_lib, storage):
     for s in (s_big, s_small, alone):
         s.close()
     b.close()
+
+
+def test_batch_autotune_preserves_state_and_budgets(product, oracle_lib):
+    """Tuning the batch's block shape steps the members and undoes it: their
+    steps, budgets and states are as before, and stepping on reproduces an
+    untuned batch to FP32 rounding (the restored state is re-collided by the
+    prologue kernel, and the block shape groups the per-warp force
+    partials)."""
+    names = ["cylinder_mei", "step"]
+
+    def batch_of():
+        b = product.Batch()
+        mem = []
+        for n in names:
+            spec = CS.CASES[n]
+            s = make(product, oracle_lib, n, "fp32")
+            b.add(s, spec["tau"], spec["u"])
+            mem.append(s)
+        b.set_budget(mem[1], 9)
+        return b, mem
+
+    ref_b, ref = batch_of()
+    ref_b.step(3)
+    ref_b.step(10)
+    ref_b.synchronize()
+    b, mem = batch_of()
+    b.step(3)
+    b.synchronize()
+    before = [s.info().steps_done for s in mem]
+    b.autotune(steps=2)
+    assert [s.info().steps_done for s in mem] == before
+    assert b.budget(mem[0]) == -1 and b.budget(mem[1]) == 6
+    b.step(10)
+    b.synchronize()
+    for s, r in zip(mem, ref):
+        assert s.info().steps_done == r.info().steps_done
+        assert rel_l2(s.f, r.f) <= 1e-6
+        fx, fy = s.force_history()
+        rx, ry = r.force_history()
+        assert len(fx) == len(rx) and np.allclose(fx, rx, rtol=1e-6) and np.allclose(fy, ry, rtol=1e-6)
+    for x in mem + ref:
+        x.close()
+    b.close()
+    ref_b.close()
