@@ -198,10 +198,11 @@ int lbm2d_get_info(lbm2d_solver *h, lbm2d_info *info);
  * 32, at most 1024).  0,0 restores the tuned default. */
 int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
 /* Step-kernel variant.  0 (default): the fastest kernel the configuration
- * allows -- the row pipeline (nx a multiple of 8, non-thermal, FP32/FP16/BF16
- * storage, not a batch member), else two x-neighbours per thread with packed
- * FP32x2 arithmetic (nx even), else one node per thread.  1: one node per
- * thread.  2: two x-neighbours per thread where nx is even.  Same results to
+ * allows -- the row pipeline (non-thermal FP32 with nx a multiple of 4, or
+ * FP16/BF16 with nx a multiple of 8; in a batch only members of at least
+ * 2^20 nodes), else two x-neighbours per thread with packed FP32x2
+ * arithmetic (nx even), else one node per thread.  1: one node per thread.
+ * 2: two x-neighbours per thread where nx is even.  Same results to
  * rounding; lbm2d_get_info reports the kernel in use. */
 int lbm2d_set_kernel_variant(lbm2d_solver *h, int variant);
 /* The CUDA stream the handle launches on (cudaStream_t as void*). */

@@ -5,7 +5,8 @@
 // Blackwell bulk-copy engine fills ahead of the computation:
 //
 //   * work unit = a row tile: W = 512 consecutive nodes of one lattice row
-//     (nx a multiple of 8).  The 9 source rows of a tile (direction j reads
+//     (nx a multiple of 4 for FP32, 8 for FP16/BF16, so every row starts on
+//     a 16-byte boundary).  The 9 source rows of a tile (direction j reads
 //     row y - cy_j, x range [x0 - PAD, x0 + W + PAD)) and the tile's flags
 //     are brought in by 10 cp.async.bulk copies (plus 16-byte copies for the
 //     periodic x wrap at the row ends), completing on an mbarrier;
@@ -461,8 +462,11 @@ int launch_rows_t(const KParams& p, int grid, cudaStream_t s) {
 
 }  // namespace
 
+// Every staged row must start on a 16-byte boundary: nx a multiple of 4
+// (FP32) or 8 (FP16/BF16).
 bool rows_eligible(int storage, int nx, int ny, bool thermal) {
-    return !thermal && (storage == ST_FP32 || storage == ST_FP16 || storage == ST_BF16) && nx % 8 == 0 && nx >= 16 &&
+    const int q = storage == ST_FP32 ? 4 : 8;
+    return !thermal && (storage == ST_FP32 || storage == ST_FP16 || storage == ST_BF16) && nx % q == 0 && nx >= 16 &&
            ny >= 2;
 }
 

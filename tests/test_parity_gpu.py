@@ -49,7 +49,7 @@ def run(product, O, spec, storage, variant=0):
 @pytest.mark.parametrize("name", sorted(CS.CASES))
 def test_gpu_matches_reference(product, oracle_lib, name, storage, variant):
     """variant 0: the fastest kernel for the case (row pipeline where nx is a
-    multiple of 8, else paired nodes); 1: one node per thread; 2: paired
+    multiple of 4 (FP32), else paired nodes); 1: one node per thread; 2: paired
     nodes per thread (packed FP32x2) where nx is even."""
     spec = CS.CASES[name]
     gold = np.load(os.path.join(GOLD, f"{name}.npz"))

@@ -20,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 WIDE = {
     "ribs_les_1032": ("ribs_les", 1032, 24, 12),
+    "ribs_les_1028": ("ribs_les", 1028, 24, 12),  # FP32 only: nx % 8 == 4
     "ribs_les_520": ("ribs_les", 520, 20, 12),
     "step_1024": ("step", 1024, 30, 12),
     "cylinder_mei_1544": ("cylinder_mei", 1544, 40, 10),
@@ -101,7 +102,10 @@ def test_kernel_selection(product):
     s.set_kernel_variant(1)
     assert s.info().kernel == product.KERNEL_SCALAR
     s.close()
-    for nx, storage in ((1036, "fp32"), (1032, "fp64")):
+    for nx, storage in ((1034, "fp32"), (1036, "fp16"), (1032, "fp64")):
         s = product.Solver(nx, 8, product.RIBS, storage=storage)
-        assert s.info().kernel != product.KERNEL_ROWS
+        assert s.info().kernel != product.KERNEL_ROWS, (nx, storage)
         s.close()
+    s = product.Solver(1036, 8, product.RIBS, storage="fp32")  # 16-byte rows in FP32
+    assert s.info().kernel == product.KERNEL_ROWS
+    s.close()
