@@ -487,6 +487,7 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
     if (!rc) rc = dalloc(h, &h->d_seed, 16);
     if (!rc) rc = dalloc(h, &h->d_counter, 16);
     if (!rc) rc = dalloc(h, &h->d_last, 16);
+    if (!rc && cudaMallocHost(&h->h_last, 2 * sizeof(double)) != cudaSuccess) rc = LBM2D_ERR_CUDA;
     if (!rc) rc = dalloc(h, &h->d_hist, (size_t)h->hist_cap * 2 * sizeof(double));
     if (!rc) rc = ensure_stage(h, false);
     if (!rc) rc = ensure_populations(h);
@@ -518,6 +519,7 @@ int lbm2d_destroy(lbm2d_solver* h) {
         if (b) cudaFreeAsync(b, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
+    if (h->h_last) cudaFreeHost(h->h_last);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LBM2D_OK;
@@ -740,11 +742,11 @@ int lbm2d_synchronize(lbm2d_solver* h) {
 int lbm2d_force_sums(lbm2d_solver* h, double* fx, double* fy) {
     int rc;
     if ((rc = check_handle(h))) return rc;
-    double v[2] = {0.0, 0.0};
-    CK(cudaMemcpyAsync(v, h->d_last, sizeof(v), cudaMemcpyDeviceToHost, h->stream), "force D2H");
+    // into pinned memory: a direct copy, no staging through a bounce buffer
+    CK(cudaMemcpyAsync(h->h_last, h->d_last, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "force D2H");
     CK(cudaStreamSynchronize(h->stream), "force sync");
-    if (fx) *fx = v[0];
-    if (fy) *fy = v[1];
+    if (fx) *fx = h->h_last[0];
+    if (fy) *fy = h->h_last[1];
     return LBM2D_OK;
 }
 

@@ -882,7 +882,9 @@ __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla,
                 csq = cd * cd;
             }
             const F2 a = mpxx - pxx_eq, b = mpxy - pxy_eq;
-            const F2 Q = sqrt2(sp2(2.0f) * fma2(a, a, b * b));  // Q * S
+            // Q * S; the 1e-30 (far below any nonzero 2|Pi_neq|^2 in FP32)
+            // keeps the argument positive, so no zero guard is needed
+            const F2 Q = sqrt2_pos(fma2(sp2(2.0f), fma2(a, a, b * b), sp2(1e-30f)));
             const F2 A = sp2(4.5f) * csq * Q * k;
             const F2 te2 = sp2(q.tau) + sqrt2_pos(fma2(sp2(q.tau), sp2(q.tau), sp2(4.0f) * A));
             const F2 s2 = sp2(2.0f) * rcp2(te2);

@@ -77,6 +77,7 @@ struct lbm2d_solver {
     int hist_cap = 1 << 18;
     unsigned long long* d_counter = nullptr;
     double* d_last = nullptr;
+    double* h_last = nullptr;  // pinned host copy of the last (Fx, Fy)
     unsigned int* d_nan = nullptr;
     uint32_t* d_seed = nullptr;  // rounding-noise seed words, one per population buffer
     double* d_stage_f = nullptr;
