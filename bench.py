@@ -504,6 +504,42 @@ def run_batch(args):
     return 0
 
 
+def run_frame(args):
+    """Frame export on the channel workload: the JSON frame's fields
+    (downsampled by NX/100, as the reference's writer does) and the VTK
+    writer's full-resolution fields computed on the device, against what the
+    mirror-based writer needs first: the full FP64 state on the host."""
+    import lbm2d
+    lbm2d.build(quiet=True)
+    nx, ny = args.nx, args.ny
+    mask, circles = make_geometry(nx, ny)
+    s = configure(lbm2d, "fp32", mask, circles, 0, nx, ny, True)
+    s.init_equilibrium(1.0, U0, 0.0)
+    s.step(TAU, U0, 100)
+    s.synchronize()
+    ds = max(1, nx // 100)
+
+    def med(fn, reps):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3
+
+    frame_ms = med(lambda: s.frame_fields(ds), 20)
+    vtk_ms = med(lambda: s.frame_fields(1, sanitize=False), 5)
+    host_ms = med(lambda: s.f, 3)
+    line = {"metric": "frame export: device fields vs host-mirror download", "unit": "ms",
+            "json_frame_device_ms": frame_ms, "vtk_fields_device_ms": vtk_ms, "state_download_ms": host_ms,
+            "json_frame_speedup": host_ms / frame_ms, "frame_points": ((nx + ds - 1) // ds) * ((ny + ds - 1) // ds),
+            "config": {"workload": workload_name(nx, ny), "storage": "fp32", "ds": ds}}
+    s.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_precision(args):
     """Error of FP32 / FP16 / BF16 storage against an FP64 run of the same
     kernel on the channel workload: relative L2 of the velocity field over
@@ -555,7 +591,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (default: --steps)")
-    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "precision"])
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "precision", "frame"])
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--batch-storage", default="fp32")
     ap.add_argument("--autotune", action="store_true")
@@ -577,6 +613,8 @@ def main():
         return run_serve(args)
     if args.mode == "precision":
         return run_precision(args)
+    if args.mode == "frame":
+        return run_frame(args)
 
     import torch
 

@@ -182,6 +182,25 @@ int lbm2d_download_force_field(lbm2d_solver *h, double *fx_body, double *fy_body
 int lbm2d_download_macros(lbm2d_solver *h, double *rho, double *u, double *v, double *T);
 int lbm2d_download_wall_dist(lbm2d_solver *h, double *wall_dist);
 
+/* Fields of the reference's frame writers, computed on the device from the
+ * state of the last step: save_json_frame (src/lbm.hpp:588-701),
+ * save_json_frame_thermal (:707-817) and save_vtk_frame (:860-926).  Point
+ * (i, j) of the nxd x nyd output grid, nxd = ceil(nx / ds), nyd =
+ * ceil(ny / ds), is node (i*ds, j*ds); outputs are row-major, nxd wide.
+ * rho, u, v follow compute_macros in the reference's FP64 operation order,
+ * vel = sqrt(u*u + v*v), omega is the writers' downsampled central
+ * difference dv/dx - du/dy (one-sided at the grid edges), T the sum of g
+ * (zero without the thermal DDF).  obstacle is 1 at solid points, where
+ * rho, u, v, vel and omega are 0 and T is T_wall.  sanitize = 1 applies the
+ * JSON writers' replacements (rho < 1e-12 or NaN -> rho 1, u = v = 0; NaN
+ * u, v, vel -> 0; NaN T -> 1); sanitize = 0 reports raw values, as the VTK
+ * writer prints them.  Only nxd*nyd values per field cross to the host.  Any
+ * output may be NULL.  Errors: LBM2D_ERR_INVALID for ds < 1,
+ * LBM2D_ERR_STATE before the first step after an upload.  Not in the
+ * reference (its writers loop over the host state). */
+int lbm2d_frame_fields(lbm2d_solver *h, int ds, int sanitize, double T_wall, double *rho, double *u, double *v,
+                       double *vel, double *omega, double *T, uint8_t *obstacle);
+
 /* FP64 reductions over the fluid nodes of the current state: total mass
  * (the quantity of the reference's conservation test, src/lbm_test.cpp:
  * 173-198), x/y momentum, and the steady-state residual

@@ -884,6 +884,54 @@ int lbm2d_download_macros(lbm2d_solver* h, double* rho, double* u, double* v, do
     return ret;
 }
 
+int lbm2d_frame_fields(lbm2d_solver* h, int ds, int sanitize, double T_wall, double* rho, double* u, double* v,
+                       double* vel, double* omega, double* T, uint8_t* obstacle) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (ds < 1) return fail(h, LBM2D_ERR_INVALID, "frame downsampling factor must be >= 1");
+    if (h->staged || h->steps_since_collide == 0) return fail(h, LBM2D_ERR_STATE, "no step since the last upload");
+    const int nxd = (h->nx + ds - 1) / ds, nyd = (h->ny + ds - 1) / ds;
+    const size_t nd = (size_t)nxd * nyd;
+    // one scratch block: six FP64 fields, then the obstacle bytes
+    char* buf = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&buf), nd * (6 * sizeof(double) + 1), h->stream) != cudaSuccess)
+        return fail(h, LBM2D_ERR_OOM, "frame buffer");
+    double* d = reinterpret_cast<double*>(buf);
+    FOut o;
+    o.rho = d;
+    o.u = d + nd;
+    o.v = d + 2 * nd;
+    o.vel = d + 3 * nd;
+    o.omega = d + 4 * nd;
+    o.T = d + 5 * nd;
+    o.obstacle = reinterpret_cast<uint8_t*>(d + 6 * nd);
+    o.T_wall = T_wall;
+    o.ds = ds;
+    o.nxd = nxd;
+    o.nyd = nyd;
+    o.sanitize = sanitize ? 1 : 0;
+    KParams p = rebuild_params(h);
+    const int e = launch_frame(h->storage, p, o, h->stream);
+    h->launches += 2;
+    int ret = e ? cuda_fail(h, (cudaError_t)e, "frame fields") : LBM2D_OK;
+    const double* srcs[6] = {o.rho, o.u, o.v, o.vel, o.omega, o.T};
+    double* outs[6] = {rho, u, v, vel, omega, T};
+    for (int k = 0; k < 6 && !ret; ++k)
+        if (outs[k]) {
+            const cudaError_t ce =
+                cudaMemcpyAsync(outs[k], srcs[k], nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+            if (ce != cudaSuccess) ret = cuda_fail(h, ce, "D2H frame");
+        }
+    if (!ret && obstacle) {
+        const cudaError_t ce = cudaMemcpyAsync(obstacle, o.obstacle, nd, cudaMemcpyDeviceToHost, h->stream);
+        if (ce != cudaSuccess) ret = cuda_fail(h, ce, "D2H frame obstacle");
+    }
+    cudaFreeAsync(buf, h->stream);
+    const cudaError_t se = cudaStreamSynchronize(h->stream);
+    if (!ret && se != cudaSuccess) ret = cuda_fail(h, se, "frame fields");
+    return ret;
+}
+
 int lbm2d_diagnostics(lbm2d_solver* h, double* mass, double* mom_x, double* mom_y, double* residual) {
     int rc;
     if ((rc = check_handle(h))) return rc;

@@ -111,6 +111,17 @@ struct ROut {
     double *fx, *fy;
 };
 
+// Downsampled frame fields: the point (i, j) of an nxd x nyd grid is node
+// (i*ds, j*ds); arrays are row-major, nxd wide.  All pointers are device
+// arrays of nxd*nyd entries and must be set.
+struct FOut {
+    double *rho, *u, *v, *vel, *omega, *T;
+    uint8_t* obstacle;
+    double T_wall;  // temperature reported at solid points
+    int ds, nxd, nyd;
+    int sanitize;  // 1: the JSON writers' NaN / zero-density replacements
+};
+
 // One instance's second-stage force reduction in a batched launch.
 struct ReduceJob {
     const double* partials;
@@ -124,6 +135,9 @@ struct ReduceJob {
 // Launchers (lbm2d_kernels.cu).  All return a cudaError_t as int.
 int launch_step(int storage, const KParams& p, int bx, int by, void* stream);
 int launch_readback(int storage, const KParams& p, const ROut& o, void* stream);
+// Frame fields of the post-stream state (two launches: point fields, then
+// the vorticity stencil over them).
+int launch_frame(int storage, const KParams& p, const FOut& o, void* stream);
 // Collide an FP64 AoS state S (device) into the stored post-collision state.
 int launch_prologue(int storage, const KParams& p, const double* f_aos, const double* g_aos, void* stream);
 // Step several instances at once: inst[] holds one KParams per instance and

@@ -247,6 +247,84 @@ __global__ void readback_kernel(const KParams p, const ROut o) {
     }
 }
 
+// Fields of the reference's frame writers at one downsampled point
+// (src/lbm.hpp:609-630 and :728-754 for JSON frames, :860-910 for VTK):
+// compute_macros in the reference's order (sequential sums in slot order,
+// u = mx / rho; src/lbm_types.hpp:278-288), the temperature as the plain sum
+// of g (src/thermal.hpp:55-60) and the speed sqrt(u*u + v*v).  Every
+// operation is an explicitly rounded FP64 operation, so nothing is fused and
+// the results equal the host writers' on the same state.  With `sanitize`
+// the JSON writers' replacements apply: rho < 1e-12 or NaN -> (1, 0, 0),
+// NaN u, v, speed -> 0, NaN T -> 1.  Solid points report zeros (T = T_wall).
+template <class T, bool TH>
+__global__ void frame_kernel(const KParams p, const FOut o) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= o.nxd || j >= o.nyd) return;
+    const int x = i * o.ds, y = j * o.ds;
+    const size_t n = (size_t)y * p.nx + x;
+    const size_t k = (size_t)j * o.nxd + i;
+    const uint32_t fl = p.flags[n];
+    const bool solid = (fl & FLAG_SOLID) != 0;
+    double rho = 0.0, u = 0.0, v = 0.0, vel = 0.0, Tn = o.T_wall;
+    if (!solid) {
+        double f[9], g[9];
+        state_fp64<T, TH>(p, x, y, fl, f, g);
+        double mx = 0.0, my = 0.0;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            rho = __dadd_rn(rho, f[q]);
+            mx = __dadd_rn(mx, __dmul_rn(f[q], double(CXf(q))));
+            my = __dadd_rn(my, __dmul_rn(f[q], double(CYf(q))));
+        }
+        u = __ddiv_rn(mx, rho);
+        v = __ddiv_rn(my, rho);
+        Tn = 0.0;
+        if (TH) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Tn = __dadd_rn(Tn, g[q]);
+        }
+        if (o.sanitize) {
+            if (rho < 1e-12 || isnan(rho)) {
+                rho = 1.0;
+                u = 0.0;
+                v = 0.0;
+            }
+            if (isnan(u)) u = 0.0;
+            if (isnan(v)) v = 0.0;
+            if (TH && isnan(Tn)) Tn = 1.0;
+        }
+        vel = __dsqrt_rn(__dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v)));
+        if (o.sanitize && isnan(vel)) vel = 0.0;
+    }
+    o.rho[k] = rho;
+    o.u[k] = u;
+    o.v[k] = v;
+    o.vel[k] = vel;
+    o.T[k] = Tn;
+    o.obstacle[k] = solid ? 1 : 0;
+}
+
+// Vorticity dv/dx - du/dy on the downsampled grid with one-sided
+// differences at its edges (src/lbm.hpp:632-653); zero at solid points.
+__global__ void frame_omega_kernel(const FOut o) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= o.nxd || j >= o.nyd) return;
+    const int k = j * o.nxd + i;
+    double om = 0.0;
+    if (!o.obstacle[k]) {
+        const int il = max(0, i - 1), ir = min(o.nxd - 1, i + 1);
+        const int jd = max(0, j - 1), ju = min(o.nyd - 1, j + 1);
+        const double dvdx = __ddiv_rn(__dsub_rn(o.v[j * o.nxd + ir], o.v[j * o.nxd + il]),
+                                      __dmul_rn(2.0, double((ir - il) * o.ds)));
+        const double dudy = __ddiv_rn(__dsub_rn(o.u[ju * o.nxd + i], o.u[jd * o.nxd + i]),
+                                      __dmul_rn(2.0, double((ju - jd) * o.ds)));
+        om = __dsub_rn(dvdx, dudy);
+    }
+    o.omega[k] = om;
+}
+
 template <class T, bool TH>
 __global__ void prologue_kernel(const KParams p, const double* __restrict__ fa, const double* __restrict__ ga) {
     using R = typename Pop<T>::R;
@@ -468,6 +546,17 @@ int launch_readback_t(const KParams& p, const ROut& o, cudaStream_t s) {
 }
 
 template <class T>
+int launch_frame_t(const KParams& p, const FOut& o, cudaStream_t s) {
+    dim3 blk(64, 4), grd((o.nxd + 63) / 64, (o.nyd + 3) / 4);
+    if (p.thermal)
+        frame_kernel<T, true><<<grd, blk, 0, s>>>(p, o);
+    else
+        frame_kernel<T, false><<<grd, blk, 0, s>>>(p, o);
+    frame_omega_kernel<<<grd, blk, 0, s>>>(o);
+    return (int)cudaGetLastError();
+}
+
+template <class T>
 int launch_prologue_t(const KParams& p, const double* fa, const double* ga, cudaStream_t s) {
     if (p.pair) {
         if constexpr (!std::is_same<T, double>::value) {
@@ -505,6 +594,17 @@ int launch_readback(int storage, const KParams& p, const ROut& o, void* stream) 
         case ST_FP16: return launch_readback_t<__half>(p, o, s);
         case ST_BF16: return launch_readback_t<__nv_bfloat16>(p, o, s);
         case ST_FP64: return launch_readback_t<double>(p, o, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_frame(int storage, const KParams& p, const FOut& o, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_frame_t<float>(p, o, s);
+        case ST_FP16: return launch_frame_t<__half>(p, o, s);
+        case ST_BF16: return launch_frame_t<__nv_bfloat16>(p, o, s);
+        case ST_FP64: return launch_frame_t<double>(p, o, s);
     }
     return (int)cudaErrorInvalidValue;
 }

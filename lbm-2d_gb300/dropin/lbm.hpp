@@ -195,19 +195,12 @@ inline void place_polygon(LBMCapabilities& sys, const std::vector<std::pair<doub
 
 // ---------------------------------------------------------------- output writers (host)
 namespace lbm2d_dropin {
-// Downsampled macroscopic fields + vorticity, the frame format of
-// src/lbm.hpp:588-701 (and :707-817 with a temperature channel).
-inline void write_frame(const LBMCapabilities& sys, int step, const std::string& output_dir, bool thermal,
-                        double T_wall) {
-    const int ds = std::max(1, NX / 100);
-    const int nxd = (NX + ds - 1) / ds, nyd = (NY + ds - 1) / ds, nd = nxd * nyd;
-    const std::string dir = output_dir + "/frames";
-    std::filesystem::create_directories(dir);
-    std::ofstream out(dir + "/frame_" + std::to_string(step) + ".json");
-    out.precision(6);
-    out << std::fixed;
-    std::vector<double> vel(nd, 0.0), ua(nd, 0.0), va(nd, 0.0), ra(nd, 0.0), om(nd, 0.0), ta(nd, 0.0);
-    std::vector<int> ob(nd, 0);
+// The frame fields from the host mirrors (used when the host has changed
+// the state since the last step).
+inline void host_frame_fields(const LBMCapabilities& sys, int ds, int nxd, int nyd, bool thermal, double T_wall,
+                              std::vector<double>& vel, std::vector<double>& ua, std::vector<double>& va,
+                              std::vector<double>& ra, std::vector<double>& om, std::vector<double>& ta,
+                              std::vector<int>& ob) {
     const double* f = sys.f.data();
     const double* g = thermal ? sys.g_thermal.data() : nullptr;
     int k = 0;
@@ -250,6 +243,32 @@ inline void write_frame(const LBMCapabilities& sys, int step, const std::string&
             const double dudy = (ua[ju * nxd + i] - ua[jd * nxd + i]) / (2.0 * static_cast<double>((ju - jd) * ds));
             om[idx] = dvdx - dudy;
         }
+}
+
+// Downsampled macroscopic fields + vorticity, the frame format of
+// src/lbm.hpp:588-701 (and :707-817 with a temperature channel).
+inline void write_frame(const LBMCapabilities& sys, int step, const std::string& output_dir, bool thermal,
+                        double T_wall) {
+    const int ds = std::max(1, NX / 100);
+    const int nxd = (NX + ds - 1) / ds, nyd = (NY + ds - 1) / ds, nd = nxd * nyd;
+    const std::string dir = output_dir + "/frames";
+    std::filesystem::create_directories(dir);
+    std::ofstream out(dir + "/frame_" + std::to_string(step) + ".json");
+    out.precision(6);
+    out << std::fixed;
+    std::vector<double> vel(nd, 0.0), ua(nd, 0.0), va(nd, 0.0), ra(nd, 0.0), om(nd, 0.0), ta(nd, 0.0);
+    std::vector<int> ob(nd, 0);
+    if (sys.device_state_current(thermal)) {
+        // the same fields computed on the device; only the nd points cross
+        std::vector<uint8_t> ob8(nd);
+        lbm2d_solver* h = sys.device_handle();
+        check(lbm2d_frame_fields(h, ds, 1, T_wall, ra.data(), ua.data(), va.data(), vel.data(), om.data(),
+                                 thermal ? ta.data() : nullptr, ob8.data()),
+              h, "frame fields");
+        for (int i = 0; i < nd; ++i) ob[i] = ob8[i];
+    } else {
+        host_frame_fields(sys, ds, nxd, nyd, thermal, T_wall, vel, ua, va, ra, om, ta, ob);
+    }
     auto arr = [&](const char* name, auto&& get, bool first) {
         out << (first ? "" : "],") << "\"" << name << "\":[";
         for (int i = 0; i < nd; ++i) {
@@ -336,42 +355,47 @@ inline void save_vtk_frame(const LBMCapabilities& sys, int frame, const std::str
     out << "DIMENSIONS " << NX << " " << NY << " 1\n";
     out << "ORIGIN 0 0 0\nSPACING 1 1 1\n";
     out << "POINT_DATA " << NX * NY << "\n";
-    const double* f = sys.f.data();
-    auto macros_at = [&](int idx, double& rho, double& u, double& v) {
-        compute_macros(f + static_cast<size_t>(idx) * 9, rho, u, v);
-    };
-    out << "SCALARS VelocityMagnitude double 1\nLOOKUP_TABLE default\n";
-    for (int idx = 0; idx < NX * NY; ++idx) {
-        if (sys.obstacle[idx]) {
-            out << "0.0\n";
-            continue;
+    const size_t n = static_cast<size_t>(NX) * NY;
+    std::vector<double> sp(n), ua(n), va(n), ra(n);
+    std::vector<uint8_t> ob(n);
+    if (sys.device_state_current(false)) {
+        // full-resolution raw fields from the device (no NaN replacement)
+        lbm2d_solver* h = sys.device_handle();
+        lbm2d_dropin::check(lbm2d_frame_fields(h, 1, 0, 0.0, ra.data(), ua.data(), va.data(), sp.data(), nullptr,
+                                               nullptr, ob.data()),
+                            h, "frame fields");
+    } else {
+        const double* f = sys.f.data();
+        for (size_t idx = 0; idx < n; ++idx) {
+            ob[idx] = sys.obstacle[idx] ? 1 : 0;
+            if (ob[idx]) continue;
+            compute_macros(f + idx * 9, ra[idx], ua[idx], va[idx]);
+            sp[idx] = std::sqrt(ua[idx] * ua[idx] + va[idx] * va[idx]);
         }
-        double rho, u, v;
-        macros_at(idx, rho, u, v);
-        out << std::sqrt(u * u + v * v) << "\n";
+    }
+    out << "SCALARS VelocityMagnitude double 1\nLOOKUP_TABLE default\n";
+    for (size_t idx = 0; idx < n; ++idx) {
+        if (ob[idx])
+            out << "0.0\n";
+        else
+            out << sp[idx] << "\n";
     }
     out << "VECTORS Velocity double\n";
-    for (int idx = 0; idx < NX * NY; ++idx) {
-        if (sys.obstacle[idx]) {
+    for (size_t idx = 0; idx < n; ++idx) {
+        if (ob[idx])
             out << "0 0 0\n";
-            continue;
-        }
-        double rho, u, v;
-        macros_at(idx, rho, u, v);
-        out << u << " " << v << " 0\n";
+        else
+            out << ua[idx] << " " << va[idx] << " 0\n";
     }
     out << "SCALARS Density double 1\nLOOKUP_TABLE default\n";
-    for (int idx = 0; idx < NX * NY; ++idx) {
-        if (sys.obstacle[idx]) {
+    for (size_t idx = 0; idx < n; ++idx) {
+        if (ob[idx])
             out << "0.0\n";
-            continue;
-        }
-        double rho, u, v;
-        macros_at(idx, rho, u, v);
-        out << rho << "\n";
+        else
+            out << ra[idx] << "\n";
     }
     out << "SCALARS DragForce double 1\nLOOKUP_TABLE default\n";
-    for (int idx = 0; idx < NX * NY; ++idx) {
+    for (size_t idx = 0; idx < n; ++idx) {
         const double fx = sys.fx_body[idx], fy = sys.fy_body[idx];
         if (fx != 0.0 || fy != 0.0)
             out << fx << "\n";

@@ -310,6 +310,14 @@ struct LBMCapabilities {
     // One execute_time_step on the device (called by lbm.hpp).
     void device_step(double tau, double u_inflow);
     lbm2d_solver* handle() { return h_; }
+    // True when the device holds the newest state and the host has changed
+    // none of the mirrors the frame writers read since the last step, so the
+    // writers can take their fields from the device (lbm2d_frame_fields).
+    bool device_state_current(bool thermal) const {
+        return h_ && step_version_ > 0 && f.stale() && !obstacle.dirty() &&
+               (!thermal || (use_thermal && g_thermal.stale()));
+    }
+    lbm2d_solver* device_handle() const { return h_; }
 
    private:
     void ensure_handle();

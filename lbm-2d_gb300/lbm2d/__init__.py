@@ -112,6 +112,7 @@ _SIGS = {
     "lbm2d_download_force_field": ([_P, _DP, _DP], _I),
     "lbm2d_download_macros": ([_P, _DP, _DP, _DP, _DP], _I),
     "lbm2d_download_wall_dist": ([_P, _DP], _I),
+    "lbm2d_frame_fields": ([_P, _I, _I, _D, _DP, _DP, _DP, _DP, _DP, _DP, _U8P], _I),
     "lbm2d_diagnostics": ([_P, _DP, _DP, _DP, _DP], _I),
     "lbm2d_synchronize": ([_P], _I),
     "lbm2d_get_info": ([_P, C.POINTER(Info)], _I),
@@ -458,6 +459,22 @@ class Solver:
         T = np.empty(n) if thermal else None
         self._ck(self.L.lbm2d_download_macros(self.h, _d(rho), _d(u), _d(v), _d(T) if thermal else None))
         return (rho, u, v, T) if thermal else (rho, u, v)
+
+    def frame_fields(self, ds, sanitize=True, T_wall=0.0):
+        """Fields of the reference's frame writers at nodes (i*ds, j*ds),
+        computed on the device: dict of (nyd, nxd) arrays rho, u, v, vel,
+        omega, T (float64) and obstacle (uint8).  sanitize=True applies the
+        JSON writers' NaN / zero-density replacements, False gives the raw
+        values the VTK writer prints."""
+        d = max(int(ds), 1)  # the library rejects ds < 1
+        nxd, nyd = (self.nx + d - 1) // d, (self.ny + d - 1) // d
+        out = {k: np.empty(nxd * nyd) for k in ("rho", "u", "v", "vel", "omega", "T")}
+        ob = np.empty(nxd * nyd, np.uint8)
+        self._ck(self.L.lbm2d_frame_fields(self.h, int(ds), 1 if sanitize else 0, float(T_wall),
+                                           *(_d(out[k]) for k in ("rho", "u", "v", "vel", "omega", "T")),
+                                           _u8(ob)))
+        out["obstacle"] = ob
+        return {k: a.reshape(nyd, nxd) for k, a in out.items()}
 
     def diagnostics(self):
         """(mass, momentum x, momentum y, residual) in FP64 over fluid nodes."""

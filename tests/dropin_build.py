@@ -9,8 +9,9 @@ SHIM = os.path.join(ROOT, "tests", "dropin")
 LIBDIR = os.path.join(ROOT, "lbm-2d_gb300", "lib")
 
 
-def compile_dropin(src: str, out: str, extra_after: str | None = None) -> subprocess.CompletedProcess:
-    cmd = ["g++", "-std=c++20", "-O2", "-fopenmp", f"-I{SHIM}", f"-I{DROPIN}", f"-I{INCLUDE}"]
+def compile_dropin(src: str, out: str, extra_after: str | None = None,
+                   flags: tuple = ()) -> subprocess.CompletedProcess:
+    cmd = ["g++", "-std=c++20", "-O2", "-fopenmp", *flags, f"-I{SHIM}", f"-I{DROPIN}", f"-I{INCLUDE}"]
     if extra_after:
         cmd += ["-idirafter", extra_after]
     cmd += [src, f"-L{LIBDIR}", "-llbm2d", f"-Wl,-rpath,{LIBDIR}", "-o", out]
