@@ -63,6 +63,10 @@ typedef struct {
     int has_moving_wall;
     double omega, rot_cx, rot_cy;
     int use_mei_bb;
+    /* immersed boundary (src/ibm.hpp:27-38), driven as src/airfoil_ibm.cpp */
+    int ibm_n;
+    double *ibm_X, *ibm_Y, *ibm_U, *ibm_V, *ibm_FX, *ibm_FY;
+    double ibm_dt, ibm_uwx, ibm_uwy;
 } or_state;
 
 static inline int nidx(const or_state *s, int x, int y) { return y * s->nx + x; }
@@ -353,7 +357,9 @@ or_state *or_create(int nx, int ny) {
 void or_destroy(or_state *s) {
     if (!s) return;
     free(s->f); free(s->f_next); free(s->g); free(s->g_next); free(s->wall_dist);
-    free(s->fx); free(s->fy); free(s->obstacle); free(s->poly); free(s);
+    free(s->fx); free(s->fy); free(s->obstacle); free(s->poly);
+    free(s->ibm_X); free(s->ibm_Y); free(s->ibm_U); free(s->ibm_V); free(s->ibm_FX); free(s->ibm_FY);
+    free(s);
 }
 
 void or_set_case(or_state *s, int case_type, int collision, int use_les, double cs) {
@@ -860,4 +866,136 @@ void or_init_thermal_uniform(or_state *s, double T, double u, double v) {
     size_t nn = (size_t)s->nx * s->ny;
     for (size_t k = 0; k < nn; ++k)
         for (int i = 0; i < 9; ++i) s->g[k * 9 + i] = or_thermal_equilibrium(i, T, u, v);
+}
+
+/* ---------------------------------------------------------------- immersed boundary */
+
+/* ibm_delta, src/ibm.hpp:16-19 (4-point cosine delta) */
+double or_ibm_delta(double r) {
+    if (fabs(r) >= 2.0) return 0.0;
+    return 0.25 * (1.0 + cos(0.5 * M_PI * r));
+}
+
+/* ibm_kernel, src/ibm.hpp:22-24 */
+double or_ibm_kernel(double dx, double dy) { return or_ibm_delta(dx) * or_ibm_delta(dy); }
+
+/* ImmersedBoundary::build_from_polygon, src/ibm.hpp:42-69: points spaced
+ * uniformly in the polygon's vertex parameter.  Writes at most cap points;
+ * returns the point count. */
+int or_ibm_points_from_polygon(const double *xy, int n, double spacing, double *X, double *Y, int cap) {
+    if (n < 3) return 0;
+    double total_len = 0.0;
+    for (int i = 0; i < n; ++i) {
+        int j = (i + 1) % n;
+        double dx = xy[2 * j] - xy[2 * i];
+        double dy = xy[2 * j + 1] - xy[2 * i + 1];
+        total_len += sqrt(dx * dx + dy * dy);
+    }
+    int n_points = (int)(total_len / spacing);
+    if (n_points < 8) n_points = 8;
+    for (int k = 0; k < n_points && k < cap; ++k) {
+        double t = (double)k / n_points;
+        double seg = t * n;
+        int i = (int)seg % n;
+        int j = (i + 1) % n;
+        double f = seg - floor(seg);
+        X[k] = xy[2 * i] + f * (xy[2 * j] - xy[2 * i]);
+        Y[k] = xy[2 * i + 1] + f * (xy[2 * j + 1] - xy[2 * i + 1]);
+    }
+    return n_points;
+}
+
+/* Install the Lagrangian points; the no-slip target velocity is (uwx, uwy)
+ * (src/ibm.hpp:139-149).  n = 0 removes the boundary. */
+void or_ibm_set(or_state *s, const double *X, const double *Y, int n, double dt, double uwx, double uwy) {
+    free(s->ibm_X); free(s->ibm_Y); free(s->ibm_U); free(s->ibm_V); free(s->ibm_FX); free(s->ibm_FY);
+    s->ibm_X = s->ibm_Y = s->ibm_U = s->ibm_V = s->ibm_FX = s->ibm_FY = NULL;
+    s->ibm_n = n;
+    s->ibm_dt = dt; s->ibm_uwx = uwx; s->ibm_uwy = uwy;
+    if (n <= 0) return;
+    s->ibm_X = malloc(n * sizeof(double)); s->ibm_Y = malloc(n * sizeof(double));
+    s->ibm_U = calloc(n, sizeof(double)); s->ibm_V = calloc(n, sizeof(double));
+    s->ibm_FX = calloc(n, sizeof(double)); s->ibm_FY = calloc(n, sizeof(double));
+    memcpy(s->ibm_X, X, n * sizeof(double));
+    memcpy(s->ibm_Y, Y, n * sizeof(double));
+}
+
+/* One iteration of the airfoil driver loop, src/airfoil_ibm.cpp:121-176:
+ * 1. velocity at each Lagrangian point from the fluid nodes of its 5x5
+ *    stencil (:124-147); 2. no-slip force (U_wall - U)/dt (src/ibm.hpp:
+ *    139-149); 3. spread to the grid in point order (src/ibm.hpp:72-103);
+ * 4. the time step; 5. explicit forcing of every fluid node,
+ *    f_i += w_i (3 c_i.F + 9 (c_i.0)(c_i.F)) (:158-176). */
+void or_ibm_step(or_state *s, double tau, double u_in) {
+    const int nx = s->nx, ny = s->ny, np = s->ibm_n;
+    size_t N = (size_t)nx * ny;
+    for (int p = 0; p < np; ++p) {
+        double X = s->ibm_X[p], Y = s->ibm_Y[p];
+        double u = 0, v = 0;
+        int x0 = (int)floor(X) - 2, x1 = (int)floor(X) + 2;
+        int y0 = (int)floor(Y) - 2, y1 = (int)floor(Y) + 2;
+        for (int y = y0; y <= y1; ++y) {
+            if (y < 0 || y >= ny) continue;
+            for (int x = x0; x <= x1; ++x) {
+                if (x < 0 || x >= nx) continue;
+                double kernel = or_ibm_kernel(x - X, y - Y);
+                if (kernel == 0.0) continue;
+                int idx = nidx(s, x, y);
+                if (s->obstacle[idx]) continue;
+                double rho, uu, vv;
+                or_macros(&s->f[(size_t)idx * 9], &rho, &uu, &vv);
+                u += uu * kernel;
+                v += vv * kernel;
+            }
+        }
+        s->ibm_U[p] = u;
+        s->ibm_V[p] = v;
+    }
+    for (int p = 0; p < np; ++p) {
+        s->ibm_FX[p] = (s->ibm_uwx - s->ibm_U[p]) / s->ibm_dt;
+        s->ibm_FY[p] = (s->ibm_uwy - s->ibm_V[p]) / s->ibm_dt;
+    }
+    double *fxg = calloc(N, sizeof(double)), *fyg = calloc(N, sizeof(double));
+    for (int p = 0; p < np; ++p) {
+        double X = s->ibm_X[p], Y = s->ibm_Y[p];
+        double fx = s->ibm_FX[p], fy = s->ibm_FY[p];
+        int x0 = (int)floor(X) - 2, x1 = (int)floor(X) + 2;
+        int y0 = (int)floor(Y) - 2, y1 = (int)floor(Y) + 2;
+        for (int y = y0; y <= y1; ++y) {
+            if (y < 0 || y >= ny) continue;
+            for (int x = x0; x <= x1; ++x) {
+                if (x < 0 || x >= nx) continue;
+                double kernel = or_ibm_kernel(x - X, y - Y);
+                if (kernel == 0.0) continue;
+                int idx = y * nx + x;
+                fxg[idx] += fx * kernel;
+                fyg[idx] += fy * kernel;
+            }
+        }
+    }
+    or_step(s, tau, u_in);
+    for (int y = 0; y < ny; ++y) {
+        for (int x = 0; x < nx; ++x) {
+            int idx = nidx(s, x, y);
+            if (s->obstacle[idx]) continue;
+            double *fn = &s->f[(size_t)idx * 9];
+            double fx = fxg[idx], fy = fyg[idx];
+            for (int i = 0; i < 9; ++i) {
+                double edotu = OR_CX[i] * 0 + OR_CY[i] * 0;
+                double Fdot = OR_CX[i] * fx + OR_CY[i] * fy;
+                double correction = OR_W[i] * (3.0 * Fdot + 9.0 * edotu * (OR_CX[i] * fx + OR_CY[i] * fy));
+                fn[i] += correction;
+            }
+        }
+    }
+    free(fxg);
+    free(fyg);
+}
+
+/* Lagrangian velocities and forces of the last or_ibm_step. */
+void or_ibm_lagrangian(const or_state *s, double *U, double *V, double *FX, double *FY) {
+    for (int p = 0; p < s->ibm_n; ++p) {
+        U[p] = s->ibm_U[p]; V[p] = s->ibm_V[p];
+        FX[p] = s->ibm_FX[p]; FY[p] = s->ibm_FY[p];
+    }
 }

@@ -82,6 +82,29 @@ def _load(path: str, prefix: str) -> C.CDLL:
         fn = getattr(lib, prefix + name)
         fn.argtypes = args
         fn.restype = res
+    # immersed boundary: the harness wraps the reference's ImmersedBoundary,
+    # the restatement takes the points explicitly
+    if stateful:
+        ibm = {
+            "or_ibm_points_from_polygon": ([_DP, _I, _D, _DP, _DP, _I], _I),
+            "or_ibm_set": ([_P, _DP, _DP, _I, _D, _D, _D], None),
+            "or_ibm_step": ([_P, _D, _D], None),
+            "or_ibm_lagrangian": ([_P, _DP, _DP, _DP, _DP], None),
+            "or_ibm_kernel": ([_D, _D], _D),
+        }
+    else:
+        ibm = {
+            "ref_ibm_from_polygon": ([_DP, _I, _D], _I),
+            "ref_ibm_points": ([_DP, _DP], None),
+            "ref_ibm_set_dt": ([_D], None),
+            "ref_ibm_step": ([_D, _D], None),
+            "ref_ibm_lagrangian": ([_DP, _DP, _DP, _DP], None),
+            "ref_ibm_kernel": ([_D, _D], _D),
+        }
+    for name, (args, res) in ibm.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
     return lib
 
 
@@ -215,6 +238,47 @@ class Solver:
 
     def init_thermal_uniform(self, T, u, v):
         self._c("init_thermal_uniform", float(T), float(u), float(v))
+
+    # immersed boundary (src/ibm.hpp, driven as src/airfoil_ibm.cpp:121-176)
+    def ibm_from_polygon(self, xy, spacing=1.0, dt=1.0):
+        """Lagrangian points of ImmersedBoundary::build_from_polygon, installed
+        for ibm_step; returns them as an (n, 2) array."""
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        if self.kind == "ref":
+            n = self.lib.ref_ibm_from_polygon(_dptr(a), len(a) // 2, float(spacing))
+            X, Y = np.zeros(n), np.zeros(n)
+            self.lib.ref_ibm_points(_dptr(X), _dptr(Y))
+            self.lib.ref_ibm_set_dt(float(dt))
+        else:
+            X, Y = ibm_points_from_polygon(a.reshape(-1, 2), spacing).T.copy()
+            self.lib.or_ibm_set(self.h, _dptr(X), _dptr(Y), len(X), float(dt), 0.0, 0.0)
+        self._ibm_n = len(X)
+        return np.stack([X, Y], 1)
+
+    def ibm_step(self, tau, u_in, n=1):
+        for _ in range(n):
+            self._c("ibm_step", float(tau), float(u_in))
+
+    def ibm_lagrangian(self):
+        """(U, V, FX, FY) at the Lagrangian points after the last ibm_step."""
+        out = [np.zeros(self._ibm_n) for _ in range(4)]
+        self._c("ibm_lagrangian", *(_dptr(a) for a in out))
+        return tuple(out)
+
+
+def ibm_points_from_polygon(xy, spacing=1.0) -> np.ndarray:
+    """ImmersedBoundary::build_from_polygon (src/ibm.hpp:42-69), restated."""
+    L, _ = lib("oracle")
+    a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+    n = L.or_ibm_points_from_polygon(_dptr(a), len(a) // 2, float(spacing), None, None, 0)
+    X, Y = np.zeros(n), np.zeros(n)
+    L.or_ibm_points_from_polygon(_dptr(a), len(a) // 2, float(spacing), _dptr(X), _dptr(Y), n)
+    return np.stack([X, Y], 1)
+
+
+def ibm_kernel(dx, dy, kind: str = "oracle") -> float:
+    L, p = lib(kind)
+    return getattr(L, p + "ibm_kernel")(float(dx), float(dy))
 
 
 def naca_coords(series: int, n: int = 200, kind: str = "oracle") -> np.ndarray:

@@ -181,4 +181,92 @@ void ref_init_thermal_uniform(double T, double u, double v) {
         for (int i = 0; i < 9; ++i) g_sys->g_thermal[n * 9 + i] = thermal_equilibrium(i, T, u, v);
 }
 
+// ---- immersed boundary (src/ibm.hpp) driven as src/airfoil_ibm.cpp:121-176 does
+static ImmersedBoundary g_ibm;
+static std::vector<double> g_fx_lag, g_fy_lag;
+static double g_ibm_dt = 1.0;
+
+int ref_ibm_from_polygon(const double* xy, int n, double spacing) {
+    std::vector<std::pair<double, double>> p(n);
+    for (int k = 0; k < n; ++k) p[k] = {xy[2 * k], xy[2 * k + 1]};
+    g_ibm = ImmersedBoundary();
+    g_ibm.build_from_polygon(p, spacing);
+    g_fx_lag.assign(g_ibm.points.size(), 0.0);
+    g_fy_lag.assign(g_ibm.points.size(), 0.0);
+    return static_cast<int>(g_ibm.points.size());
+}
+
+void ref_ibm_points(double* X, double* Y) {
+    for (size_t p = 0; p < g_ibm.points.size(); ++p) {
+        X[p] = g_ibm.points[p].X;
+        Y[p] = g_ibm.points[p].Y;
+    }
+}
+
+void ref_ibm_set_dt(double dt) { g_ibm_dt = dt; }
+
+double ref_ibm_kernel(double dx, double dy) { return ibm_kernel(dx, dy); }
+
+// One iteration of the airfoil driver's loop: interpolate the velocity at the
+// Lagrangian points (fluid nodes only), no-slip force, spread, step, then the
+// explicit forcing of the fluid nodes.
+void ref_ibm_step(double tau, double u_inflow) {
+    LBMCapabilities& system = *g_sys;
+    ImmersedBoundary& iboundary = g_ibm;
+    for (size_t p = 0; p < iboundary.points.size(); ++p) {
+        double X = iboundary.points[p].X;
+        double Y = iboundary.points[p].Y;
+        double u = 0, v = 0;
+        int x0 = static_cast<int>(std::floor(X)) - 2;
+        int x1 = static_cast<int>(std::floor(X)) + 2;
+        int y0 = static_cast<int>(std::floor(Y)) - 2;
+        int y1 = static_cast<int>(std::floor(Y)) + 2;
+        for (int y = y0; y <= y1; ++y) {
+            if (y < 0 || y >= NY) continue;
+            for (int x = x0; x <= x1; ++x) {
+                if (x < 0 || x >= NX) continue;
+                double kernel = ibm_kernel(x - X, y - Y);
+                if (kernel == 0.0) continue;
+                int idx = node_index(x, y);
+                if (system.obstacle[idx]) continue;
+                double rho, uu, vv;
+                compute_macros(&system.f[idx * 9], rho, uu, vv);
+                u += uu * kernel;
+                v += vv * kernel;
+            }
+        }
+        iboundary.points[p].U = u;
+        iboundary.points[p].V = v;
+    }
+    iboundary.compute_no_slip_force(g_ibm_dt, g_fx_lag, g_fy_lag);
+    std::vector<double> fx_grid(NX * NY, 0.0), fy_grid(NX * NY, 0.0);
+    iboundary.spread_force(g_fx_lag, g_fy_lag, fx_grid, fy_grid, NX, NY);
+    execute_time_step(system, tau, u_inflow);
+    for (int y = 0; y < NY; ++y) {
+        for (int x = 0; x < NX; ++x) {
+            int idx = node_index(x, y);
+            if (system.obstacle[idx]) continue;
+            double* f_node = &system.f[idx * 9];
+            double fx = fx_grid[idx];
+            double fy = fy_grid[idx];
+            for (int i = 0; i < 9; ++i) {
+                double edotu = cx[i] * 0 + cy[i] * 0;
+                double Fdot = cx[i] * fx + cy[i] * fy;
+                double correction = weights[i] * (3.0 * Fdot + 9.0 * edotu * (cx[i] * fx + cy[i] * fy));
+                f_node[i] += correction;
+            }
+        }
+    }
+}
+
+// Lagrangian velocities and forces of the last ref_ibm_step.
+void ref_ibm_lagrangian(double* U, double* V, double* FX, double* FY) {
+    for (size_t p = 0; p < g_ibm.points.size(); ++p) {
+        U[p] = g_ibm.points[p].U;
+        V[p] = g_ibm.points[p].V;
+        FX[p] = g_fx_lag[p];
+        FY[p] = g_fy_lag[p];
+    }
+}
+
 }  // extern "C"

@@ -220,3 +220,41 @@ def thermal_pre(s, spec, pre):
         Tw = pre[1]
         for n in np.nonzero(ob)[0]:
             g[n * 9:(n + 1) * 9] = w * Tw * 1.0
+
+
+# --------------------------------------------------------------------------- immersed boundary
+
+# Airfoil with immersed-boundary direct forcing, set up as src/airfoil_ibm.cpp
+# does: NACA polygon (naca_coords(series, npts)) centred at (NX/4, NY/2),
+# chord NY/3, rotated by the angle of attack; obstacle = nodes inside the
+# polygon (point_in_polygon, no bounce-back geometry); uniform equilibrium at
+# u_in (cos a, sin a); Lagrangian points every `spacing` cells; tau from
+# nu = u (NY/5) / Re; the default case type (CYLINDER: Zou/He inlet, outflow).
+IBM_CASES = {
+    "airfoil_ibm": dict(nx=120, ny=48, naca=2412, npts=100, aoa=8.0, re=100.0, u=0.1, steps=40,
+                        spacing=1.5, les=False),
+    "airfoil_ibm_les": dict(nx=96, ny=40, naca=12, npts=60, aoa=4.0, re=300.0, u=0.1, steps=30,
+                            spacing=1.5, les=True, cs=0.12),
+}
+
+
+def ibm_tau(spec):
+    nu = spec["u"] * (spec["ny"] / 5.0) / spec["re"]
+    return 0.5 + 3.0 * nu
+
+
+def ibm_setup(s, spec, naca_fn, transform_fn, pip_fn, eq_fn):
+    """Drive a solver with the oracle's surface through the airfoil set-up;
+    returns the airfoil polygon (the Lagrangian points are made from it)."""
+    nx, ny = spec["nx"], spec["ny"]
+    s.set_case(CYLINDER, MRT, spec.get("les", False), spec.get("cs", 0.12))
+    poly = transform_fn(naca_fn(spec["naca"], spec["npts"]), nx / 4, ny / 2, ny / 3.0, spec["aoa"])
+    ob = s.obstacle
+    for y in range(ny):
+        for x in range(nx):
+            if pip_fn(float(x), float(y), poly):
+                ob[y * nx + x] = 1
+    a = spec["aoa"] * math.pi / 180.0
+    eq = np.array([eq_fn(i, 1.0, spec["u"] * math.cos(a), spec["u"] * math.sin(a)) for i in range(9)])
+    s.f[:] = np.tile(eq, nx * ny)
+    return poly

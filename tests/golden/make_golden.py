@@ -81,6 +81,29 @@ def kat(kind: str) -> dict:
     return out
 
 
+def run_ibm_case(kind: str, spec: dict) -> dict:
+    """The airfoil immersed-boundary driver loop (src/airfoil_ibm.cpp:121-176)
+    on the reference's ImmersedBoundary (kind "ref") or the restatement."""
+    s = O.Solver(spec["nx"], spec["ny"], kind)
+    poly = CS.ibm_setup(s, spec,
+                        naca_fn=lambda ser, n: O.naca_coords(ser, n, kind),
+                        transform_fn=lambda p, *a: O.transform_points(p, *a, kind=kind),
+                        pip_fn=lambda x, y, p: O.point_in_polygon(x, y, p, kind),
+                        eq_fn=lambda i, r, u, v: O.equilibrium(i, r, u, v, kind))
+    out = {"mask": s.obstacle.copy(), "f0": s.f.copy(), "poly": poly}
+    out["points"] = s.ibm_from_polygon(poly, spec["spacing"])
+    tau = CS.ibm_tau(spec)
+    sums = []
+    for _ in range(spec["steps"]):
+        s.ibm_step(tau, spec["u"])
+        sums.append(s.force_sums())
+    out["f"] = s.f.copy()
+    out["U"], out["V"], out["FX"], out["FY"] = s.ibm_lagrangian()
+    out["sums"] = np.array(sums, np.float64)
+    s.close()
+    return out
+
+
 def main():
     if not os.path.exists(O.LIB_REF):
         sys.exit("oracle/_ref/libref.so missing: build it with `make -C oracle ref`")
@@ -88,6 +111,10 @@ def main():
         res = run_case("ref", spec)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
         print(f"{name}: steps={spec['steps']} sums[-1]={res['sums'][-1]}")
+    for name, spec in CS.IBM_CASES.items():
+        res = run_ibm_case("ref", spec)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
+        print(f"{name}: points={len(res['points'])} steps={spec['steps']}")
     np.savez_compressed(os.path.join(HERE, "kat.npz"), **kat("ref"))
     print("kat written")
 
