@@ -540,6 +540,97 @@ def run_frame(args):
     return 0
 
 
+def _airfoil_solver(lbm2d, nx, ny, storage, aoa=8.0, re=100.0, spacing=1.5, ibm=True):
+    """The airfoil driver's set-up (src/airfoil_ibm.cpp): NACA 2412 at
+    (NX/4, NY/2), chord NY/3, obstacle by point-in-polygon, uniform inflow at
+    the angle of attack; Lagrangian points every `spacing` cells."""
+    import math
+    poly = lbm2d.transform_points(lbm2d.naca_coords(2412, 100), nx / 4, ny / 2, ny / 3.0, aoa)
+    mask = np.zeros(nx * ny, np.uint8)
+    flat = np.ascontiguousarray(poly.reshape(-1))
+    lbm2d.lib().lbm2d_mask_polygon(nx, ny, lbm2d._u8(mask), lbm2d._d(flat), len(poly))
+    s = lbm2d.Solver(nx, ny, lbm2d.CYLINDER, lbm2d.MRT, False, 0.12, storage)
+    s.set_mask(mask)
+    a = aoa * math.pi / 180.0
+    s.upload_f(lbm2d.equilibrium_field(nx, ny, 1.0, 0.1 * math.cos(a), 0.1 * math.sin(a)))
+    pts = lbm2d.ibm_points_from_polygon(poly, spacing)
+    if ibm:
+        s.set_ibm(pts)
+    tau = 0.5 + 3.0 * 0.1 * (ny / 5.0) / re
+    return s, tau, pts, mask, poly
+
+
+def run_ibm(args):
+    """Immersed-boundary airfoil (the reference's airfoil driver loop on the
+    device): step throughput with and without the boundary attached, and the
+    reference loop on the host cores (oracle restatement) for a bounded
+    sample."""
+    import torch
+
+    import lbm2d
+    lbm2d.build(quiet=True)
+    out = {}
+    for nx, ny in ((800, 300), (4096, 1536)):
+        row = {}
+        for label, ibm in (("plain", False), ("ibm", True)):
+            s, tau, pts, _, _ = _airfoil_solver(lbm2d, nx, ny, "fp32", ibm=ibm)
+            stream = torch.cuda.ExternalStream(s.stream)
+            s.step(tau, 0.1, 20)
+            s.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            steps = 2000 if nx * ny < 1 << 20 else 500
+            l0 = s.launches
+            e0.record(stream)
+            s.step(tau, 0.1, steps)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            diverged = False
+            try:
+                s.synchronize()
+            except lbm2d.LBMError:
+                diverged = True
+            row[label] = {"ms_per_step": ms, "glups": nx * ny / ms / 1e6, "launches_per_step": (s.launches - l0) / steps,
+                          "diverged": diverged}
+            if ibm:
+                row["points"] = len(pts)
+            s.close()
+        row["ibm_overhead"] = row["ibm"]["ms_per_step"] / row["plain"]["ms_per_step"]
+        out[f"{nx}x{ny}"] = row
+    # the reference loop on the host cores: oracle restatement, 800x300
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, ROOT)
+        from oracle import oracle as O
+        if not os.path.exists(O.LIB_ORACLE):
+            O.build()
+        nx, ny = 800, 300
+        s, tau, pts, mask, poly = _airfoil_solver(lbm2d, nx, ny, "fp32", ibm=False)
+        s.close()
+        o = O.Solver(nx, ny, "oracle")
+        o.set_case(O.CYLINDER)
+        o.obstacle[:] = mask
+        o.f[:] = lbm2d.equilibrium_field(nx, ny, 1.0, 0.1 * np.cos(np.radians(8.0)), 0.1 * np.sin(np.radians(8.0)))
+        o.ibm_from_polygon(poly, 1.5)
+        o.ibm_step(tau, 0.1, 2)
+        t0 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t0 < 10.0 and n < 400:
+            o.ibm_step(tau, 0.1)
+            n += 1
+        dt = time.perf_counter() - t0
+        o.close()
+        cpu = {"value": nx * ny * n / dt / 1e9, "unit": "GLUPS", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} immersed-boundary iterations of the airfoil loop at 800x300 (oracle restatement, "
+                         f"OpenMP step)"}
+    line = {"metric": "immersed-boundary airfoil: step throughput with the boundary's forcing", "unit": "GLUPS",
+            "results": out, "cpu_baseline": cpu,
+            "config": {"workload": "NACA 2412 airfoil, chord NY/3 at (NX/4, NY/2), AoA 8 deg, Re 100 on NY/5, "
+                                   "u=0.1, Lagrangian spacing 1.5, FP32 storage", "storage": "fp32"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_precision(args):
     """Error of FP32 / FP16 / BF16 storage against an FP64 run of the same
     kernel on the channel workload: relative L2 of the velocity field over
@@ -591,7 +682,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (default: --steps)")
-    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "precision", "frame"])
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "precision", "frame", "ibm"])
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--batch-storage", default="fp32")
     ap.add_argument("--autotune", action="store_true")
@@ -615,6 +706,8 @@ def main():
         return run_precision(args)
     if args.mode == "frame":
         return run_frame(args)
+    if args.mode == "ibm":
+        return run_ibm(args)
 
     import torch
 

@@ -201,6 +201,25 @@ int lbm2d_download_wall_dist(lbm2d_solver *h, double *wall_dist);
 int lbm2d_frame_fields(lbm2d_solver *h, int ds, int sanitize, double T_wall, double *rho, double *u, double *v,
                        double *vel, double *omega, double *T, uint8_t *obstacle);
 
+/* Immersed-boundary direct forcing (src/ibm.hpp) applied around every step
+ * as the airfoil driver's loop does it (src/airfoil_ibm.cpp:121-176): the
+ * velocity at each Lagrangian point (X[p], Y[p]) is interpolated with the
+ * 4-point cosine delta from the fluid nodes of its 5x5 stencil, the no-slip
+ * force (u_wall - U) / dt is spread back to the grid in point order, and
+ * after the step every fluid node gets f_i += w_i (3 c_i.F + 9 (c_i.0)(c_i.F)).
+ * The points are fixed until the next call; npts = 0 removes the boundary.
+ * The momentum-exchange force (fx_body) still comes from the state before
+ * the forcing, as in the reference; downloads of f, macros and frames see the
+ * forced state.  Not with the thermal DDF or inside a batch
+ * (LBM2D_ERR_INVALID).  The reference's driver loop has no library entry
+ * point; this call replaces it. */
+int lbm2d_set_ibm(lbm2d_solver *h, const double *X, const double *Y, int npts, double dt, double u_wall_x,
+                  double u_wall_y);
+/* The Lagrangian velocities U, V and forces FX, FY (ImmersedBoundary::points
+ * and the driver's fx_lag / fy_lag, src/ibm.hpp:27-34, 139-149) that produced
+ * the forcing of the last step.  Any output may be NULL. */
+int lbm2d_ibm_lagrangian(lbm2d_solver *h, double *U, double *V, double *FX, double *FY);
+
 /* FP64 reductions over the fluid nodes of the current state: total mass
  * (the quantity of the reference's conservation test, src/lbm_test.cpp:
  * 173-198), x/y momentum, and the steady-state residual
@@ -373,6 +392,11 @@ int lbm2d_naca_coords(int series, int n, double *out);
 int lbm2d_transform_points(double *xy, int n, double cx, double cy, double scale, double angle_deg);
 /* compute_wall_distance's result, src/lbm_types.hpp:231-264 */
 int lbm2d_wall_distance(int nx, int ny, const uint8_t *mask, double *wall_dist);
+/* Lagrangian points of ImmersedBoundary::build_from_polygon (src/ibm.hpp:
+ * 42-69): max(8, perimeter / spacing) points spaced uniformly in the
+ * polygon's vertex parameter.  Writes at most cap points to X, Y (either may
+ * be NULL to query the count); returns the point count. */
+int lbm2d_ibm_points_from_polygon(const double *xy, int n, double spacing, double *X, double *Y, int cap);
 
 /* Statistics of a drag/lift series as the reference's post-processing
  * computes them (scripts/extract_forces.py:91-121 and :137-158): means of

@@ -326,6 +326,7 @@ int lbm2d_batch_add(lbm2d_batch* b, lbm2d_solver* h, double tau, double u) {
     if (h->device != b->device) return bfail(b, LBM2D_ERR_INVALID, "member lives on another device");
     if (!(tau > 0.0)) return bfail(b, LBM2D_ERR_INVALID, "tau must be positive");
     if (member_index(b, h) >= 0) return bfail(b, LBM2D_ERR_INVALID, "already a member");
+    if (ibm_active(h)) return bfail(b, LBM2D_ERR_INVALID, "a solver with an immersed boundary steps alone");
     b->members.push_back({h, tau, u});
     h->in_batch = true;
     b->layout_dirty = true;

@@ -323,6 +323,7 @@ KParams rebuild_params(const lbm2d_solver* h) {
     p.fin = h->P[h->cur ^ 1];
     p.gin = h->G[h->cur ^ 1];
     set_u_bc(p, h->u_last);
+    ibm_state_params(h, p);
     return p;
 }
 
@@ -374,6 +375,8 @@ int prologue(lbm2d_solver* h, const CollideParams& c) {
     int e = launch_prologue(h->storage, p, h->d_stage_f, h->thermal ? h->d_stage_g : nullptr, h->stream);
     ++h->launches;
     if (e) return cuda_fail(h, (cudaError_t)e, "prologue");
+    // immersed boundary: the force of the first step comes from the staged state
+    if ((rc = ibm_from_stage(h, p))) return rc;
     h->staged = false;
     h->cp_of_P = c;
     h->steps_since_collide = 0;
@@ -511,6 +514,8 @@ int lbm2d_destroy(lbm2d_solver* h) {
     if (!h) return LBM2D_OK;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->pair_graph) cudaGraphExecDestroy(h->pair_graph);
+    ibm_release(h);
     void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
                     h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
                     h->d_counter, h->d_last, h->d_nan, h->d_seed, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
@@ -614,6 +619,8 @@ int lbm2d_set_thermal(lbm2d_solver* h, int use, double T_ref, double alpha, doub
     int rc;
     if ((rc = check_handle(h))) return rc;
     const bool on = use != 0;
+    if (on && ibm_active(h))
+        return fail(h, LBM2D_ERR_INVALID, "the thermal DDF is not available with an immersed boundary");
     if (on != h->thermal || (on && T_ref != h->T_ref)) {
         if ((rc = before_setting_change(h))) return rc;
         if (on && (rc = ensure_stage(h, true))) return rc;
@@ -678,6 +685,116 @@ int lbm2d_init_equilibrium(lbm2d_solver* h, double rho, double u, double v, doub
     return LBM2D_OK;
 }
 
+}  // extern "C"
+
+namespace lbm2d {
+namespace rt {
+namespace {
+
+// Launch one step from buffer h->cur (step kernel, force reduction,
+// immersed-boundary forcing); host state is not advanced.  With profiling
+// events, e0 / e1 bracket the step kernel alone.
+int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
+    p.fin = h->P[h->cur];
+    p.fout = h->P[h->cur ^ 1];
+    p.gin = h->G[h->cur];
+    p.gout = h->G[h->cur ^ 1];
+    p.seed_in = h->d_seed + h->cur;
+    p.seed_out = h->d_seed + (h->cur ^ 1);
+    p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
+    if (e0) CK(cudaEventRecord(e0, h->stream), "event");
+    int e = h->slot_kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
+                                        : launch_step(h->storage, p, h->bx, h->by, h->stream);
+    if (e1) CK(cudaEventRecord(e1, h->stream), "event");
+    ++h->launches;
+    if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
+    if (h->nslots > 0) {
+        e = launch_force_reduce(h->d_partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last, h->stream);
+        ++h->launches;
+        if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");
+    }
+    return ibm_after_step(h, p);
+}
+
+void advance(lbm2d_solver* h, long long n) {
+    if (n & 1) {
+        h->cur ^= 1;
+        if (ibm_active(h)) h->ibm_next ^= 1;
+    }
+    h->steps_since_collide += n;
+    h->steps_done += n;
+}
+
+// Everything a captured step pair depends on: the parameters of its first
+// step, the launch shape and the buffers passed outside the parameters.
+std::vector<unsigned char> pair_key(lbm2d_solver* h, const KParams& p0) {
+    KParams p = p0;
+    p.fin = h->P[h->cur];
+    p.fout = h->P[h->cur ^ 1];
+    p.gin = h->G[h->cur];
+    p.gout = h->G[h->cur ^ 1];
+    p.seed_in = h->d_seed + h->cur;
+    p.seed_out = h->d_seed + (h->cur ^ 1);
+    p.skip_settled_solids = (h->hook != 1) ? 1 : 0;
+    const long long extra[] = {h->slot_kind, h->slot_grid, h->bx, h->by, h->storage, h->cur, h->ibm_next,
+                               h->nslots, h->hist_cap, h->ibm_np, h->ibm_nb,
+                               (long long)(uintptr_t)h->d_hist, (long long)(uintptr_t)h->d_counter,
+                               (long long)(uintptr_t)h->d_last, (long long)(uintptr_t)h->d_ibm_buf,
+                               (long long)(uintptr_t)h->d_ibm_band, (long long)(uintptr_t)h->d_ibm_tab};
+    std::vector<unsigned char> k(sizeof(p) + sizeof(extra) + sizeof(IbmParams));
+    std::memcpy(k.data(), &p, sizeof(p));
+    std::memcpy(k.data() + sizeof(p), extra, sizeof(extra));
+    std::memcpy(k.data() + sizeof(p) + sizeof(extra), &h->ibm_q, sizeof(IbmParams));  // table offsets, dt, u_wall
+    return k;
+}
+
+// Capture two consecutive steps from the current buffers into a graph.
+int capture_pair(lbm2d_solver* h, const KParams& p0, std::vector<unsigned char>&& key) {
+    if (h->pair_graph) cudaGraphExecDestroy(h->pair_graph);
+    h->pair_graph = nullptr;
+    h->pair_key.clear();
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const long long l0 = h->launches;
+    const int cur0 = h->cur, next0 = h->ibm_next;
+    const long long ssc = h->steps_since_collide, sd = h->steps_done;
+    KParams p = p0;
+    int rc = launch_one_step(h, p);
+    if (!rc) {
+        advance(h, 1);
+        rc = launch_one_step(h, p);
+    }
+    h->cur = cur0;
+    h->ibm_next = next0;
+    h->steps_since_collide = ssc;
+    h->steps_done = sd;
+    const long long per_pair = h->launches - l0;
+    h->launches = l0;  // counted when replayed
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "end capture");
+    const cudaError_t ei = cudaGraphInstantiate(&h->pair_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return cuda_fail(h, ei, "instantiate");
+    h->pair_key = std::move(key);
+    h->pair_launches = per_pair;
+    return LBM2D_OK;
+}
+
+}  // namespace
+}  // namespace rt
+}  // namespace lbm2d
+
+extern "C" {
+
+// Steps run one launch sequence each until the per-step parameters are
+// stable (two steps after the last collision), then whole step pairs replay
+// a captured CUDA graph: one graph launch instead of 2-10 kernel launches per
+// pair, which is what bounds small grids.  The graph is kept while the
+// parameters, the launch shape and the buffers stay the same.
 int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
     int rc;
     if ((rc = check_handle(h))) return rc;
@@ -685,14 +802,24 @@ int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
     if (nsteps == 0) return LBM2D_OK;
     KParams p;
     if ((rc = prepare_steps(h, tau, u_inflow, p))) return rc;
-    for (int k = 0; k < nsteps; ++k) {
-        p.fin = h->P[h->cur];
-        p.fout = h->P[h->cur ^ 1];
-        p.gin = h->G[h->cur];
-        p.gout = h->G[h->cur ^ 1];
-        p.seed_in = h->d_seed + h->cur;
-        p.seed_out = h->d_seed + (h->cur ^ 1);
-        p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
+    int k = 0;
+    while (k < nsteps) {
+        const int left = nsteps - k;
+        if (!h->profiling && left >= 2 && h->steps_since_collide >= 2) {
+            std::vector<unsigned char> key = pair_key(h, p);
+            const bool have = h->pair_graph && key == h->pair_key;
+            if (!have && k >= 2 && left >= 4) {
+                if ((rc = capture_pair(h, p, std::move(key)))) return rc;
+            }
+            if (h->pair_graph && (have || k >= 2) && pair_key(h, p) == h->pair_key) {
+                const int pairs = left / 2;
+                for (int i = 0; i < pairs; ++i) CK(cudaGraphLaunch(h->pair_graph, h->stream), "graph launch");
+                h->launches += h->pair_launches * pairs;
+                advance(h, 2LL * pairs);
+                k += 2 * pairs;
+                continue;
+            }
+        }
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (h->profiling) {
             if (h->ev_used + 2 > h->ev_pool.size()) {
@@ -704,22 +831,10 @@ int lbm2d_step(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
             }
             e0 = h->ev_pool[h->ev_used++];
             e1 = h->ev_pool[h->ev_used++];
-            CK(cudaEventRecord(e0, h->stream), "event");
         }
-        int e = h->slot_kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
-                                            : launch_step(h->storage, p, h->bx, h->by, h->stream);
-        if (e1) CK(cudaEventRecord(e1, h->stream), "event");
-        ++h->launches;
-        if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
-        if (h->nslots > 0) {
-            e = launch_force_reduce(h->d_partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last,
-                                    h->stream);
-            ++h->launches;
-            if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");
-        }
-        h->cur ^= 1;
-        ++h->steps_since_collide;
-        ++h->steps_done;
+        if ((rc = launch_one_step(h, p, e0, e1))) return rc;
+        advance(h, 1);
+        ++k;
     }
     h->u_last = u_inflow;
     return LBM2D_OK;

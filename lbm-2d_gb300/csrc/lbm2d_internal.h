@@ -101,7 +101,13 @@ struct KParams {
     // unlimited); read from left_in, decremented into left_out
     const int* left_in;
     int* left_out;
+    // immersed boundary (state rebuilds only; null in step launches): band
+    // index of each node (-1 outside the band) and the grid force (fx, fy)
+    // per band node whose forcing the current state carries
+    const int* ibm_band;
+    const double* ibm_F;
 };
+static_assert(sizeof(KParams) % 16 == 0, "KParams is staged with 16-byte copies");
 
 // Readback outputs (any may be null).
 struct ROut {
@@ -122,6 +128,27 @@ struct FOut {
     int sanitize;  // 1: the JSON writers' NaN / zero-density replacements
 };
 
+// Immersed-boundary tables and buffers of one solver (device pointers).
+// Band nodes: every node in the support of some Lagrangian point's delta
+// kernel.  Spread lists (per band node, points in increasing order) and
+// interpolation lists (per point, stencil nodes in the reference's y-major
+// order) carry the host-computed kernel weights.
+struct IbmParams {
+    int nb, np;
+    const uint32_t* band_node;
+    const int* sp_start;
+    const int* sp_pt;
+    const double* sp_w;
+    const int* ip_start;
+    const int* ip_band;
+    const double* ip_w;
+    double* uv;             // [2*nb] band velocities of the latest state
+    double* F;              // [2*nb] grid force the latest state carries
+    const double* lag_in;   // [4*np] U, V, FX, FY whose forces the step applies
+    double* lag_out;        // [4*np] the same from the new state (next step)
+    double dt, uwx, uwy;
+};
+
 // One instance's second-stage force reduction in a batched launch.
 struct ReduceJob {
     const double* partials;
@@ -135,6 +162,15 @@ struct ReduceJob {
 // Launchers (lbm2d_kernels.cu).  All return a cudaError_t as int.
 int launch_step(int storage, const KParams& p, int bx, int by, void* stream);
 int launch_readback(int storage, const KParams& p, const ROut& o, void* stream);
+// Immersed boundary, after each step kernel (p: that step's parameters, fin
+// its input buffer): per band node, the grid force from q.lag_in, the forced
+// state, its velocity and its collision into p.fout; then per point the new
+// velocity and force into q.lag_out.
+int launch_ibm_after_step(int storage, const KParams& p, const IbmParams& q, void* stream);
+// Band velocities of the staged FP64 AoS state (and a zero pending force),
+// then the points' velocities and forces into q.lag_out, before the first
+// step from it.
+int launch_ibm_from_stage(int storage, const KParams& p, const IbmParams& q, const double* aos, void* stream);
 // Frame fields of the post-stream state (two launches: point fields, then
 // the vorticity stencil over them).
 int launch_frame(int storage, const KParams& p, const FOut& o, void* stream);

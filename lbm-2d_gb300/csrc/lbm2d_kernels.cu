@@ -186,10 +186,12 @@ __global__ void __launch_bounds__(512) batch_step_pair_kernel(const KParams* __r
         step_pair_block<T>(sp, t % sp.gx, t / sp.gx, sp.gx);
 }
 
-// Post-stream state of node (x, y) in FP64: stored deviations are widened
-// before the shift is added back, so the FP64 value is exact.
+// Post-stream state of node (x, y) in FP64 as the step rebuilds it (before
+// any immersed-boundary forcing): stored deviations are widened before the
+// shift is added back, so the FP64 value is exact.
 template <class T, bool TH>
-__device__ __forceinline__ void state_fp64(const KParams& p, int x, int y, uint32_t fl, double f[9], double g[9]) {
+__device__ __forceinline__ void state_raw_fp64(const KParams& p, int x, int y, uint32_t fl, double f[9],
+                                               double g[9]) {
     if constexpr (std::is_same<T, double>::value) {
         build_state<T, TH>(p, x, y, fl, f, g);
     } else {
@@ -204,6 +206,37 @@ __device__ __forceinline__ void state_fp64(const KParams& p, int x, int y, uint3
     }
 }
 
+// Explicit forcing of a fluid node by the immersed boundary's grid force
+// (src/airfoil_ibm.cpp:158-176): f_i += w_i (3 c_i.F + 9 (c_i.0)(c_i.F)),
+// each operation rounded on its own in the reference's order (c_i.0 is the
+// integer zero of the driver's "u ~ 0" approximation).
+__device__ __forceinline__ void ibm_force_node(double f[9], double fx, double fy) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const double cxd = double(CXf(i)), cyd = double(CYf(i));
+        const double edotu = 0.0;
+        const double Fdot = __dadd_rn(__dmul_rn(cxd, fx), __dmul_rn(cyd, fy));
+        const double t = __dadd_rn(__dmul_rn(3.0, Fdot), __dmul_rn(__dmul_rn(9.0, edotu), Fdot));
+        f[i] = __dadd_rn(f[i], __dmul_rn(wgt(i), t));
+    }
+}
+
+// The immersed boundary's forcing carried by the current state, if any.
+__device__ __forceinline__ void ibm_apply(const KParams& p, size_t n, uint32_t fl, double f[9]) {
+    if (p.ibm_band && !(fl & FLAG_SOLID)) {
+        const int b = p.ibm_band[n];
+        if (b >= 0) ibm_force_node(f, p.ibm_F[2 * b], p.ibm_F[2 * b + 1]);
+    }
+}
+
+// The reference's state S_n of node (x, y) in FP64: the rebuilt post-stream
+// state plus the immersed-boundary forcing applied after the step.
+template <class T, bool TH>
+__device__ __forceinline__ void state_fp64(const KParams& p, int x, int y, uint32_t fl, double f[9], double g[9]) {
+    state_raw_fp64<T, TH>(p, x, y, fl, f, g);
+    if (!TH) ibm_apply(p, (size_t)y * p.nx + x, fl, f);
+}
+
 template <class T, bool TH>
 __global__ void readback_kernel(const KParams p, const ROut o) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -212,7 +245,21 @@ __global__ void readback_kernel(const KParams p, const ROut o) {
     const size_t n = (size_t)y * p.nx + x;
     const uint32_t fl = p.flags[n];
     double f[9], g[9];  // the reference's post-stream state in FP64
-    state_fp64<T, TH>(p, x, y, fl, f, g);
+    state_raw_fp64<T, TH>(p, x, y, fl, f, g);
+    // momentum exchange from the state before the immersed-boundary forcing
+    // (the reference's force pass ends its step; the driver forces after it)
+    double fxn = 0.0, fyn = 0.0;
+    if (o.fx && !(fl & FLAG_SOLID) && (fl & FLAG_BOUNDARY)) {
+        const uint32_t fm = p.rec_force[fl >> 2];
+        for (int i = 0; i < 9; ++i) {  // reference accumulation order (src/lbm.hpp:550-577)
+            const int j = BBf(i);
+            if (fm & (1u << j)) {
+                fxn += double(CXf(i)) * 2.0 * double(f[j]);
+                fyn += double(CYf(i)) * 2.0 * double(f[j]);
+            }
+        }
+    }
+    if (!TH) ibm_apply(p, n, fl, f);
     if (o.f_aos)
         for (int j = 0; j < 9; ++j) o.f_aos[n * 9 + j] = f[j];
     if (TH && o.g_aos)
@@ -231,19 +278,173 @@ __global__ void readback_kernel(const KParams p, const ROut o) {
         o.T[n] = T;
     }
     if (o.fx) {
-        double fx = 0.0, fy = 0.0;
-        if (!(fl & FLAG_SOLID) && (fl & FLAG_BOUNDARY)) {
-            const uint32_t fm = p.rec_force[fl >> 2];
-            for (int i = 0; i < 9; ++i) {  // reference accumulation order (src/lbm.hpp:550-577)
-                const int j = BBf(i);
-                if (fm & (1u << j)) {
-                    fx += double(CXf(i)) * 2.0 * double(f[j]);
-                    fy += double(CYf(i)) * 2.0 * double(f[j]);
-                }
-            }
+        o.fx[n] = fxn;
+        o.fy[n] = fyn;
+    }
+}
+
+// compute_macros (src/lbm_types.hpp:278-288) in the reference's FP64
+// operation order: sequential sums in slot order, u = mx / rho, every
+// operation rounded on its own.
+__device__ __forceinline__ void macros_ref(const double f[9], double& rho, double& u, double& v) {
+    double r = 0.0, mx = 0.0, my = 0.0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        r = __dadd_rn(r, f[q]);
+        mx = __dadd_rn(mx, __dmul_rn(f[q], double(CXf(q))));
+        my = __dadd_rn(my, __dmul_rn(f[q], double(CYf(q))));
+    }
+    rho = r;
+    u = __ddiv_rn(mx, r);
+    v = __ddiv_rn(my, r);
+}
+
+// ----------------------------------------------------------------- immersed boundary
+// The airfoil driver's loop (src/airfoil_ibm.cpp:121-176) around the step:
+// velocity at the Lagrangian points from the fluid nodes of their delta
+// stencils, no-slip force (U_wall - U) / dt, spread to the grid, step, then
+// explicit forcing of the fluid nodes.  On the device the forcing is folded
+// into the stored state.  After the step kernel, a launch over the band (the
+// nodes in some point's stencil) spreads the points' forces to each band
+// node, forces the rebuilt node, records its velocity and collides it again
+// over the step kernel's value; a launch over the points then interpolates
+// the new velocities and forms the forces of the next step.  Nodes outside
+// the band carry no force and keep the step kernel's result.  The
+// momentum-exchange force of the step kernel comes from the unforced state,
+// as the reference computes it inside its step.  FP64 storage keeps the
+// reference's FP64 operations and order (R = double); the other storages
+// compute in FP32 with the same order.
+
+// Band node b after the step kernel: its grid force (the points' forces
+// q.lag_in times the kernel weights, summed in point order from zero,
+// src/ibm.hpp:72-103), the reference's state after the step with that
+// forcing, its velocity, and its collision into p.fout.
+template <class T>
+__global__ void ibm_band_kernel(const KParams p, const IbmParams q) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= q.nb) return;
+    using R = typename std::conditional<std::is_same<T, double>::value, double, float>::type;
+    const uint32_t n = q.band_node[b];
+    const int y = (int)(n / (uint32_t)p.nx), x = (int)(n - (uint32_t)y * (uint32_t)p.nx);
+    const uint32_t fl = p.flags[n];
+    R ax = R(0), ay = R(0);
+    const int k0 = q.sp_start[b], k1 = q.sp_start[b + 1];
+#pragma unroll 4
+    for (int k = k0; k < k1; ++k) {
+        const int pt = q.sp_pt[k];
+        const R w = R(q.sp_w[k]);
+        if constexpr (std::is_same<R, double>::value) {
+            ax = __dadd_rn(ax, __dmul_rn(q.lag_in[2 * q.np + pt], w));
+            ay = __dadd_rn(ay, __dmul_rn(q.lag_in[3 * q.np + pt], w));
+        } else {
+            ax = fmaf(float(q.lag_in[2 * q.np + pt]), w, ax);
+            ay = fmaf(float(q.lag_in[3 * q.np + pt]), w, ay);
         }
-        o.fx[n] = fx;
-        o.fy[n] = fy;
+    }
+    const double Fx = double(ax), Fy = double(ay);
+    q.F[2 * b] = Fx;  // the forcing the new state carries (readbacks add it)
+    q.F[2 * b + 1] = Fy;
+    if (fl & FLAG_SOLID) {
+        q.uv[2 * b] = 0.0;
+        q.uv[2 * b + 1] = 0.0;
+        return;
+    }
+    T* __restrict__ Fo = static_cast<T*>(p.fout);
+    const size_t N = (size_t)p.N;
+    if constexpr (std::is_same<T, double>::value) {
+        double f[9], g[9];
+        state_raw_fp64<T, false>(p, x, y, fl, f, g);
+        ibm_force_node(f, Fx, Fy);
+        double rho, u, v;
+        macros_ref(f, rho, u, v);
+        q.uv[2 * b] = u;
+        q.uv[2 * b + 1] = v;
+        collide<double, false>(p, fl, f, g);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) Fo[j * N + n] = f[j];
+    } else {
+        // on deviations, as the step kernels: the forcing adds w_i 3 c_i.F
+        float d[9], e[9];
+        build_dev<T, false>(p, x, y, fl, d, e);
+        const float fx = float(Fx), fy = float(Fy);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) d[j] = fmaf(float(wgt(j)) * 3.0f, float(CXf(j)) * fx + float(CYf(j)) * fy, d[j]);
+        const float drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+        const float mx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
+        const float my = (d[2] - d[4]) + (d[5] + d[6]) - (d[7] + d[8]);
+        const float inv = 1.0f / (1.0f + drho);
+        q.uv[2 * b] = double(mx * inv);
+        q.uv[2 * b + 1] = double(my * inv);
+        collide_dev<false>(p, fl, d, e);
+        uint32_t rb[9] = {};
+        if constexpr (Pop<T>::kRounds) rand9(seed_key(*p.seed_out ^ 0x2545F491u) + n, rb);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) Pop<T>::std_(Fo + j * N, n, d[j], rb[j]);
+    }
+}
+
+// Band velocities of a freshly staged FP64 AoS state; the staged state
+// carries no pending forcing.
+__global__ void ibm_stage_uv_kernel(const KParams p, const IbmParams q, const double* __restrict__ aos) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= q.nb) return;
+    const uint32_t n = q.band_node[b];
+    double u = 0.0, v = 0.0;
+    if (!(p.flags[n] & FLAG_SOLID)) {
+        double f[9], rho;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) f[j] = aos[(size_t)n * 9 + j];
+        macros_ref(f, rho, u, v);
+    }
+    q.uv[2 * b] = u;
+    q.uv[2 * b + 1] = v;
+    q.F[2 * b] = 0.0;
+    q.F[2 * b + 1] = 0.0;
+}
+
+// Point pt: velocity from the band velocities in the driver's y-major
+// stencil order (src/airfoil_ibm.cpp:124-147) and the no-slip force
+// (src/ibm.hpp:139-149) into q.lag_out = [U | V | FX | FY].  Solid stencil
+// nodes, which the reference skips, hold a zero velocity; adding +0 leaves
+// every partial sum unchanged bit for bit (a sum that starts at +0 under
+// round-to-nearest is never -0).
+// One warp per point: lane k loads stencil entry k (a stencil has at most
+// 5 x 5 = 25 entries) and forms its products in parallel; lane 0 then adds
+// them in stencil order, so the sum is the reference's sequential one.
+template <class R>
+__global__ void ibm_interp_kernel(const IbmParams q) {
+    const int pt = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (pt >= q.np) return;  // whole warps exit together
+    const int k0 = q.ip_start[pt], cnt = q.ip_start[pt + 1] - k0;
+    R pu = R(0), pv = R(0);
+    if (lane < cnt) {
+        const int b = q.ip_band[k0 + lane];
+        const R w = R(q.ip_w[k0 + lane]);
+        if constexpr (std::is_same<R, double>::value) {
+            pu = __dmul_rn(q.uv[2 * b], w);
+            pv = __dmul_rn(q.uv[2 * b + 1], w);
+        } else {
+            pu = float(q.uv[2 * b]) * w;
+            pv = float(q.uv[2 * b + 1]) * w;
+        }
+    }
+    R U = R(0), V = R(0);
+    for (int k = 0; k < cnt; ++k) {
+        const R a = __shfl_sync(0xffffffffu, pu, k), c = __shfl_sync(0xffffffffu, pv, k);
+        if constexpr (std::is_same<R, double>::value) {
+            U = __dadd_rn(U, a);
+            V = __dadd_rn(V, c);
+        } else {
+            U = __fadd_rn(U, a);
+            V = __fadd_rn(V, c);
+        }
+    }
+    if (lane == 0) {
+        q.lag_out[pt] = double(U);
+        q.lag_out[q.np + pt] = double(V);
+        q.lag_out[2 * q.np + pt] = __ddiv_rn(__dsub_rn(q.uwx, double(U)), q.dt);
+        q.lag_out[3 * q.np + pt] = __ddiv_rn(__dsub_rn(q.uwy, double(V)), q.dt);
     }
 }
 
@@ -270,15 +471,7 @@ __global__ void frame_kernel(const KParams p, const FOut o) {
     if (!solid) {
         double f[9], g[9];
         state_fp64<T, TH>(p, x, y, fl, f, g);
-        double mx = 0.0, my = 0.0;
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            rho = __dadd_rn(rho, f[q]);
-            mx = __dadd_rn(mx, __dmul_rn(f[q], double(CXf(q))));
-            my = __dadd_rn(my, __dmul_rn(f[q], double(CYf(q))));
-        }
-        u = __ddiv_rn(mx, rho);
-        v = __ddiv_rn(my, rho);
+        macros_ref(f, rho, u, v);
         Tn = 0.0;
         if (TH) {
 #pragma unroll
@@ -596,6 +789,43 @@ int launch_readback(int storage, const KParams& p, const ROut& o, void* stream) 
         case ST_FP64: return launch_readback_t<double>(p, o, s);
     }
     return (int)cudaErrorInvalidValue;
+}
+
+// The band and point kernels are short chains of dependent loads and
+// arithmetic over a few thousand threads: one-warp blocks spread them over as
+// many SMs as possible.
+constexpr int kIbmBlock = 32;
+
+template <class T>
+int launch_ibm_band_t(const KParams& p, const IbmParams& q, cudaStream_t s) {
+    using R = typename std::conditional<std::is_same<T, double>::value, double, float>::type;
+    if (q.nb > 0) ibm_band_kernel<T><<<(q.nb + kIbmBlock - 1) / kIbmBlock, kIbmBlock, 0, s>>>(p, q);
+    if (q.np > 0) ibm_interp_kernel<R><<<(q.np + 3) / 4, 128, 0, s>>>(q);  // a warp per point
+    return (int)cudaGetLastError();
+}
+
+int launch_ibm_after_step(int storage, const KParams& p, const IbmParams& q, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (storage) {
+        case ST_FP32: return launch_ibm_band_t<float>(p, q, s);
+        case ST_FP16: return launch_ibm_band_t<__half>(p, q, s);
+        case ST_BF16: return launch_ibm_band_t<__nv_bfloat16>(p, q, s);
+        case ST_FP64: return launch_ibm_band_t<double>(p, q, s);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_ibm_from_stage(int storage, const KParams& p, const IbmParams& q, const double* aos, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (q.nb > 0) ibm_stage_uv_kernel<<<(q.nb + kIbmBlock - 1) / kIbmBlock, kIbmBlock, 0, s>>>(p, q, aos);
+    if (q.np > 0) {
+        const int g = (q.np + 3) / 4;  // a warp per point
+        if (storage == ST_FP64)
+            ibm_interp_kernel<double><<<g, 128, 0, s>>>(q);
+        else
+            ibm_interp_kernel<float><<<g, 128, 0, s>>>(q);
+    }
+    return (int)cudaGetLastError();
 }
 
 int launch_frame(int storage, const KParams& p, const FOut& o, void* stream) {

@@ -97,7 +97,10 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
             ++h->launches;
             if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");
         }
+        // immersed boundary: launches only, its buffers exist since lbm2d_set_ibm
+        if ((rc = ibm_after_step(h, p))) return rc;
         h->cur ^= 1;
+        if (ibm_active(h)) h->ibm_next ^= 1;
         ++h->steps_since_collide;
         ++h->steps_done;
     }

@@ -104,6 +104,20 @@ struct lbm2d_solver {
     int variant = 0;
     bool in_batch = false;  // a batch member is stepped by the batched kernels
     bool profiling = false;
+    // immersed boundary (lbm2d_set_ibm); ibm_np == 0: none.  F and the
+    // Lagrangian values are double-buffered: slot ibm_next holds the force
+    // for the next step, slot ibm_next ^ 1 the force the current state
+    // carries (and the point values that produced it).
+    int ibm_np = 0, ibm_nb = 0, ibm_next = 0;
+    double ibm_dt = 1.0, ibm_uwx = 0.0, ibm_uwy = 0.0;
+    int* d_ibm_band = nullptr;    // per node: band index, -1 outside the band
+    char* d_ibm_tab = nullptr;    // band nodes, spread and interpolation lists
+    double* d_ibm_buf = nullptr;  // uv[2nb], F[2][2nb], lag[2][4np]
+    lbm2d::IbmParams ibm_q{};     // table pointers; uv; F_out / lag set per launch
+    // multi-step calls replay a captured pair of steps (see lbm2d_step)
+    cudaGraphExec_t pair_graph = nullptr;
+    std::vector<unsigned char> pair_key;
+    long long pair_launches = 0;
     std::vector<cudaEvent_t> ev_pool;  // even/odd = start/stop
     size_t ev_used = 0;
     std::string err;
@@ -129,6 +143,16 @@ int materialize(lbm2d_solver* h);
 int before_setting_change(lbm2d_solver* h);
 int prologue(lbm2d_solver* h, const CollideParams& c);
 int check_handle(lbm2d_solver* h);
+// Immersed boundary (lbm2d_ibm.cpp).  ibm_after_step runs after each step
+// kernel (p: that step's parameters; the caller then flips ibm_next with
+// cur); ibm_from_stage after a prologue
+// computes the first force from the staged state; ibm_state_params adds the
+// forcing the current state carries to rebuild parameters.
+inline bool ibm_active(const lbm2d_solver* h) { return h->ibm_np > 0; }
+int ibm_after_step(lbm2d_solver* h, const KParams& p);
+int ibm_from_stage(lbm2d_solver* h, const KParams& p);
+void ibm_state_params(const lbm2d_solver* h, KParams& p);
+void ibm_release(lbm2d_solver* h);
 // Two x-neighbours per thread (packed FP32x2 collision) when nx is even and
 // the step is non-thermal FP32/FP16/BF16.
 bool use_pair(const lbm2d_solver* h);

@@ -18,9 +18,7 @@
 #include "geometry.hpp"
 #include "lbm_types.hpp"
 #include "thermal.hpp"
-#if __has_include("ibm.hpp")
-#include "ibm.hpp"  // immersed-boundary helpers of the reference (host side, optional)
-#endif
+#include "ibm.hpp"
 #if __has_include("wall_functions.hpp")
 #include "wall_functions.hpp"
 #endif

@@ -318,6 +318,16 @@ struct LBMCapabilities {
                (!thermal || (use_thermal && g_thermal.stale()));
     }
     lbm2d_solver* device_handle() const { return h_; }
+    // Immersed-boundary points whose direct forcing the device applies
+    // around every step (lbm2d_dropin::attach_ibm); sent with the next step.
+    void set_ibm_points(std::vector<double> X, std::vector<double> Y, double dt, double uwx, double uwy) {
+        ibm_X_ = std::move(X);
+        ibm_Y_ = std::move(Y);
+        ibm_dt_ = dt;
+        ibm_uwx_ = uwx;
+        ibm_uwy_ = uwy;
+        ibm_dirty_ = true;
+    }
 
    private:
     void ensure_handle();
@@ -333,6 +343,9 @@ struct LBMCapabilities {
     std::vector<std::pair<double, double>> sent_poly_;
     bool sent_is_poly_ = false, sent_moving_ = false, sent_mei_ = true;
     double sent_omega_ = 0, sent_rcx_ = 0, sent_rcy_ = 0;
+    std::vector<double> ibm_X_, ibm_Y_;
+    double ibm_dt_ = 1.0, ibm_uwx_ = 0.0, ibm_uwy_ = 0.0;
+    bool ibm_dirty_ = false;
 };
 
 inline void LBMCapabilities::ensure_handle() {
@@ -399,6 +412,12 @@ inline void LBMCapabilities::push_settings() {
     if (g_thermal.dirty() || (step_version_ == 0 && use_thermal)) {
         check(lbm2d_upload_g(h_, g_thermal.raw().data()), h_, "upload g");
         g_thermal.clear_dirty();
+    }
+    if (ibm_dirty_) {
+        check(lbm2d_set_ibm(h_, ibm_X_.data(), ibm_Y_.data(), static_cast<int>(ibm_X_.size()), ibm_dt_, ibm_uwx_,
+                            ibm_uwy_),
+              h_, "immersed boundary");
+        ibm_dirty_ = false;
     }
 }
 

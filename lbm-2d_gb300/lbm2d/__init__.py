@@ -153,6 +153,9 @@ _SIGS = {
     "lbm2d_naca_coords": ([_I, _I, _DP], _I),
     "lbm2d_transform_points": ([_DP, _I, _D, _D, _D, _D], _I),
     "lbm2d_wall_distance": ([_I, _I, _U8P, _DP], _I),
+    "lbm2d_ibm_points_from_polygon": ([_DP, _I, _D, _DP, _DP, _I], _I),
+    "lbm2d_set_ibm": ([_P, _DP, _DP, _I, _D, _D, _D], _I),
+    "lbm2d_ibm_lagrangian": ([_P, _DP, _DP, _DP, _DP], _I),
     "lbm2d_force_stats": ([_DP, _DP, _I, _D, C.POINTER(ForceStats)], _I),
     "lbm2d_boundary_links": ([_I, _I, _I, _U8P, C.POINTER(BBGeometry), _I, C.POINTER(C.c_int32),
                               C.POINTER(C.c_int8), C.POINTER(C.c_int8), _DP, _DP, _DP,
@@ -246,6 +249,17 @@ def wall_distance(nx, ny, mask) -> np.ndarray:
     return out
 
 
+def ibm_points_from_polygon(xy, spacing=1.0) -> np.ndarray:
+    """Lagrangian points of ImmersedBoundary::build_from_polygon as an (n, 2)
+    array."""
+    a = np.ascontiguousarray(xy, np.float64).reshape(-1)
+    L = lib()
+    n = L.lbm2d_ibm_points_from_polygon(_d(a), len(a) // 2, float(spacing), None, None, 0)
+    X, Y = np.zeros(n), np.zeros(n)
+    L.lbm2d_ibm_points_from_polygon(_d(a), len(a) // 2, float(spacing), _d(X), _d(Y), n)
+    return np.stack([X, Y], 1)
+
+
 def boundary_links(nx, ny, case_type, mask, cylinder=None, polygon=None, moving_wall=None) -> dict:
     """The reference's bounce-back link list for a mask (see include/lbm2d.h)."""
     m = np.ascontiguousarray(mask, np.uint8).reshape(-1)
@@ -296,6 +310,7 @@ class Solver:
         self.nx, self.ny = nx, ny
         self.storage = storage
         self._mask = np.zeros(nx * ny, np.uint8)
+        self._ibm_n = 0
 
     # -- plumbing
     def _ck(self, rc):
@@ -459,6 +474,23 @@ class Solver:
         T = np.empty(n) if thermal else None
         self._ck(self.L.lbm2d_download_macros(self.h, _d(rho), _d(u), _d(v), _d(T) if thermal else None))
         return (rho, u, v, T) if thermal else (rho, u, v)
+
+    def set_ibm(self, points, dt=1.0, u_wall=(0.0, 0.0)):
+        """Immersed-boundary direct forcing around every step at the (n, 2)
+        Lagrangian points (the airfoil driver's loop); an empty array
+        removes it."""
+        pts = np.ascontiguousarray(points, np.float64).reshape(-1, 2)
+        X, Y = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+        self._ibm_n = len(X)
+        self._ck(self.L.lbm2d_set_ibm(self.h, _d(X), _d(Y), len(X), float(dt), float(u_wall[0]),
+                                      float(u_wall[1])))
+
+    def ibm_lagrangian(self):
+        """(U, V, FX, FY) at the points: the values that produced the forcing
+        of the last step."""
+        out = [np.zeros(self._ibm_n) for _ in range(4)]
+        self._ck(self.L.lbm2d_ibm_lagrangian(self.h, *(_d(a) for a in out)))
+        return tuple(out)
 
     def frame_fields(self, ds, sanitize=True, T_wall=0.0):
         """Fields of the reference's frame writers at nodes (i*ds, j*ds),

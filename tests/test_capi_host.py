@@ -51,6 +51,23 @@ def test_equilibrium_and_geometry_kats(product):
     assert np.array_equal(np.array(pip, np.uint8), kat["pip"])
 
 
+@pytest.mark.parametrize("name", sorted(CS.IBM_CASES))
+def test_ibm_points_and_airfoil_mask_bit_exact(product, name):
+    """Lagrangian points (ImmersedBoundary::build_from_polygon) and the
+    airfoil's point-in-polygon mask equal the reference's."""
+    spec = CS.IBM_CASES[name]
+    gold = np.load(os.path.join(GOLD, f"{name}.npz"))
+    nx, ny = spec["nx"], spec["ny"]
+    poly = product.transform_points(product.naca_coords(spec["naca"], spec["npts"]), nx / 4, ny / 2, ny / 3.0,
+                                    spec["aoa"])
+    assert np.array_equal(poly, gold["poly"])
+    assert np.array_equal(product.ibm_points_from_polygon(poly, spec["spacing"]), gold["points"])
+    m = np.zeros(nx * ny, np.uint8)
+    product.lib().lbm2d_mask_polygon(nx, ny, product._u8(m), product._d(np.ascontiguousarray(poly.reshape(-1))),
+                                     len(poly))
+    assert np.array_equal(m, gold["mask"])
+
+
 @pytest.mark.parametrize("name", sorted(CS.CASES))
 def test_masks_bit_exact_with_reference(product, name):
     """Masks made by the product's place_* helpers equal the reference's."""
