@@ -570,15 +570,19 @@ def run_ibm(args):
     import lbm2d
     lbm2d.build(quiet=True)
     out = {}
-    for nx, ny in ((800, 300), (4096, 1536)):
+    # default: the driver's grid and a large one; --nx/--ny pick one size and
+    # --steps/--warmup its step counts (a short case for profiling)
+    custom = (args.nx, args.ny) != (NX, NY)
+    sizes = [(args.nx, args.ny)] if custom else [(800, 300), (4096, 1536)]
+    for nx, ny in sizes:
         row = {}
         for label, ibm in (("plain", False), ("ibm", True)):
             s, tau, pts, _, _ = _airfoil_solver(lbm2d, nx, ny, "fp32", ibm=ibm)
             stream = torch.cuda.ExternalStream(s.stream)
-            s.step(tau, 0.1, 20)
+            s.step(tau, 0.1, args.warmup if custom else 20)
             s.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            steps = 2000 if nx * ny < 1 << 20 else 500
+            steps = args.steps if custom else (2000 if nx * ny < 1 << 20 else 500)
             l0 = s.launches
             e0.record(stream)
             s.step(tau, 0.1, steps)
