@@ -52,7 +52,7 @@ struct lbm2d_batch {
     std::vector<Member> members;
     std::vector<Group> groups;
     bool layout_dirty = true;
-    int bx = 128, by = 2;
+    int bx = 32, by = 4;  // one-warp-wide blocks (64 nodes for the paired kernel)
     // host staging (pinned) for parameters and budgets
     KParams* h_params = nullptr;
     size_t h_params_cap = 0;
@@ -454,9 +454,9 @@ int lbm2d_batch_synchronize(lbm2d_batch* b) {
 
 int lbm2d_batch_set_block(lbm2d_batch* b, int bx, int by) {
     if (!b) return LBM2D_ERR_INVALID;
-    if (bx == 0 && by == 0) {
-        bx = 128;
-        by = 2;
+    if (bx == 0 && by == 0) {  // the default: narrow blocks for mixes of small grids
+        bx = 32;
+        by = 4;
     }
     if (bx <= 0 || by <= 0 || bx * by > 512 || (bx * by) % 32 != 0)
         return bfail(b, LBM2D_ERR_INVALID, "block must have a multiple of 32 threads, at most 512");

@@ -352,9 +352,9 @@ int lbm2d_server_create(int device, double budget_bytes, int max_active, int ste
     s->max_active = max_active;
     s->steps_per_tick = steps_per_tick;
     int rc = lbm2d_batch_create(device, &s->batch);
-    // narrow blocks (128 nodes wide): a serving mix holds many small grids
-    // (measured 3.5% faster than 256-node-wide blocks on the 200-request mix)
-    if (!rc) rc = lbm2d_batch_set_block(s->batch, 64, 4);
+    // narrow blocks: a serving mix holds many small grids, and a block that
+    // overhangs a grid's right edge idles its overhanging threads
+    if (!rc) rc = lbm2d_batch_set_block(s->batch, 32, 4);
     if (rc) {
         delete s;
         return rc;
