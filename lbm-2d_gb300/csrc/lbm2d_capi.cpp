@@ -307,6 +307,14 @@ int ensure_slots(lbm2d_solver* h) {
     if ((rc = dalloc(h, &h->d_partials, (size_t)std::max(h->nslots, 1) * 2 * sizeof(double)))) return rc;
     CK(cudaMemcpyAsync(h->d_block_slot, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream),
        "slots H2D");
+    // arrival count of the fused second stage (blocks holding slots)
+    h->red_blocks = 0;
+    for (int s : slots)
+        if (s >= 0) ++h->red_blocks;
+    if (!h->d_red_done) {
+        if ((rc = dalloc(h, &h->d_red_done, sizeof(unsigned int)))) return rc;
+        CK(cudaMemsetAsync(h->d_red_done, 0, sizeof(unsigned int), h->stream), "reduction count");
+    }
     CK(cudaStreamSynchronize(h->stream), "slots");
     h->slot_bx = h->bx;
     h->slot_by = h->by;
@@ -519,7 +527,7 @@ int lbm2d_destroy(lbm2d_solver* h) {
     void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
                     h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
                     h->d_counter, h->d_last, h->d_nan, h->d_seed, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
-                    h->d_diag, h->d_prev_uv};
+                    h->d_diag, h->d_prev_uv, h->d_red_done};
     for (void* b : bufs)
         if (b) cudaFreeAsync(b, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -702,13 +710,25 @@ int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0 = nullptr, cudaE
     p.seed_in = h->d_seed + h->cur;
     p.seed_out = h->d_seed + (h->cur ^ 1);
     p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
+    // the drag/lift second stage runs in the step launch's last force block
+    // when every block has the 128 threads it needs (the row pipeline has 256
+    // consumers); otherwise in its own launch
+    const bool fused = h->nslots > 0 && h->red_blocks > 0 &&
+                       (h->slot_kind == KERNEL_ROWS || h->bx * h->by >= 128);
+    p.red_done = fused ? h->d_red_done : nullptr;
+    p.red_hist = h->d_hist;
+    p.red_counter = h->d_counter;
+    p.red_last = h->d_last;
+    p.red_blocks = h->red_blocks;
+    p.red_nslots = h->nslots;
+    p.red_cap = h->hist_cap;
     if (e0) CK(cudaEventRecord(e0, h->stream), "event");
     int e = h->slot_kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
                                         : launch_step(h->storage, p, h->bx, h->by, h->stream);
     if (e1) CK(cudaEventRecord(e1, h->stream), "event");
     ++h->launches;
     if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
-    if (h->nslots > 0) {
+    if (h->nslots > 0 && !fused) {
         e = launch_force_reduce(h->d_partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last, h->stream);
         ++h->launches;
         if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");

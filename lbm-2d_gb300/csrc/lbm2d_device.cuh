@@ -727,6 +727,79 @@ __device__ __forceinline__ void block_reduce2(double& a, double& b) {
     }
 }
 
+// Second stage of the drag/lift reduction in a fixed order that does not
+// depend on the reducing block's shape: 128 lanes, lane t adds slots t,
+// t + 128, ... in order; each of the four warps folds its lanes with the same
+// shuffle tree; the four warp sums are added in warp order.  Every thread of
+// the calling group calls it (threads 0..127 add), `sync` is the group's
+// barrier, and the sums land in thread 0.  Partials are read through L2:
+// other blocks of the same launch may have written them.
+template <class Sync>
+__device__ __forceinline__ void sum_slots128(const double* part, int nslots, int t, double* w8, Sync sync, double& a,
+                                             double& b) {
+    a = 0.0;
+    b = 0.0;
+    if (t < 128) {
+        for (int k = t; k < nslots; k += 128) {
+            a += __ldcg(part + 2 * k);
+            b += __ldcg(part + 2 * k + 1);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if ((t & 31) == 0) {
+            w8[2 * (t >> 5)] = a;
+            w8[2 * (t >> 5) + 1] = b;
+        }
+    }
+    sync();
+    if (t == 0) {
+        a = ((w8[0] + w8[2]) + w8[4]) + w8[6];
+        b = ((w8[1] + w8[3]) + w8[5]) + w8[7];
+    }
+}
+
+// One step's sums appended to the force history (while it has room) and kept
+// as the last pair.
+__device__ __forceinline__ void record_forces(double* hist, int cap, unsigned long long* counter, double* last,
+                                              double a, double b) {
+    const unsigned long long k = *counter;
+    if (k < (unsigned long long)cap) {
+        hist[2 * k] = a;
+        hist[2 * k + 1] = b;
+    }
+    last[0] = a;
+    last[1] = b;
+    *counter = k + 1;
+}
+
+// The fused second stage, for a block that has written its force partials:
+// every thread of the block (or of the consumer group, `sync` being its
+// barrier, at least 128 threads) calls it after its writes.  The writes are
+// made visible device-wide before the block counts itself; the last block to
+// count sums all slots and resets the count for the next launch.  No thread
+// waits on another block.
+template <class Sync>
+__device__ __forceinline__ void fused_force_finish(const KParams& p, int tid, Sync sync) {
+    __shared__ unsigned int s_last;
+    __shared__ double s_w8[8];
+    __threadfence();
+    sync();
+    if (tid == 0) s_last = atomicAdd(p.red_done, 1u) == (unsigned int)(p.red_blocks - 1) ? 1u : 0u;
+    sync();
+    if (s_last) {
+        __threadfence();
+        double a, b;
+        sum_slots128(p.partials, p.red_nslots, tid, s_w8, sync, a, b);
+        if (tid == 0) {
+            record_forces(p.red_hist, p.red_cap, p.red_counter, p.red_last, a, b);
+            *p.red_done = 0u;
+        }
+    }
+}
+
 // ----------------------------------------------------------------- kernels
 // One step of the block (bxi, byi) of an instance whose block grid is gx wide.
 template <class T, bool TH>
@@ -811,6 +884,7 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
                 p.partials[2 * slot] = double(a);
                 p.partials[2 * slot + 1] = double(b);
             }
+            if (p.red_done) fused_force_finish(p, tid, [] { __syncthreads(); });
         }
     }
 }

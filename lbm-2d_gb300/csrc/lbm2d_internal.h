@@ -106,6 +106,15 @@ struct KParams {
     // per band node whose forcing the current state carries
     const int* ibm_band;
     const double* ibm_F;
+    // drag/lift second stage fused into a single-instance step launch (null:
+    // a separate reduction launch).  The blocks that hold force slots count
+    // themselves in red_done; the last to arrive sums every slot in the fixed
+    // order of sum_slots128, records the sums and resets the count.
+    unsigned int* red_done;
+    double* red_hist;
+    unsigned long long* red_counter;
+    double* red_last;
+    int red_blocks, red_nslots, red_cap, red_pad;
 };
 static_assert(sizeof(KParams) % 16 == 0, "KParams is staged with 16-byte copies");
 

@@ -105,6 +105,7 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
                 p.partials[2 * slot] = double(a);
                 p.partials[2 * slot + 1] = double(b);
             }
+            if (p.red_done) fused_force_finish(p, tid, [] { __syncthreads(); });
         }
     }
 }
@@ -652,24 +653,14 @@ __global__ void prologue_pair_kernel(const KParams p, const double* __restrict__
 
 // Deterministic second stage of the force reduction: one block sums the
 // per-block partials in a fixed order and appends (fx, fy) to the history.
+// Launched with 128 threads: the same fixed-order sum as the fused form, so
+// both give the same bits for the same partials.
 __global__ void force_reduce_kernel(const double* __restrict__ part, int nslots, double* hist, int cap,
                                     unsigned long long* counter, double* last) {
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < nslots; k += blockDim.x) {
-        a += part[2 * k];
-        b += part[2 * k + 1];
-    }
-    block_reduce2(a, b);
-    if (threadIdx.x == 0) {
-        const unsigned long long k = *counter;
-        if (k < (unsigned long long)cap) {
-            hist[2 * k] = a;
-            hist[2 * k + 1] = b;
-        }
-        last[0] = a;
-        last[1] = b;
-        *counter = k + 1;
-    }
+    __shared__ double w8[8];
+    double a, b;
+    sum_slots128(part, nslots, threadIdx.x, w8, [] { __syncthreads(); }, a, b);
+    if (threadIdx.x == 0) record_forces(hist, cap, counter, last, a, b);
 }
 
 // Force reduction of several instances: block b reduces job b.
@@ -902,7 +893,7 @@ int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, dou
 
 int launch_force_reduce(const double* partials, int nslots, double* hist, int cap, unsigned long long* counter,
                         double* last, void* stream) {
-    force_reduce_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(partials, nslots, hist, cap, counter,
+    force_reduce_kernel<<<1, 128, 0, static_cast<cudaStream_t>(stream)>>>(partials, nslots, hist, cap, counter,
                                                                            last);
     return (int)cudaGetLastError();
 }

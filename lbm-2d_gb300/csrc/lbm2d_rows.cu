@@ -384,11 +384,16 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
             ++y;
         }
     }
-    if (force && lane == 0) {
-        const int base = p.block_slot[blockIdx.x];
+    if (force) {
+        const int base = p.block_slot[blockIdx.x];  // uniform per CTA
         if (base >= 0) {
-            p.partials[2 * (base + warp)] = acc[2 * warp];
-            p.partials[2 * (base + warp) + 1] = acc[2 * warp + 1];
+            if (lane == 0) {
+                p.partials[2 * (base + warp)] = acc[2 * warp];
+                p.partials[2 * (base + warp) + 1] = acc[2 * warp + 1];
+            }
+            // the producer warp has left: the consumers' own named barrier
+            if (p.red_done)
+                fused_force_finish(p, warp * 32 + lane, [] { asm volatile("bar.sync 1, 256;" ::: "memory"); });
         }
     }
 }

@@ -72,6 +72,8 @@ struct lbm2d_solver {
     double* d_rec_uw = nullptr;
     double* d_partials = nullptr;
     int* d_block_slot = nullptr;
+    unsigned int* d_red_done = nullptr;  // arrivals of the fused force reduction
+    int red_blocks = 0;                  // blocks (CTAs) that hold force slots
     int nslots = 0, slot_bx = 0, slot_by = 0, slot_kind = -1, slot_grid = 0;
     double* d_hist = nullptr;
     int hist_cap = 1 << 18;
