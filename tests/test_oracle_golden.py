@@ -129,3 +129,38 @@ def test_mass_conservation_10_steps(oracle_lib):
     m1 = s.f.reshape(-1, 9)[fluid].sum()
     s.close()
     assert abs(m1 - m0) < 0.01 * m0
+
+
+def test_oracle_long_setups_match_reference(oracle_lib):
+    """The full-length fixtures (tests/golden/make_long_golden.py): the
+    restatement reproduces their masks, the cylinder driver's seeded initial
+    state (SHA-256 of the populations), the first 300 drag/lift sums of the
+    cylinder wake and the cavity's total mass after 1000 steps, bit for bit."""
+    import hashlib
+
+    import make_long_golden as LG
+    O = oracle_lib
+    c = LG.CYLINDER_LONG
+    gold = np.load(os.path.join(GOLD, "long_cylinder_800x300.npz"))
+    s = O.Solver(c["nx"], c["ny"], "oracle")
+    s.set_case(CS.CYLINDER, CS.MRT)
+    s.place_cylinder(c["cx"], c["cy"], c["r"])
+    s.init_cylinder_wake(c["u"], c["cx"], c["seed"], c["amp"])
+    assert np.array_equal(s.obstacle, gold["mask"])
+    assert hashlib.sha256(s.f.tobytes()).hexdigest() == str(gold["f0_sha"])
+    sums = []
+    for _ in range(300):
+        s.step(c["tau"], c["u"])
+        sums.append(s.force_sums())
+    s.close()
+    assert np.array_equal(np.array(sums), gold["sums_head"][:300])
+    c = LG.CAVITY_LONG
+    gold = np.load(os.path.join(GOLD, "long_cavity_800x300.npz"))
+    s = O.Solver(c["nx"], c["ny"], "oracle")
+    s.set_case(CS.CAVITY, CS.MRT)
+    s.place_walls()
+    s.init_uniform(1.0, 0.0, 0.0)
+    assert np.array_equal(s.obstacle, gold["mask"])
+    s.step(c["tau"], c["u"], n=c["every"])
+    assert float(s.f.sum()) == float(gold["mass"][0])
+    s.close()
