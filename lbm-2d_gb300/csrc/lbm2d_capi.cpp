@@ -497,8 +497,13 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
     if (!rc) rc = dalloc(h, &h->d_nan, 16);
     if (!rc) rc = dalloc(h, &h->d_seed, 16);
     if (!rc) rc = dalloc(h, &h->d_counter, 16);
-    if (!rc) rc = dalloc(h, &h->d_last, 16);
-    if (!rc && cudaMallocHost(&h->h_last, 2 * sizeof(double)) != cudaSuccess) rc = LBM2D_ERR_CUDA;
+    // The last step's drag/lift lives in mapped pinned memory: the kernel that
+    // records it writes straight to the host, so a read needs no copy.
+    if (!rc && (cudaHostAlloc(&h->h_last, 2 * sizeof(double), cudaHostAllocMapped | cudaHostAllocPortable) !=
+                    cudaSuccess ||
+                cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->d_last), h->h_last, 0) != cudaSuccess))
+        rc = fail(h, LBM2D_ERR_CUDA, "mapped force buffer");
+    if (!rc) h->h_last[0] = h->h_last[1] = 0.0;
     if (!rc) rc = dalloc(h, &h->d_hist, (size_t)h->hist_cap * 2 * sizeof(double));
     if (!rc) rc = ensure_stage(h, false);
     if (!rc) rc = ensure_populations(h);
@@ -506,7 +511,6 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
         cudaMemsetAsync(h->d_nan, 0, 16, h->stream);
         cudaMemsetAsync(h->d_seed, 0, 16, h->stream);
         cudaMemsetAsync(h->d_counter, 0, 16, h->stream);
-        cudaMemsetAsync(h->d_last, 0, 16, h->stream);
         if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = LBM2D_ERR_CUDA;
     }
     if (rc) {
@@ -526,13 +530,13 @@ int lbm2d_destroy(lbm2d_solver* h) {
     ibm_release(h);
     void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
                     h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
-                    h->d_counter, h->d_last, h->d_nan, h->d_seed, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
+                    h->d_counter, h->d_nan, h->d_seed, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
                     h->d_diag, h->d_prev_uv, h->d_red_done};
     for (void* b : bufs)
         if (b) cudaFreeAsync(b, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
-    if (h->h_last) cudaFreeHost(h->h_last);
+    if (h->h_last) cudaFreeHost(h->h_last);  // d_last is its device alias
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LBM2D_OK;
@@ -877,8 +881,8 @@ int lbm2d_synchronize(lbm2d_solver* h) {
 int lbm2d_force_sums(lbm2d_solver* h, double* fx, double* fy) {
     int rc;
     if ((rc = check_handle(h))) return rc;
-    // into pinned memory: a direct copy, no staging through a bounce buffer
-    CK(cudaMemcpyAsync(h->h_last, h->d_last, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "force D2H");
+    // the recording kernel wrote the sums into mapped host memory: once the
+    // stream has drained they are here, with no copy
     CK(cudaStreamSynchronize(h->stream), "force sync");
     if (fx) *fx = h->h_last[0];
     if (fy) *fy = h->h_last[1];

@@ -78,8 +78,8 @@ struct lbm2d_solver {
     double* d_hist = nullptr;
     int hist_cap = 1 << 18;
     unsigned long long* d_counter = nullptr;
-    double* d_last = nullptr;
-    double* h_last = nullptr;  // pinned host copy of the last (Fx, Fy)
+    double* d_last = nullptr;  // device alias of h_last
+    double* h_last = nullptr;  // last (Fx, Fy): mapped pinned memory the kernels write
     unsigned int* d_nan = nullptr;
     uint32_t* d_seed = nullptr;  // rounding-noise seed words, one per population buffer
     double* d_stage_f = nullptr;
