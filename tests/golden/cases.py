@@ -61,10 +61,12 @@ def channel_circles_mask(nx, ny, n_circles, rmin, rmax, seed):
         cy = int(rng.integers(r + 3, ny - r - 3))
         if all((cx - a) ** 2 + (cy - b) ** 2 > (r + c + 3) ** 2 for a, b, c in circles):
             circles.append((cx, cy, r))
-    yy, xx = np.mgrid[0:ny, 0:nx]
     for cx, cy, r in circles:
+        # only the circle's bounding box can hold nodes with d < r
+        y0, y1, x0, x1 = max(cy - r, 0), min(cy + r + 1, ny), max(cx - r, 0), min(cx + r + 1, nx)
+        yy, xx = np.mgrid[y0:y1, x0:x1]
         d = np.sqrt(((xx - cx).astype(np.float64)) ** 2 + ((yy - cy).astype(np.float64)) ** 2)
-        m[d < r] = 1
+        m[y0:y1, x0:x1][d < r] = 1
     return m.reshape(-1), circles
 
 
