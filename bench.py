@@ -195,13 +195,30 @@ def time_e2e(lbm2d, s, torch, steps, f0_pinned, fout_pinned):
     return (t1 - t0) * 1e3, s.launches - l0
 
 
-def _oracle_channel(size):
+def _cpu_impl():
+    """Which CPU implementation of the reference step times the CPU legs: the
+    reference's own headers compiled here (oracle/_ref, kind "reference")
+    when that build exists and loads on this host, else the C restatement
+    (kind "port")."""
+    from oracle import oracle as O
+    if os.path.exists(O.LIB_REF):
+        try:
+            O.Solver(8, 8, "ref").close()
+            return "ref", "reference", "the reference's src/lbm.hpp step compiled by oracle/Makefile (OpenMP)"
+        except OSError:
+            pass
+    if not os.path.exists(O.LIB_ORACLE):
+        O.build()
+    return "oracle", "port", "oracle/lbm_oracle.c (OpenMP restatement of the reference step)"
+
+
+def _oracle_channel(size, kind="oracle"):
     from oracle import oracle as O
     if not os.path.exists(O.LIB_ORACLE):
         O.build()
     nc = max(1, int(round(N_CIRCLES * (size * size) / (NX * NY))))
     mask, _ = CS.channel_circles_mask(size, size, nc, RMIN, RMAX, SEED)
-    s = O.Solver(size, size)
+    s = O.Solver(size, size, kind)
     s.set_case(O.RIBS, O.MRT, True, CS_LES)
     s.obstacle[:] = mask
     s.set_body_force(BODY_FORCE)
@@ -214,7 +231,8 @@ def cpu_sample(size: int = 1024, budget_s: float = 12.0, max_steps: int = 50):
     per-step wall-distance sweep under LES) on a bounded sample of the
     workload: the same generator and physics at size x size, circles scaled
     by area; steps are timed until about `budget_s` of CPU work."""
-    s, nc = _oracle_channel(size)
+    kind, _, _ = _cpu_impl()
+    s, nc = _oracle_channel(size, kind)
     s.step(TAU, U0)  # warm-up
     n, t0 = 0, time.perf_counter()
     while n < max_steps and (time.perf_counter() - t0) < budget_s:
@@ -231,7 +249,8 @@ def run_reference(args):
         return 0
     cores = os.cpu_count() or 1
     size = args.cpu_size
-    s, nc = _oracle_channel(size)
+    kind, ckind, what = _cpu_impl()
+    s, nc = _oracle_channel(size, kind)
     for _ in range(min(args.warmup, 1)):
         s.step(TAU, U0)
     per = []
@@ -253,9 +272,9 @@ def run_reference(args):
         "config": {"workload": workload_name(args.nx, args.ny),
                    "sample": f"{size}x{size} with {nc} circles (same generator and physics), "
                              f"{len(per)} of {args.steps} requested steps within {args.ref_budget:.0f} s"},
-        "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": "port",
-                         "sample": f"oracle/lbm_oracle.c (OpenMP restatement of the reference step incl. its "
-                                   f"per-step wall-distance sweep), {cores} threads, {size}x{size}, {len(per)} steps"},
+        "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": ckind,
+                         "sample": f"{what}, its per-step wall-distance sweep included, {cores} threads, "
+                                   f"{size}x{size}, {len(per)} steps"},
         "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -823,13 +842,14 @@ def main():
     if not args.no_cpu:
         try:
             cores = os.cpu_count() or 1
+            _, ckind, what = _cpu_impl()
             mlups, dt, nc, n = cpu_sample(args.cpu_size)
-            cpu = {"value": mlups / 1e3, "unit": "GLUPS", "cores": cores, "kind": "port",
-                   "sample": f"oracle/lbm_oracle.c (OpenMP restatement of the reference step, per-step "
-                             f"wall-distance sweep included), {cores} threads, same generator and physics at "
-                             f"{args.cpu_size}x{args.cpu_size} with {nc} circles, {n} steps in {dt:.1f} s"}
+            cpu = {"value": mlups / 1e3, "unit": "GLUPS", "cores": cores, "kind": ckind,
+                   "sample": f"{what}, per-step wall-distance sweep included, {cores} threads, same generator "
+                             f"and physics at {args.cpu_size}x{args.cpu_size} with {nc} circles, {n} steps in "
+                             f"{dt:.1f} s"}
         except Exception as ex:  # the CPU leg never blocks the GPU line
-            cpu = {"value": None, "unit": "GLUPS", "cores": os.cpu_count(), "kind": "port",
+            cpu = {"value": None, "unit": "GLUPS", "cores": os.cpu_count(), "kind": None,
                    "sample": f"failed: {ex}"}
     line = {
         "metric": "GLUPS (D2Q9 step, lattice updates/s) & %HBM roofline, FP32 vs FP16/BF16 storage",
