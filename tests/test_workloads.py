@@ -76,3 +76,21 @@ def test_serving_requests():
         if r["geometry"] == 3:
             assert 2.0 <= r["param"] <= 5.0
     assert B._c5_requests(200) == req
+
+
+def test_cpu_leg_picks_reference_build_or_port(oracle_lib, monkeypatch, tmp_path):
+    """The CPU legs time the reference's own compiled step when that build
+    loads on the host, and fall back to the restatement when it is missing
+    or cannot load (an x86 build on an Arm host)."""
+    import os
+
+    O = oracle_lib
+    if os.path.exists(O.LIB_REF):
+        assert B._cpu_impl()[:2] == ("ref", "reference")
+    monkeypatch.setattr(O, "LIB_REF", str(tmp_path / "missing.so"))
+    assert B._cpu_impl()[:2] == ("oracle", "port")
+    bad = tmp_path / "bad.so"
+    bad.write_bytes(b"not a shared object")
+    monkeypatch.setattr(O, "LIB_REF", str(bad))
+    monkeypatch.setattr(O, "_LIBS", {k: v for k, v in O._LIBS.items() if k == "oracle"})  # no cached load
+    assert B._cpu_impl()[:2] == ("oracle", "port")
