@@ -320,11 +320,16 @@ def _c5_requests(n, seed=11):
 
 
 def run_serve(args):
+    import lbm2d
+    lbm2d.build(quiet=True)
+    print(json.dumps(serve_block(args, lbm2d)), flush=True)
+    return 0
+
+
+def serve_block(args, lbm2d):
     """Poisson arrivals (rate --rate) of --requests solves through the serving
     loop, against the same requests solved one at a time with the plain
     per-solve API (lbm2d_step) on the same GPU."""
-    import lbm2d
-    lbm2d.build(quiet=True)
     reqs = _c5_requests(args.requests)
     scale = args.budget_scale  # scales every step budget (bounded run time)
     for r in reqs:
@@ -405,14 +410,14 @@ def run_serve(args):
                                  "+ drag/lift read-back")
         seq["bulk"]["note"] = "same, but one lbm2d_step call for each request's whole budget"
     line = {"metric": "serving: p50/p99 time-to-solution and aggregate GLUPS", "unit": "GLUPS",
-            "value": serve["glups"], "serve": serve, "sequential": seq or None,
+            "value": serve["glups"], "p50_s": serve["p50_s"], "p99_s": serve["p99_s"], "glups": serve["glups"],
+            "budget_scale": scale, "serve": serve, "sequential": seq or None,
             "speedup_vs_sequential_dropin": (serve["glups"] / seq["dropin"]["glups"]) if seq else None,
             "speedup_vs_sequential_bulk": (serve["glups"] / seq["bulk"]["glups"]) if seq else None,
             "config": {"workload": f"{len(reqs)} requests, Poisson {args.rate}/s, grids 128x64..2048x768, "
                                    f"{{cavity, step, cylinder, side-by-side}}, Re 50-2000, budgets 1k-50k x {scale}",
                        "storage": storage, "tick": args.tick, "budget_gb": args.serve_budget_gb}}
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def _plain_solver(lbm2d, r, storage):
@@ -475,15 +480,18 @@ def _plain_solver(lbm2d, r, storage):
 
 
 def run_batch(args):
-    """256 uneven solves stepped together (one packed launch per step per
-    storage group) against the same solves stepped one after another."""
-    import torch
-
     import lbm2d
     lbm2d.build(quiet=True)
+    print(json.dumps(batch_block(args, lbm2d, args.batch_storage, args.steps)), flush=True)
+    return 0
+
+
+def batch_block(args, lbm2d, storage, steps):
+    """256 uneven solves stepped together (one packed launch per step per
+    storage group) against the same solves stepped one after another, each
+    in one whole-budget call."""
+    import torch
     inst = _c4_instances(args.instances)
-    steps = args.steps
-    storage = args.batch_storage
     solvers = [_plain_solver(lbm2d, r, storage) for r in inst]
     nodes = sum(r["nx"] * r["ny"] for r in inst)
     # sequential: each solver alone, one after the other
@@ -515,19 +523,63 @@ def run_batch(args):
             s.synchronize()
         except lbm2d.LBMError:
             nan += 1
+    bytes_lu = sum(r["nx"] * r["ny"] * 18 * lbm2d.BYTES_PER_POP[storage] * (2 if r["geometry"] == 4 else 1)
+                   for r in inst) / nodes
+    peak, peak_kind = peaks()
+    glups = nodes * steps / t_bat / 1e9
     line = {"metric": "batched uneven solves: aggregate GLUPS", "unit": "GLUPS",
-            "value": nodes * steps / t_bat / 1e9, "sequential_glups": nodes * steps / t_seq / 1e9,
+            "value": glups, "glups": glups, "sequential_glups": nodes * steps / t_seq / 1e9,
             "speedup_vs_sequential": t_seq / t_bat, "steps": steps, "instances": len(inst), "nodes": nodes,
             "batch_launches": b.launches - l0, "diverged": nan,
             "thermal_instances": sum(1 for r in inst if r["geometry"] == 4),
+            "alg_bytes_per_update": bytes_lu, "roofline_frac": glups * bytes_lu / peak, "peak_kind": peak_kind,
             "config": {"workload": "256 uneven cavity/step/cylinder solves, sides log-uniform 64-1024, aspect 1-3, "
                                    "Re U[50,1000], u=0.1, 30% heated cavities (Pr 0.71, Ra<=1e5)",
-                       "storage": storage, "block": [b.L and 0, 0]}}
+                       "storage": storage,
+                       "sequential": "the same solves one after another, one lbm2d_step call per whole budget"}}
     b.close()
     for s in solvers:
         s.close()
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
+
+
+def thermal_block(lbm2d, torch, n=2048, steps=200, storages=("fp32", "fp16")):
+    """The thermal double-distribution step on its own: the heated-cavity
+    driver's set-up (src/thermal_cavity.cpp: walls all round, hot left and cold
+    right columns, adiabatic top and bottom rows, Boussinesq buoyancy at
+    Ra = 1e5, Pr 0.71, tau 0.8) on an n x n grid, device-timed over `steps`
+    steps of one multi-step call.  Bytes per update count both population
+    sets (FP32: 144 B, FP16: 72 B)."""
+    peak, peak_kind = peaks()
+    out = {}
+    for st in storages:
+        r = dict(nx=n, ny=n, geometry=4, re=0.0, param=1e5)
+        s = _plain_solver(lbm2d, r, st)
+        stream = torch.cuda.ExternalStream(s.stream)
+        s.step(s._tau, s._ubc, 20)
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = s.launches
+        e0.record(stream)
+        s.step(s._tau, s._ubc, steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        launches = s.launches - l0
+        diverged = False
+        try:
+            s.synchronize()
+        except lbm2d.LBMError:
+            diverged = True
+        kernel = KERNEL_NAMES[s.info().kernel][0]
+        s.close()
+        bpu = 2 * 2 * 9 * lbm2d.BYTES_PER_POP[st]
+        glups = n * n * steps / (ms * 1e-3) / 1e9
+        out[st] = {"glups": glups, "ms_per_step": ms / steps, "bytes_per_update": bpu,
+                   "achieved_gbs": glups * bpu, "roofline_frac": glups * bpu / peak, "kernel": kernel,
+                   "launches_per_step": launches / steps, "diverged": diverged}
+    return {"workload": f"heated cavity {n}x{n}, Ra 1e5, Pr 0.71, tau 0.8 (src/thermal_cavity.cpp set-up)",
+            "steps": steps, "peak_gbs": peak, "peak_kind": peak_kind, "results": out}
 
 
 def run_frame(args):
@@ -662,12 +714,17 @@ def run_ibm(args):
 
 
 def run_precision(args):
-    """Error of FP32 / FP16 / BF16 storage against an FP64 run of the same
-    kernel on the channel workload: relative L2 of the velocity field over
-    fluid nodes and relative error of the mean drag over the run."""
     import lbm2d
     lbm2d.build(quiet=True)
-    nx, ny, steps = args.nx, args.ny, args.steps
+    print(json.dumps(precision_block(lbm2d, args.nx, args.ny, args.steps)), flush=True)
+    return 0
+
+
+def precision_block(lbm2d, nx, ny, steps):
+    """Error of FP32 / FP16 / BF16 storage against an FP64 run of the same
+    kernel on the channel workload: relative L2 of the velocity field over
+    fluid nodes and relative error of the mean drag over the second half of
+    the run."""
     mask, circles = make_geometry(nx, ny)
     fluid = mask == 0
     out = {}
@@ -688,12 +745,10 @@ def run_precision(args):
                      np.sum(ref[0][fluid] ** 2 + ref[1][fluid] ** 2))
         drag_ref = float(np.mean(ref[2][steps // 2:]))
         drag = float(np.mean(fx[steps // 2:]))
-        out[st] = {"velocity_rel_l2": float(du), "drag_rel_err": abs(drag - drag_ref) / abs(drag_ref),
+        out[st] = {"velocity_rel_l2_vs_fp64": float(du), "drag_rel_err_vs_fp64": abs(drag - drag_ref) / abs(drag_ref),
                    "drag": drag, "drag_fp64": drag_ref}
-    line = {"metric": "storage precision vs FP64 (same kernel)", "config": {"workload": workload_name(nx, ny),
+    return {"metric": "storage precision vs FP64 (same kernel)", "config": {"workload": workload_name(nx, ny),
             "steps": steps}, "results": out}
-    print(json.dumps(line), flush=True)
-    return 0
 
 
 def main():
@@ -718,12 +773,17 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=200.0)
-    ap.add_argument("--budget-scale", type=float, default=0.1)
+    ap.add_argument("--budget-scale", type=float, default=1.0)
     ap.add_argument("--serve-storage", default="fp16")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--max-active", type=int, default=512)
     ap.add_argument("--tick", type=int, default=200)
     ap.add_argument("--no-sequential", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the precision, thermal, batch and serving blocks of the default line")
+    ap.add_argument("--precision-steps", type=int, default=1000)
+    ap.add_argument("--batch-steps", type=int, default=5000)
+    ap.add_argument("--thermal-n", type=int, default=2048)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -872,6 +932,18 @@ def main():
         "cpu_baseline": cpu,
         "drag_lift": r0.get("force"),
     }
+    if world == 1 and not args.no_extras:
+        # the other rows of the metric, on the same GPU after the timed step:
+        # storage error against FP64, the thermal step, the C4 batch and the
+        # C5 serving stream
+        pe = precision_block(lbm2d, nx, ny, args.precision_steps)
+        line["precision_vs_fp64"] = pe
+        for st, res in pe["results"].items():
+            if st in prec:
+                prec[st].update({k: res[k] for k in ("velocity_rel_l2_vs_fp64", "drag_rel_err_vs_fp64")})
+        line["thermal"] = thermal_block(lbm2d, torch, args.thermal_n)
+        line["batch"] = {st: batch_block(args, lbm2d, st, args.batch_steps) for st in ("fp32", "fp16")}
+        line["serving"] = serve_block(args, lbm2d)
     print(json.dumps(line), flush=True)
     reps.close()
     return 0

@@ -243,6 +243,13 @@ int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
  * 2: two x-neighbours per thread where nx is even.  Same results to
  * rounding; lbm2d_get_info reports the kernel in use. */
 int lbm2d_set_kernel_variant(lbm2d_solver *h, int variant);
+/* Limit, in SM cycles, of the row pipeline's consumer-side waits for its
+ * staged tiles (0, the default: about one second).  A wait that runs out
+ * makes the kernel stop early and the next lbm2d_synchronize report
+ * LBM2D_ERR_TIMEOUT, with the context still usable; a limit of a few cycles
+ * exercises that path on purpose (failure-path tests).  The producer's own
+ * waits keep the default.  No counterpart in the reference. */
+int lbm2d_set_wait_limit(lbm2d_solver *h, long long cycles);
 /* The CUDA stream the handle launches on (cudaStream_t as void*). */
 void *lbm2d_stream(lbm2d_solver *h);
 /* Count of kernel launches made by this handle since creation. */
@@ -263,10 +270,13 @@ int lbm2d_profile(lbm2d_solver *h, double *step_kernel_ms, long long *n_launches
  * prior lbm2d_step with the same tau and settings (else LBM2D_ERR_STATE);
  * the force-reduction scratch is a fixed 2 MiB array inside the library
  * (at most 131072 per-warp force slots, else LBM2D_ERR_INVALID), held on
- * every GPU that loads the library until the process exits.  The first call
- * on a device looks the array's address up (cudaGetSymbolAddress); make that
- * first call before any stream capture.  All callers share the array: calls
- * that overlap on the GPU (e.g. two solvers on different streams) race. */
+ * every GPU that loads the library until the process exits.  The preparing
+ * lbm2d_step looks the array's address up on its device (once per device,
+ * cudaGetSymbolAddress), so the first lbm2d_step_noalloc call needs no set-up
+ * of its own; it launches the same kernels as lbm2d_step.  It refuses to run
+ * while profiling is on (LBM2D_ERR_STATE).  All callers share the array:
+ * calls that overlap on the GPU (e.g. two solvers on different streams) race
+ * and corrupt each other's drag/lift; serialize them on one stream. */
 int lbm2d_step_noalloc(lbm2d_solver *h, double tau, double u_inflow, int nsteps);
 
 /* Device-resident variants for callers that keep populations on the GPU:
@@ -355,6 +365,15 @@ typedef struct lbm2d_server_stats_t {
 typedef struct lbm2d_server lbm2d_server;
 int lbm2d_server_create(int device, double budget_bytes, int max_active, int steps_per_tick, lbm2d_server **out);
 int lbm2d_server_submit(lbm2d_server *s, const lbm2d_request *r, long long *id);
+/* lbm2d_server_submit with caller state: f_init (may be NULL) is the
+ * request's initial population field, FP64 AoS [nx*ny*9], copied before the
+ * call returns and uploaded in place of the geometry's equilibrium start;
+ * f_out / g_out (may be NULL; g_out only for LBM2D_GEOM_HEATED_CAVITY)
+ * receive the final populations / temperature populations when the request
+ * retires (also when it diverged), before its result is reported -- the
+ * buffers must stay valid until then.  No counterpart in the reference. */
+int lbm2d_server_submit_state(lbm2d_server *s, const lbm2d_request *r, const double *f_init, double *f_out,
+                              double *g_out, long long *id);
 /* Block until at least n_finished requests are done (or timeout). */
 int lbm2d_server_wait(lbm2d_server *s, long long n_finished, double timeout_s);
 int lbm2d_server_results(lbm2d_server *s, lbm2d_result *out, int capacity, int *count);

@@ -122,6 +122,7 @@ KParams base_params(const lbm2d_solver* h) {
     p.pd.T_ref = h->T_ref;
     p.pf.T_ref = float(h->T_ref);
     p.nan_flag = h->d_nan;
+    p.consumer_wait = h->consumer_wait;
     p.pair = use_pair(h) ? 1 : 0;
     const int nbw = h->bx * (p.pair ? 2 : 1);  // node width of a block
     p.gx = (h->nx + nbw - 1) / nbw;
@@ -410,6 +411,9 @@ int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p) {
     }
     if ((rc = upload_geometry(h))) return rc;
     if ((rc = ensure_slots(h))) return rc;
+    // set-up of the allocation-free entry point on this device (once); a
+    // failure here is reported by that entry point, not by this step
+    noalloc_bind_device(h->device);
     if (h->staged) {
         if ((rc = prologue(h, c))) return rc;
     }
@@ -701,12 +705,13 @@ int lbm2d_init_equilibrium(lbm2d_solver* h, double rho, double u, double v, doub
 
 namespace lbm2d {
 namespace rt {
-namespace {
 
 // Launch one step from buffer h->cur (step kernel, force reduction,
-// immersed-boundary forcing); host state is not advanced.  With profiling
-// events, e0 / e1 bracket the step kernel alone.
-int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
+// immersed-boundary forcing); host state is not advanced.  The per-warp
+// force partials go to p.partials (the handle's buffer, or the fixed scratch
+// of the allocation-free entry point).  With profiling events, e0 / e1
+// bracket the step kernel alone.
+int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0, cudaEvent_t e1) {
     p.fin = h->P[h->cur];
     p.fout = h->P[h->cur ^ 1];
     p.gin = h->G[h->cur];
@@ -733,7 +738,7 @@ int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0 = nullptr, cudaE
     ++h->launches;
     if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
     if (h->nslots > 0 && !fused) {
-        e = launch_force_reduce(h->d_partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last, h->stream);
+        e = launch_force_reduce(p.partials, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last, h->stream);
         ++h->launches;
         if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");
     }
@@ -748,6 +753,8 @@ void advance(lbm2d_solver* h, long long n) {
     h->steps_since_collide += n;
     h->steps_done += n;
 }
+
+namespace {
 
 // Everything a captured step pair depends on: the parameters of its first
 // step, the launch shape and the buffers passed outside the parameters.
@@ -1156,6 +1163,14 @@ int lbm2d_profile(lbm2d_solver* h, double* ms, long long* n) {
     if (ms) *ms = total;
     if (n) *n = (long long)(h->ev_used / 2);
     h->ev_used = 0;
+    return LBM2D_OK;
+}
+
+int lbm2d_set_wait_limit(lbm2d_solver* h, long long cycles) {
+    int rc;
+    if ((rc = check_handle(h))) return rc;
+    if (cycles < 0) return fail(h, LBM2D_ERR_INVALID, "negative wait limit");
+    h->consumer_wait = cycles;
     return LBM2D_OK;
 }
 

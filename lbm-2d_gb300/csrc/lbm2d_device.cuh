@@ -813,7 +813,7 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
         skey = seed_key(s);
         pass_seed(p, s, bxi == 0 && byi == 0 && threadIdx.x == 0 && threadIdx.y == 0);
     }
-    R fxs = R(0), fys = R(0);
+    double fxs = 0.0, fys = 0.0;  // momentum exchange, accumulated in FP64
     if (x < p.nx && y < p.ny) {
         const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
         const uint32_t fl = __ldg(p.flags + n);
@@ -829,9 +829,9 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
 #pragma unroll
                 for (int j = 1; j < 9; ++j)
                     if (fm & (1u << j)) {
-                        const R fj = f[j] + R(p.shf[j]);
-                        fxs -= R(CXf(j)) * R(2) * fj;
-                        fys -= R(CYf(j)) * R(2) * fj;
+                        const double fj = double(f[j] + R(p.shf[j]));
+                        fxs -= double(CXf(j)) * 2.0 * fj;
+                        fys -= double(CYf(j)) * 2.0 * fj;
                     }
             }
             if constexpr (std::is_same<T, double>::value)
@@ -867,11 +867,10 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
     if (p.block_slot) {
         const int base = p.block_slot[byi * gx + bxi];
         if (base >= 0) {  // uniform per block; no barrier: one slot per warp
-            // Warp sum in the compute precision (FP32 per-node terms carry FP32
-            // rounding already; the FP64 variant stays FP64), only in warps that
-            // hold a force node; the cross-warp sum is FP64.
-            R a = fxs, b = fys;
-            if (__any_sync(0xffffffffu, a != R(0) || b != R(0))) {
+            // FP64 warp sum, only in warps that hold a force node; the
+            // cross-warp sum is FP64 as well.
+            double a = fxs, b = fys;
+            if (__any_sync(0xffffffffu, a != 0.0 || b != 0.0)) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     a += __shfl_down_sync(0xffffffffu, a, o);
@@ -881,8 +880,8 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
             const int tid = threadIdx.y * blockDim.x + threadIdx.x;
             if ((tid & 31) == 0) {
                 const int slot = base + (tid >> 5);
-                p.partials[2 * slot] = double(a);
-                p.partials[2 * slot + 1] = double(b);
+                p.partials[2 * slot] = a;
+                p.partials[2 * slot + 1] = b;
             }
             if (p.red_done) fused_force_finish(p, tid, [] { __syncthreads(); });
         }

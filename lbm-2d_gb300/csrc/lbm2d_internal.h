@@ -115,6 +115,11 @@ struct KParams {
     unsigned long long* red_counter;
     double* red_last;
     int red_blocks, red_nslots, red_cap, red_pad;
+    // limit, in SM cycles, of the row pipeline's consumer-side waits on its
+    // staged tiles (0: the default of about one second); the producer's own
+    // waits keep the default
+    long long consumer_wait;
+    long long pad_tail;
 };
 static_assert(sizeof(KParams) % 16 == 0, "KParams is staged with 16-byte copies");
 

@@ -38,7 +38,7 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
         skey = seed_key(s);
         pass_seed(p, s, bxi == 0 && byi == 0 && threadIdx.x == 0 && threadIdx.y == 0);
     }
-    float fxs = 0.0f, fys = 0.0f;
+    double fxs = 0.0, fys = 0.0;  // momentum exchange, accumulated in FP64
     if (x0 < p.nx && y < p.ny) {
         const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
         const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
@@ -54,14 +54,14 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
 #pragma unroll
             for (int j = 1; j < 9; ++j) {
                 if (ma & (1u << j)) {
-                    const float f = fmaf(fa[j], iS, p.shf[j]);
-                    fxs -= float(CXf(j)) * 2.0f * f;
-                    fys -= float(CYf(j)) * 2.0f * f;
+                    const double f = double(fmaf(fa[j], iS, p.shf[j]));
+                    fxs -= double(CXf(j)) * 2.0 * f;
+                    fys -= double(CYf(j)) * 2.0 * f;
                 }
                 if (mb & (1u << j)) {
-                    const float f = fmaf(fb[j], iS, p.shf[j]);
-                    fxs -= float(CXf(j)) * 2.0f * f;
-                    fys -= float(CYf(j)) * 2.0f * f;
+                    const double f = double(fmaf(fb[j], iS, p.shf[j]));
+                    fxs -= double(CXf(j)) * 2.0 * f;
+                    fys -= double(CYf(j)) * 2.0 * f;
                 }
             }
         }
@@ -91,8 +91,8 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
     if (p.block_slot) {
         const int base = p.block_slot[byi * gx + bxi];
         if (base >= 0) {
-            float a = fxs, b = fys;
-            if (__any_sync(0xffffffffu, a != 0.0f || b != 0.0f)) {
+            double a = fxs, b = fys;  // FP64 warp sum
+            if (__any_sync(0xffffffffu, a != 0.0 || b != 0.0)) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     a += __shfl_down_sync(0xffffffffu, a, o);
@@ -102,8 +102,8 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
             const int tid = threadIdx.y * blockDim.x + threadIdx.x;
             if ((tid & 31) == 0) {
                 const int slot = base + (tid >> 5);
-                p.partials[2 * slot] = double(a);
-                p.partials[2 * slot + 1] = double(b);
+                p.partials[2 * slot] = a;
+                p.partials[2 * slot + 1] = b;
             }
             if (p.red_done) fused_force_finish(p, tid, [] { __syncthreads(); });
         }

@@ -11,7 +11,10 @@
 // lbm2d_step_noalloc advances a solver that an earlier lbm2d_step has already
 // set up, and takes the scratch space of the force reduction -- per-warp
 // partial sums -- from a fixed array compiled into this library instead of
-// the handle's own buffer.  It calls no allocating routine of any kind.
+// the handle's own buffer.  It calls no allocating routine of any kind and
+// launches exactly the kernels lbm2d_step launches (step kernel with its
+// fused force reduction, immersed-boundary kernels), so its first call loads
+// no kernel that the preparing lbm2d_step did not load already.
 #include <mutex>
 
 #include "lbm2d_runtime.h"
@@ -33,22 +36,41 @@ constexpr int kMaxDevices = 64;
 double* g_scratch[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
-// Device address of the scratch array on the current device, looked up once
-// per device (with that device current) on the first call made for it.
-int scratch_address(int device, double** out) {
+// Device address of the scratch array on `device`, or null before
+// noalloc_bind_device has resolved it there.
+double* scratch_of(int device) {
+    if (device < 0 || device >= kMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    return g_scratch[device];
+}
+
+}  // namespace
+
+namespace lbm2d {
+namespace rt {
+
+// Looks the array's device address up once per device, with that device
+// current (the caller has made it current).  lbm2d_step calls this while it
+// prepares a solver, so the lookup -- which loads this file's module, and
+// with it the array, on a device that runs lazily loaded modules -- happens
+// on the path that allocates anyway, never inside lbm2d_step_noalloc.
+int noalloc_bind_device(int device) {
     if (device < 0 || device >= kMaxDevices) return LBM2D_ERR_INVALID;
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (!g_scratch[device]) {
         void* ptr = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_partials);
-        if (e != cudaSuccess || !ptr) return LBM2D_ERR_CUDA;
+        if (e != cudaSuccess || !ptr) {
+            cudaGetLastError();
+            return LBM2D_ERR_CUDA;
+        }
         g_scratch[device] = static_cast<double*>(ptr);
     }
-    *out = g_scratch[device];
     return LBM2D_OK;
 }
 
-}  // namespace
+}  // namespace rt
+}  // namespace lbm2d
 
 extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, int nsteps) {
     int rc;
@@ -56,22 +78,23 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
     if (nsteps < 0) return fail(h, LBM2D_ERR_INVALID, "negative step count");
     if (nsteps == 0) return LBM2D_OK;
     if (!(tau > 0.0)) return fail(h, LBM2D_ERR_INVALID, "tau must be positive");
+    if (h->profiling)  // the event pool may have to grow: that is the regular path's job
+        return fail(h, LBM2D_ERR_STATE, "lbm2d_step_noalloc does not record profiling events; switch profiling off");
     // Everything the step needs must already exist: a prior lbm2d_step with the
-    // same tau and settings has uploaded the geometry, collided the state and
-    // built the force-slot table for the current launch shape.
+    // same tau and settings has uploaded the geometry, collided the state,
+    // built the force-slot table for the current launch shape and looked the
+    // scratch array up on this device.
     const CollideParams c = collide_params(h, tau);
     const int kind = kernel_kind(h);
+    double* scratch = scratch_of(h->device);
     if (h->staged || h->geom_dirty || !(c == h->cp_of_P) || h->slot_kind != kind || !h->d_block_slot ||
-        (kind != KERNEL_ROWS && (h->slot_bx != h->bx || h->slot_by != h->by)))
+        (kind != KERNEL_ROWS && (h->slot_bx != h->bx || h->slot_by != h->by)) || !scratch)
         return fail(h, LBM2D_ERR_STATE,
                     "lbm2d_step_noalloc needs a solver prepared by lbm2d_step with the same tau and settings");
     if (h->nslots > kNoAllocMaxSlots)
         return fail(h, LBM2D_ERR_INVALID,
                     "force reduction needs " + std::to_string(h->nslots) + " slots; lbm2d_step_noalloc holds at most " +
                         std::to_string(kNoAllocMaxSlots));
-    double* scratch = nullptr;
-    if ((rc = scratch_address(h->device, &scratch)))
-        return fail(h, rc, "cudaGetSymbolAddress of the fixed scratch array failed");
 
     KParams p = base_params(h);
     apply_collide(p, c);
@@ -81,28 +104,8 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
     // reduction reads it, so the shared array needs no clearing between calls.
     p.partials = scratch;
     for (int k = 0; k < nsteps; ++k) {
-        p.fin = h->P[h->cur];
-        p.fout = h->P[h->cur ^ 1];
-        p.gin = h->G[h->cur];
-        p.gout = h->G[h->cur ^ 1];
-        p.seed_in = h->d_seed + h->cur;
-        p.seed_out = h->d_seed + (h->cur ^ 1);
-        p.skip_settled_solids = (h->steps_since_collide >= 2 && h->hook != 1) ? 1 : 0;
-        int e = kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
-                                    : launch_step(h->storage, p, h->bx, h->by, h->stream);
-        ++h->launches;
-        if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
-        if (h->nslots > 0) {
-            e = launch_force_reduce(scratch, h->nslots, h->d_hist, h->hist_cap, h->d_counter, h->d_last, h->stream);
-            ++h->launches;
-            if (e) return cuda_fail(h, (cudaError_t)e, "force reduce");
-        }
-        // immersed boundary: launches only, its buffers exist since lbm2d_set_ibm
-        if ((rc = ibm_after_step(h, p))) return rc;
-        h->cur ^= 1;
-        if (ibm_active(h)) h->ibm_next ^= 1;
-        ++h->steps_since_collide;
-        ++h->steps_done;
+        if ((rc = launch_one_step(h, p))) return rc;
+        advance(h, 1);
     }
     h->u_last = u_inflow;
     return LBM2D_OK;

@@ -53,8 +53,9 @@ struct RowsCfg {
     static constexpr int STAGES = ES == 4 ? 3 : 6;
     static constexpr int MIN_BLOCKS = ES == 4 ? 2 : 3;
     static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
-    static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;  // FP64 force sums, 2 per consumer warp
-    static constexpr int SMEM = ACC_OFF + 2 * kConsumerWarps * 8;
+    // FP64 momentum-exchange sums, one (fx, fy) pair per consumer lane
+    static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;
+    static constexpr int SMEM = ACC_OFF + 32 * kConsumerWarps * 16;
     static_assert(ROW_BYTES % 16 == 0 && FLAGS_OFF % 16 == 0, "bulk-copy alignment");
 };
 
@@ -89,11 +90,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase of parity `parity` to complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = kWaitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 
@@ -189,10 +190,12 @@ struct SmemPair<__nv_bfloat16> {
 // reference's post-stream state (pull, bounce-back records, outflow column,
 // boundary conditions), the momentum-exchange force, the collision and the
 // stores -- the body of step_pair_block with shared-memory pulls, on
-// deviations.
+// deviations.  The force terms of the two nodes are added in FP64 to the
+// lane's accumulator `acc` in shared memory, so no FP64 value stays live in
+// registers across the collision.
 template <class T, int KC, int KL>
 __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
-                                             uint32_t skey, float& fxs, float& fys) {
+                                             uint32_t skey, double2* acc) {
     using C = RowsCfg<T>;
     const uint2 fl = *reinterpret_cast<const uint2*>(stage + C::FLAGS_OFF + (x - x0) * 4);
     const int e0 = (x - x0) + C::PAD;
@@ -237,19 +240,24 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
         apply_bc<float>(p, x, y, fl.x, fa);
         apply_bc<float>(p, x + 1, y, fl.y, fb);
         if ((fl.x | fl.y) & FLAG_BOUNDARY) {
-            // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
+            // momentum exchange of the nodes' links (src/lbm.hpp:565-577),
+            // accumulated in FP64 (each term 2 f exact in FP64)
             const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
             const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+            if (ma | mb) {
+                double ax = acc->x, ay = acc->y;
 #pragma unroll
-            for (int j = 1; j < 9; ++j) {
-                if (ma & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * fa[j];
-                    fys -= float(CYf(j)) * 2.0f * fa[j];
+                for (int j = 1; j < 9; ++j) {
+                    if (ma & (1u << j)) {
+                        ax -= double(CXf(j)) * 2.0 * double(fa[j]);
+                        ay -= double(CYf(j)) * 2.0 * double(fa[j]);
+                    }
+                    if (mb & (1u << j)) {
+                        ax -= double(CXf(j)) * 2.0 * double(fb[j]);
+                        ay -= double(CYf(j)) * 2.0 * double(fb[j]);
+                    }
                 }
-                if (mb & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * fb[j];
-                    fys -= float(CYf(j)) * 2.0f * fb[j];
-                }
+                *acc = make_double2(ax, ay);
             }
         }
         // back to deviations; a regular neighbour keeps its exact deviations
@@ -300,7 +308,7 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
     // (y, seg) advanced incrementally
     const int G = (int)gridDim.x, dy = G / tpr, dseg = G - dy * tpr;
     const int y_first = (int)blockIdx.x / tpr, seg_first = (int)blockIdx.x - y_first * tpr;
-    double* acc = reinterpret_cast<double*>(smem + C::ACC_OFF);
+    double2* acc = reinterpret_cast<double2*>(smem + C::ACC_OFF);
     if (threadIdx.x == 0) {
         for (int s = 0; s < C::STAGES; ++s) {
             mbar_init(full0 + 8 * s, 1);
@@ -308,7 +316,7 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (threadIdx.x < 2 * kConsumerWarps) acc[threadIdx.x] = 0.0;
+    if (threadIdx.x < 32 * kConsumerWarps) acc[threadIdx.x] = make_double2(0.0, 0.0);
     __syncthreads();
 
     if (warp == kConsumerWarps) {  // producer
@@ -349,31 +357,22 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
         pass_seed(p, s, blockIdx.x == 0 && threadIdx.x == 0);
     }
     const bool force = p.block_slot != nullptr;
+    const long long wait_limit = p.consumer_wait > 0 ? p.consumer_wait : kWaitCycles;
     int y = y_first, seg = seg_first, s = 0;
     uint32_t phase = 0;
     while (y < p.ny) {
-        if (!mbar_wait(full0 + 8 * s, phase)) {
-            atomicOr(p.nan_flag, 2u);
+        // the whole warp leaves together when a wait runs out; the producer
+        // then runs out on the stage it would refill, drains its copies and
+        // the CTA ends
+        if (!__all_sync(0xffffffffu, mbar_wait(full0 + 8 * s, phase, wait_limit))) {
+            if (lane == 0) atomicOr(p.nan_flag, 2u);
             break;
         }
         const int x0 = seg * kTileW;
         const int x = x0 + 2 * (warp * 32 + lane);
-        float fxs = 0.0f, fys = 0.0f;
-        if (x < p.nx) consume_pair<T, KC, KL>(p, smem + s * C::STAGE_BYTES, x0, x, y, skey, fxs, fys);
+        if (x < p.nx) consume_pair<T, KC, KL>(p, smem + s * C::STAGE_BYTES, x0, x, y, skey, acc + threadIdx.x);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8 * s);
-        if (force && __any_sync(0xffffffffu, fxs != 0.0f || fys != 0.0f)) {
-            // per tile: FP32 warp sum of the tile's link terms, FP64 across tiles
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                fxs += __shfl_down_sync(0xffffffffu, fxs, o);
-                fys += __shfl_down_sync(0xffffffffu, fys, o);
-            }
-            if (lane == 0) {
-                acc[2 * warp] += double(fxs);
-                acc[2 * warp + 1] += double(fys);
-            }
-        }
         if (++s == C::STAGES) {
             s = 0;
             phase ^= 1u;
@@ -388,9 +387,16 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
     if (force) {
         const int base = p.block_slot[blockIdx.x];  // uniform per CTA
         if (base >= 0) {
+            // FP64 warp sum of the lanes' accumulators (fixed shuffle tree)
+            double a = acc[threadIdx.x].x, b = acc[threadIdx.x].y;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_down_sync(0xffffffffu, a, o);
+                b += __shfl_down_sync(0xffffffffu, b, o);
+            }
             if (lane == 0) {
-                p.partials[2 * (base + warp)] = acc[2 * warp];
-                p.partials[2 * (base + warp) + 1] = acc[2 * warp + 1];
+                p.partials[2 * (base + warp)] = a;
+                p.partials[2 * (base + warp) + 1] = b;
             }
             // the producer warp has left: the consumers' own named barrier
             if (p.red_done)

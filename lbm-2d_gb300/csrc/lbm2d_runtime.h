@@ -106,6 +106,7 @@ struct lbm2d_solver {
     int variant = 0;
     bool in_batch = false;  // a batch member is stepped by the batched kernels
     bool profiling = false;
+    long long consumer_wait = 0;  // row pipeline's consumer wait limit in cycles (0: default)
     // immersed boundary (lbm2d_set_ibm); ibm_np == 0: none.  F and the
     // Lagrangian values are double-buffered: slot ibm_next holds the force
     // for the next step, slot ibm_next ^ 1 the force the current state
@@ -169,6 +170,16 @@ int kernel_kind(const lbm2d_solver* h);
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
 // kernel parameters of the next step (fin = current buffer); returns status.
 int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p);
+// Launch one step from buffer h->cur (step kernel with its force reduction
+// into p.partials, immersed-boundary kernels); advance() then moves the host
+// state on by n steps.  e0 / e1 (optional) bracket the step kernel.
+int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr);
+void advance(lbm2d_solver* h, long long n);
+// Device address of the allocation-free entry point's fixed scratch array on
+// h's device, looked up once per device while a solver is being prepared
+// (lbm2d_noalloc.cu); lbm2d_step calls it so that the first allocation-free
+// call needs no lookup.
+int noalloc_bind_device(int device);
 
 }  // namespace rt
 }  // namespace lbm2d

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -37,10 +38,20 @@ double now_s() {
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// Caller-supplied state of a request (lbm2d_server_submit_state): an initial
+// population field copied at submission, and the caller's buffers that
+// receive the final populations when the request retires.
+struct StateIO {
+    std::shared_ptr<std::vector<double>> f_init;
+    double* f_out = nullptr;
+    double* g_out = nullptr;
+};
+
 struct Pending {
     long long id;
     lbm2d_request req;
     double t_submit;
+    StateIO io;
 };
 
 struct Active {
@@ -51,6 +62,7 @@ struct Active {
     double t_submit = 0, t_admit = 0;
     size_t footprint = 0;
     double tau = 0.0, u_bc = 0.0;
+    StateIO io;
 };
 
 size_t footprint_bytes(const lbm2d_request& r) {
@@ -177,6 +189,8 @@ int setup_request(lbm2d_server* s, Active& a) {
         u_init = u;  // uniform inflow initial state
     }
     if ((rc = lbm2d_init_equilibrium(a.h, 1.0, u_init, 0.0, 1.0))) return rc;
+    if (a.io.f_init && (rc = lbm2d_upload_f(a.h, a.io.f_init->data()))) return rc;
+    a.io.f_init.reset();  // the copy is on the device now
     lbm2d_info info;  // builds and uploads the geometry here, off the stepping thread
     if ((rc = lbm2d_get_info(a.h, &info))) return rc;
     if ((rc = lbm2d_synchronize(a.h))) return rc;
@@ -206,7 +220,13 @@ void record(lbm2d_server* s, const Active& a, int status) {
 }
 
 // Free a solve that is in no batch and give its memory back to admission.
+// A request that asked for its final state gets it first (a solve that was
+// stepped, diverged or not), so the buffers are filled when the result shows.
 void release(lbm2d_server* s, const Active& a, int status) {
+    if (a.h && (status == LBM2D_OK || status == LBM2D_ERR_NAN)) {
+        if (a.io.f_out) lbm2d_download_f(a.h, a.io.f_out);
+        if (a.io.g_out && a.req.geometry == LBM2D_GEOM_HEATED_CAVITY) lbm2d_download_g(a.h, a.io.g_out);
+    }
     record(s, a, status);
     if (a.h) lbm2d_destroy(a.h);
     std::lock_guard<std::mutex> lock(s->mu);
@@ -243,6 +263,7 @@ void setup_loop(lbm2d_server* s) {
             a.req = p.req;
             a.left = p.req.steps;
             a.t_submit = p.t_submit;
+            a.io = p.io;
             a.t_admit = now_s();
             a.footprint = footprint_bytes(p.req);
             s->used += a.footprint;
@@ -369,16 +390,28 @@ int lbm2d_server_create(int device, double budget_bytes, int max_active, int ste
     return LBM2D_OK;
 }
 
-int lbm2d_server_submit(lbm2d_server* s, const lbm2d_request* r, long long* id) {
+int lbm2d_server_submit_state(lbm2d_server* s, const lbm2d_request* r, const double* f_init, double* f_out,
+                              double* g_out, long long* id) {
     if (!s || !r || r->nx < 3 || r->ny < 3 || r->steps < 0) return LBM2D_ERR_INVALID;
+    StateIO io;
+    if (f_init) {
+        const size_t n9 = (size_t)r->nx * r->ny * 9;
+        io.f_init = std::make_shared<std::vector<double>>(f_init, f_init + n9);
+    }
+    io.f_out = f_out;
+    io.g_out = g_out;
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->stop) return LBM2D_ERR_STATE;
-    Pending p{s->next_id++, *r, now_s()};
+    Pending p{s->next_id++, *r, now_s(), io};
     s->queue.push_back(p);
     ++s->submitted;
     if (id) *id = p.id;
     s->cv_setup.notify_all();
     return LBM2D_OK;
+}
+
+int lbm2d_server_submit(lbm2d_server* s, const lbm2d_request* r, long long* id) {
+    return lbm2d_server_submit_state(s, r, nullptr, nullptr, nullptr, id);
 }
 
 int lbm2d_server_wait(lbm2d_server* s, long long n_finished, double timeout_s) {

@@ -85,7 +85,11 @@ inline void enforce_lid(LBMCapabilities& sys, double u_lid) {
 
 // ---------------------------------------------------------------- node-level operators (host)
 // d'Humieres MRT of one node with optional Smagorinsky / Van Driest,
-// src/lbm.hpp:128-218.  The GPU kernel applies the same operator to every node.
+// src/lbm.hpp:128-218.  The GPU kernel applies the same operator to every
+// node.  This host form keeps the reference's operation order term by term
+// (moments, the plain and then the damped LES rate, relaxation, the inverse
+// transform as a sum over the moment vector), so with FP contraction off it
+// gives the reference's bits.
 inline void mrt_collide(double* f_node, double rho, double u, double v, const MRTParams& mrt, double cs_sq = 0.0,
                         double tau_base = 0.0, double y_plus = 0.0) {
     const double f0 = f_node[0], f1 = f_node[1], f2 = f_node[2], f3 = f_node[3], f4 = f_node[4];
@@ -98,68 +102,87 @@ inline void mrt_collide(double* f_node, double rho, double u, double v, const MR
     double pxy = f5 - f6 + f7 - f8;
     const double jx = rho * u, jy = rho * v, usq = u * u + v * v;
     const double e_eq = -2 * rho + 3 * rho * usq, eps_eq = rho - 3 * rho * usq;
+    const double qx_eq = -jx, qy_eq = -jy;
     const double pxx_eq = rho * (u * u - v * v), pxy_eq = rho * u * v;
     auto clamp = [](double s) { return (s < 0.5) ? 0.5 : ((s > 1.99) ? 1.99 : s); };
-    double s_eff = mrt.s_shear;
-    if (cs_sq > 0.0 && tau_base > 0.0) {
-        double csq = cs_sq;
-        if (y_plus > 0.0) {
-            const double cd = std::sqrt(cs_sq) * (1.0 - std::exp(-y_plus / 26.0));
-            csq = cd * cd;
-        }
+    // LES relaxation rate for a Smagorinsky constant squared c2
+    auto les_rate = [&](double c2) {
         const double a = pxx - pxx_eq, b = pxy - pxy_eq;
         const double Q = std::sqrt(2.0 * (a * a + b * b));
-        const double A = 9.0 * csq * Q / (2.0 * rho);
-        s_eff = clamp(1.0 / ((tau_base + std::sqrt(tau_base * tau_base + 4.0 * A)) / 2.0));
+        const double A = 9.0 * c2 * Q / (2.0 * rho);
+        const double t = (tau_base + std::sqrt(tau_base * tau_base + 4.0 * A)) / 2.0;
+        return clamp(1.0 / t);
+    };
+    double s_eff = mrt.s_shear;
+    if (cs_sq > 0.0 && tau_base > 0.0) s_eff = les_rate(cs_sq);
+    if (cs_sq > 0.0 && tau_base > 0.0 && y_plus > 0.0) {  // Van Driest damping overrides
+        const double cd = std::sqrt(cs_sq) * (1.0 - std::exp(-y_plus / 26.0));
+        s_eff = les_rate(cd * cd);
     }
     e -= mrt.s_bulk * (e - e_eq);
     eps -= mrt.s_bulk * (eps - eps_eq);
-    qx -= mrt.s_normal * (qx + jx);
-    qy -= mrt.s_normal * (qy + jy);
+    qx -= mrt.s_normal * (qx - qx_eq);
+    qy -= mrt.s_normal * (qy - qy_eq);
     pxx -= s_eff * (pxx - pxx_eq);
     pxy -= s_eff * (pxy - pxy_eq);
-    const double a0 = rho / 9.0;
-    const double ax = a0 - e / 36.0 - eps / 18.0, ad = a0 + e / 18.0 + eps / 36.0;
-    const double hx = (jx - qx) / 6.0, hy = (jy - qy) / 6.0;
-    const double dx = jx / 6.0 + qx / 12.0, dy = jy / 6.0 + qy / 12.0;
-    f_node[0] = a0 - e / 9.0 + eps / 9.0;
-    f_node[1] = ax + hx + pxx / 4.0;
-    f_node[2] = ax + hy - pxx / 4.0;
-    f_node[3] = ax - hx + pxx / 4.0;
-    f_node[4] = ax - hy - pxx / 4.0;
-    f_node[5] = ad + dx + dy + pxy / 4.0;
-    f_node[6] = ad - dx + dy - pxy / 4.0;
-    f_node[7] = ad - dx - dy + pxy / 4.0;
-    f_node[8] = ad + dx - dy - pxy / 4.0;
+    // inverse transform: row i of M^-1 dotted with (rho, e, eps, jx, qx, jy, qy, pxx, pxy)
+    const double m[9] = {rho, e, eps, jx, qx, jy, qy, pxx, pxy};
+    static constexpr double Minv[9][9] = {
+        {1.0 / 9, -1.0 / 9, 1.0 / 9, 0, 0, 0, 0, 0, 0},
+        {1.0 / 9, -1.0 / 36, -1.0 / 18, 1.0 / 6, -1.0 / 6, 0, 0, 1.0 / 4, 0},
+        {1.0 / 9, -1.0 / 36, -1.0 / 18, 0, 0, 1.0 / 6, -1.0 / 6, -1.0 / 4, 0},
+        {1.0 / 9, -1.0 / 36, -1.0 / 18, -1.0 / 6, 1.0 / 6, 0, 0, 1.0 / 4, 0},
+        {1.0 / 9, -1.0 / 36, -1.0 / 18, 0, 0, -1.0 / 6, 1.0 / 6, -1.0 / 4, 0},
+        {1.0 / 9, 1.0 / 18, 1.0 / 36, 1.0 / 6, 1.0 / 12, 1.0 / 6, 1.0 / 12, 0, 1.0 / 4},
+        {1.0 / 9, 1.0 / 18, 1.0 / 36, -1.0 / 6, -1.0 / 12, 1.0 / 6, 1.0 / 12, 0, -1.0 / 4},
+        {1.0 / 9, 1.0 / 18, 1.0 / 36, -1.0 / 6, -1.0 / 12, -1.0 / 6, -1.0 / 12, 0, 1.0 / 4},
+        {1.0 / 9, 1.0 / 18, 1.0 / 36, 1.0 / 6, 1.0 / 12, -1.0 / 6, -1.0 / 12, 0, -1.0 / 4}};
+    for (int i = 0; i < 9; ++i) {
+        // left to right over the nonzero entries: the reference's sum order
+        double acc = Minv[i][0] * m[0];
+        for (int k = 1; k < 9; ++k)
+            if (Minv[i][k] != 0.0) acc += Minv[i][k] * m[k];
+        f_node[i] = acc;
+    }
 }
 
-// Interpolated bounce-back of one link into sys.f_next (host), src/lbm.hpp:226-288.
+// Interpolated bounce-back of one link into sys.f_next (host), src/lbm.hpp:226-288:
+// Mei / Filippova-Hanel by default; classic Bouzidi (the source node's value
+// when q < 1/2, the node's own opposite value otherwise) with the Ladd wall
+// term when use_mei_bb is off.  Same operation order as the reference.
 inline void apply_bouzidi_bb(LBMCapabilities& sys, int x, int y, int i, const double* f_node, int node_idx) {
     if (sys.f_next.size() != sys.f.size()) sys.f_next.assign(sys.f.size(), 0.0);
     const BounceBackGeometry& g = sys.bb_geom;
     const double q = g.compute_q(static_cast<double>(x), static_cast<double>(y), i);
     const int bb = bounce_back[i];
-    double rho, u, v;
-    compute_macros(f_node, rho, u, v);
-    double uwx = 0.0, uwy = 0.0;
-    if (g.has_moving_wall) g.compute_wall_velocity(x + cx[i], y + cy[i], uwx, uwy);
-    const double ed = cx[i] * uwx + cy[i] * uwy;
+    auto wall_velocity = [&](double& uwx, double& uwy) {
+        g.compute_wall_velocity(static_cast<double>(x + cx[i]), static_cast<double>(y + cy[i]), uwx, uwy);
+    };
     double fbb;
     if (g.use_mei_bb) {
-        fbb = q * compute_equilibrium(i, rho, uwx, uwy) + (1.0 - q) * f_node[i] +
-              (2.0 * q - 1.0) * weights[i] * rho * ed * 3.0;
+        double rho, u, v;
+        compute_macros(f_node, rho, u, v);
+        double uwx = 0.0, uwy = 0.0;
+        if (g.has_moving_wall) wall_velocity(uwx, uwy);
+        const double feq_wall = compute_equilibrium(i, rho, uwx, uwy);
+        const double ed = cx[i] * uwx + cy[i] * uwy;
+        fbb = q * feq_wall + (1.0 - q) * f_node[i] + (2.0 * q - 1.0) * weights[i] * rho * ed * 3.0;
+    } else if (q < 0.5) {
+        const int sx = x - cx[i], sy = y - cy[i];
+        if (sx >= 0 && sx < NX && sy >= 0 && sy < NY)
+            fbb = 2.0 * q * f_node[i] + (1.0 - 2.0 * q) * sys.f[static_cast<size_t>(node_index(sx, sy)) * 9 + i];
+        else
+            fbb = f_node[i];
     } else {
-        if (q < 0.5) {
-            const int sx = x - cx[i], sy = y - cy[i];
-            const double fs = (sx >= 0 && sx < NX && sy >= 0 && sy < NY)
-                                  ? sys.f[static_cast<size_t>(node_index(sx, sy)) * 9 + i]
-                                  : f_node[i];
-            fbb = 2.0 * q * f_node[i] + (1.0 - 2.0 * q) * fs;
-        } else {
-            const double inv2q = 1.0 / (2.0 * q);
-            fbb = inv2q * f_node[i] + (1.0 - inv2q) * sys.f[static_cast<size_t>(node_idx) * 9 + bb];
-        }
-        if (g.has_moving_wall) fbb -= 2.0 * weights[i] * rho * ed * 3.0;
+        const double inv2q = 1.0 / (2.0 * q);
+        fbb = inv2q * f_node[i] + (1.0 - inv2q) * sys.f[static_cast<size_t>(node_idx) * 9 + bb];
+    }
+    if (g.has_moving_wall && !g.use_mei_bb) {
+        double uwx, uwy, rho, u, v;
+        wall_velocity(uwx, uwy);
+        compute_macros(f_node, rho, u, v);
+        const double ed = cx[i] * uwx + cy[i] * uwy;
+        fbb -= 2.0 * weights[i] * rho * ed * 3.0;
     }
     sys.f_next[static_cast<size_t>(node_idx) * 9 + bb] = fbb;
 }

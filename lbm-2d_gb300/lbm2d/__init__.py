@@ -118,6 +118,7 @@ _SIGS = {
     "lbm2d_get_info": ([_P, C.POINTER(Info)], _I),
     "lbm2d_set_block": ([_P, _I, _I], _I),
     "lbm2d_set_kernel_variant": ([_P, _I], _I),
+    "lbm2d_set_wait_limit": ([_P, C.c_longlong], _I),
     "lbm2d_stream": ([_P], _P),
     "lbm2d_set_profiling": ([_P, _I], _I),
     "lbm2d_profile": ([_P, _DP, C.POINTER(C.c_longlong)], _I),
@@ -139,6 +140,7 @@ _SIGS = {
     "lbm2d_autotune": ([_P, _I, _D, _D, C.POINTER(_I), C.POINTER(_I)], _I),
     "lbm2d_server_create": ([_I, _D, _I, _I, C.POINTER(_P)], _I),
     "lbm2d_server_submit": ([_P, C.POINTER(Request), C.POINTER(C.c_longlong)], _I),
+    "lbm2d_server_submit_state": ([_P, C.POINTER(Request), _DP, _DP, _DP, C.POINTER(C.c_longlong)], _I),
     "lbm2d_server_wait": ([_P, C.c_longlong, _D], _I),
     "lbm2d_server_results": ([_P, C.POINTER(Result), _I, C.POINTER(_I)], _I),
     "lbm2d_server_stats": ([_P, C.POINTER(ServerStats)], _I),
@@ -402,6 +404,11 @@ class Solver:
         (KERNEL_SCALAR / KERNEL_PAIR / KERNEL_ROWS)."""
         self._ck(self.L.lbm2d_set_kernel_variant(self.h, int(variant)))
 
+    def set_wait_limit(self, cycles: int):
+        """Limit of the row pipeline's consumer waits in SM cycles (0: the
+        default of about one second); a tiny limit exercises the timeout path."""
+        self._ck(self.L.lbm2d_set_wait_limit(self.h, int(cycles)))
+
     # -- state
     def upload_f(self, f):
         a = np.ascontiguousarray(f, np.float64).reshape(-1)
@@ -639,12 +646,30 @@ class Server:
         if rc:
             raise LBMError(rc, "server create")
         self.L, self.h = L, h
+        self._state = {}  # id -> (f_out, g_out) buffers the server writes at retirement
 
-    def submit(self, nx, ny, geometry, re, steps, storage="fp16", param=0.0, u=0.1) -> int:
+    def submit(self, nx, ny, geometry, re, steps, storage="fp16", param=0.0, u=0.1, f_init=None,
+               keep_state=False) -> int:
+        """Queue one solve.  f_init (optional): its initial populations, FP64
+        AoS, instead of the geometry's equilibrium start.  keep_state: the
+        final populations (and, for the heated cavity, the temperature
+        populations) are returned with the result as "f" / "g"."""
         r = Request(int(nx), int(ny), int(geometry), float(re), float(param), float(u), int(steps),
                     STORAGE[storage] if isinstance(storage, str) else int(storage))
         rid = C.c_longlong()
-        rc = self.L.lbm2d_server_submit(self.h, C.byref(r), C.byref(rid))
+        if f_init is None and not keep_state:
+            rc = self.L.lbm2d_server_submit(self.h, C.byref(r), C.byref(rid))
+        else:
+            n9 = int(nx) * int(ny) * 9
+            fi = None if f_init is None else np.ascontiguousarray(f_init, np.float64).reshape(-1)
+            assert fi is None or fi.size == n9
+            fo = np.full(n9, np.nan) if keep_state else None
+            go = np.full(n9, np.nan) if keep_state and int(geometry) == GEOM_HEATED_CAVITY else None
+            rc = self.L.lbm2d_server_submit_state(self.h, C.byref(r), None if fi is None else _d(fi),
+                                                  None if fo is None else _d(fo), None if go is None else _d(go),
+                                                  C.byref(rid))
+            if not rc and keep_state:
+                self._state[rid.value] = (fo, go)
         if rc:
             raise LBMError(rc, "submit")
         return rid.value
@@ -658,7 +683,11 @@ class Server:
         arr = (Result * max(n.value, 1))()
         self.L.lbm2d_server_results(self.h, arr, n.value, C.byref(n))
         keys = [k for k, _ in Result._fields_]
-        return [{k: getattr(arr[i], k) for k in keys} for i in range(n.value)]
+        out = [{k: getattr(arr[i], k) for k in keys} for i in range(n.value)]
+        for x in out:
+            if x["id"] in self._state:
+                x["f"], x["g"] = self._state[x["id"]]
+        return out
 
     def stats(self) -> dict:
         st = ServerStats()

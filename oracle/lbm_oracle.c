@@ -526,6 +526,16 @@ static void or_interp_bb(or_state *s, int x, int y, int i, const double *fn, int
     s->f_next[(size_t)node * 9 + bb] = fbb;
 }
 
+/* One interpolated bounce-back link of node (x, y), direction i, from the
+ * current f (the pre-stream state the reference passes), as or_interp_bb
+ * writes it into f_next; returns the written value.  Test hook for the C++
+ * drop-in's host apply_bouzidi_bb. */
+double or_interp_bb_link(or_state *s, int x, int y, int i) {
+    const int node = nidx(s, x, y);
+    or_interp_bb(s, x, y, i, &s->f[(size_t)node * 9], node);
+    return s->f_next[(size_t)node * 9 + OR_BB[i]];
+}
+
 /* ---------------------------------------------------------------- the time step */
 
 /* execute_time_step, src/lbm.hpp:293-582 */

@@ -91,6 +91,8 @@ def _load(path: str, prefix: str) -> C.CDLL:
             "or_ibm_step": ([_P, _D, _D], None),
             "or_ibm_lagrangian": ([_P, _DP, _DP, _DP, _DP], None),
             "or_ibm_kernel": ([_D, _D], _D),
+            "or_interp_bb_link": ([_P, _I, _I, _I], _D),
+            "or_mrt_collide": ([_DP, _D, _D, _D, _D, _D, _D, _D, _D, _D], None),
         }
     else:
         ibm = {

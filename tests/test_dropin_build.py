@@ -2,7 +2,7 @@
 the drop-in headers (lbm-2d_gb300/dropin) and link liblbm2d; the unit tests
 that need no GPU run.  Each source is copied to a temporary directory so its
 quoted includes resolve to the drop-in headers, not to the reference's own.
-Skipped where the reference sources are not present."""
+Skipped unless LBM2D_REF_SRC names the reference's src/ folder."""
 import os
 import shutil
 import subprocess
@@ -11,12 +11,14 @@ import pytest
 
 from dropin_build import compile_dropin
 
-REF_SRC = "/root/reference/src"
+# the reference's src/ folder, from the environment (no default)
+REF_SRC = os.environ.get("LBM2D_REF_SRC", "")
 DRIVERS = ["main", "cavity", "step", "thermal_cavity", "heated_cylinder", "rotating_cylinder",
            "side_by_side_cylinders", "cylinder_near_wall", "periodic_hills", "square_cylinder", "flat_plate",
            "orifice_plate", "urban_canyon", "downwash", "airfoil_ibm"]
 
-needs_ref = pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+needs_ref = pytest.mark.skipif(not (REF_SRC and os.path.isdir(REF_SRC)),
+                               reason="LBM2D_REF_SRC does not name the reference sources")
 
 
 @needs_ref

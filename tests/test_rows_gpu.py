@@ -109,3 +109,30 @@ def test_kernel_selection(product):
     s = product.Solver(1036, 8, product.RIBS, storage="fp32")  # 16-byte rows in FP32
     assert s.info().kernel == product.KERNEL_ROWS
     s.close()
+
+
+def test_pipeline_wait_timeout_reports_and_recovers(product, oracle_lib):
+    """The row pipeline's bounded waits: with the consumers' wait limit set to
+    one SM cycle, the consumers give up on their first staged tile, the kernel
+    ends (the producer drains the copies it issued) and the next
+    synchronisation reports LBM2D_ERR_TIMEOUT (7).  The context stays usable:
+    with the default limit restored, a re-uploaded state steps to exactly the
+    result of a fresh solver."""
+    spec = CS.CASES["ribs_les"]  # 64 x 40, FP32: the row pipeline
+    s = gpu_solver(product, oracle_lib, spec, "fp32")
+    assert s.info().kernel == product.KERNEL_ROWS
+    f0 = s.f
+    s.set_wait_limit(1)
+    s.step(spec["tau"], spec["u"], 1)
+    with pytest.raises(product.LBMError) as ex:
+        s.synchronize()
+    assert ex.value.code == 7
+    s.set_wait_limit(0)
+    s.upload_f(f0)
+    s.step(spec["tau"], spec["u"], 5)
+    s.synchronize()
+    ref = gpu_solver(product, oracle_lib, spec, "fp32")
+    ref.step(spec["tau"], spec["u"], 5)
+    assert np.array_equal(s.f, ref.f)
+    s.close()
+    ref.close()

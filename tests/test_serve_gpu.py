@@ -1,20 +1,28 @@
 """Serving loop: requests of different sizes, geometries and budgets are
 admitted, stepped together and retired exactly at their budgets.
 
-* Co-scheduling invariance: a request served in the mix gives bit-for-bit
-  the drag/lift it gives when it is the only request of a serving loop.
-* Against the plain per-solve API (a separately compiled kernel), drag/lift
-  agree within 1e-6 relative, except for the closed heated cavity, whose net
-  wall force is a small difference of large wall terms: 1e-4 in FP32 and
-  2e-3 in FP16.  FP16 is stored with stochastic rounding, which carries an
-  ulp-level FP32 difference between two kernels forward as a random walk
-  (round-to-nearest would mostly absorb it), so two FP16 runs differ by up
-  to the storage precision.
+* Co-scheduling invariance: a request served in the mix ends with
+  bit-for-bit the same final populations (and temperature populations for the
+  heated cavity) and drag/lift as when it is the only request of a serving
+  loop -- every geometry, the cavity included.
+* Against the plain per-solve API (a separately compiled kernel), the final
+  populations agree within FIELD_TOL relative L2 and drag/lift within 1e-6
+  relative, except for the closed heated cavity, whose net wall force is a
+  small difference of large wall terms: 1e-4 in FP32 and 2e-3 in FP16.  FP16
+  is stored with stochastic rounding, which carries an ulp-level FP32
+  difference between two kernels forward as a random walk (round-to-nearest
+  would mostly absorb it), so two FP16 runs differ by up to the storage
+  precision.
+* Failure isolation: a request whose initial state carries a NaN (seeded on
+  the host) retires with LBM2D_ERR_NAN while every other request of its mix
+  stays bit-identical to its solo run.
 * Admission respects the device-memory budget."""
 import time
 
 import numpy as np
 import pytest
+
+from gpu_cases import rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -26,14 +34,19 @@ REQS = [dict(nx=128, ny=64, geometry=2, re=100.0, steps=300, param=0.0),
         dict(nx=256, ny=96, geometry=2, re=800.0, steps=120, param=0.0)]
 
 
+# final populations, served in the mix vs the plain per-solve API
+FIELD_TOL = {"fp32": 1e-6, "fp16": 1e-4}
+
+
 def _alone(product, r, storage):
     import bench
     s = bench._plain_solver(product, r, storage)
     s.step(s._tau, s._ubc, r["steps"])
     s.synchronize()
     fx, fy = s.force_sums()
+    f = s.f
     s.close()
-    return fx, fy
+    return fx, fy, f
 
 
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
@@ -41,7 +54,8 @@ def test_served_results_match_alone(product, storage):
     srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=64)
     ids = []
     for r in REQS:
-        ids.append(srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"]))
+        ids.append(srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"],
+                              keep_state=True))
         time.sleep(0.002)
     assert srv.wait(len(REQS), 120)
     res = {x["id"]: x for x in srv.results()}
@@ -51,34 +65,69 @@ def test_served_results_match_alone(product, storage):
         assert x["status"] == 0, x
         assert x["steps"] == r["steps"] and x["nodes"] == r["nx"] * r["ny"]
         assert x["t_submit"] <= x["t_admit"] <= x["t_done"]
+        fx, fy, f = _alone(product, r, storage)
+        err_f = rel_l2(x["f"], f)
+        assert err_f <= FIELD_TOL[storage], (r, err_f)
         if r["geometry"] == 0:
-            continue  # the cavity has no momentum-exchange pass
-        fx, fy = _alone(product, r, storage)
+            assert x["fx"] == x["fy"] == 0.0  # the cavity has no momentum-exchange pass
+            continue
         scale = max(abs(fx), abs(fy), 1e-12)
         tol = (1e-4 if storage == "fp32" else 2e-3) if r["geometry"] == 4 else 1e-6
         assert abs(x["fx"] - fx) <= tol * scale and abs(x["fy"] - fy) <= tol * scale, (r, x, fx, fy)
 
 
-def _serve(product, reqs, storage, tick):
+def _serve(product, reqs, storage, tick, f_inits=None):
     srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=tick)
-    ids = [srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"]) for r in reqs]
+    f_inits = f_inits or [None] * len(reqs)
+    ids = [srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"], f_init=fi,
+                      keep_state=True) for r, fi in zip(reqs, f_inits)]
     assert srv.wait(len(reqs), 120)
     res = {x["id"]: x for x in srv.results()}
     srv.close()
     return [res[i] for i in ids]
 
 
+def _same_state(x, a):
+    """Bit-for-bit equal final populations (NaN-free) and drag/lift."""
+    assert np.isfinite(x["f"]).all() and np.array_equal(x["f"], a["f"])
+    if x["g"] is not None:
+        assert np.isfinite(x["g"]).all() and np.array_equal(x["g"], a["g"])
+    assert x["fx"] == a["fx"] and x["fy"] == a["fy"]
+
+
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
 def test_mix_equals_alone_bit_for_bit(product, storage):
     """Every request alone in a serving loop and the same request among the
     others (different tick boundaries, other solves in the same launches)
-    end with identical drag/lift."""
+    end with identical populations and drag/lift."""
     mixed = _serve(product, REQS, storage, 64)
     for r, x in zip(REQS, mixed):
         (a,) = _serve(product, [r], storage, 64)
         assert x["status"] == 0 and a["status"] == 0
         assert x["steps"] == a["steps"] == r["steps"]
-        assert x["fx"] == a["fx"] and x["fy"] == a["fy"], (r, x, a)
+        _same_state(x, a)
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_nan_request_fails_alone(product, storage):
+    """A request started from a state with one NaN population (seeded on the
+    host) diverges and retires with LBM2D_ERR_NAN (4); its mix-mates, stepped
+    in the same launches, end bit-identical to their solo runs."""
+    import bench
+    bad = dict(nx=128, ny=64, geometry=2, re=100.0, steps=200, param=0.0)
+    s = bench._plain_solver(product, bad, storage)
+    f0 = s.f  # the geometry's equilibrium start, as the server builds it
+    s.close()
+    f0[(32 * bad["nx"] + 64) * 9 + 3] = np.nan
+    reqs = REQS[:3] + [bad] + REQS[3:]
+    mixed = _serve(product, reqs, storage, 64, f_inits=[None, None, None, f0, None, None, None])
+    assert mixed[3]["status"] == 4, mixed[3]
+    for k, (r, x) in enumerate(zip(reqs, mixed)):
+        if k == 3:
+            continue
+        (a,) = _serve(product, [r], storage, 64)
+        assert x["status"] == 0 and a["status"] == 0, (r, x)
+        _same_state(x, a)
 
 
 def test_admission_respects_memory_budget(product):

@@ -8,8 +8,11 @@ into the library.  This test calls it through the C-ABI twice in a row and
 checks each result against the regular entry point on an identical solver:
 populations within the FP32 parity bound of the other GPU tests (1e-5
 relative L2) and the per-step drag/lift within the same bound.  It also
-checks that the device's free memory does not change across the second
-call.  It runs last (file name) so a failure here cannot hide another test.
+checks that the device's free memory does not change across either call:
+the preparing lbm2d_step has already looked the fixed array up on the
+device, and the allocation-free call launches only kernels that lbm2d_step
+has loaded.  It runs last (file name) so a failure here cannot hide another
+test.
 """
 import ctypes as C
 
@@ -49,8 +52,7 @@ def test_noalloc_step_matches_regular_step(product, oracle_lib):
         rc = fn(noalloc.h, tau, u, 6)
         assert rc == 0, L.lbm2d_last_error(noalloc.h).decode()
         noalloc.synchronize()
-        if call == 1:  # the first call may load the library's fixed scratch array
-            assert _free_bytes() == free_before
+        assert _free_bytes() == free_before, call
         assert rel_l2(noalloc.f, regular.f) <= TOL
         fx_a, fy_a = regular.force_history()
         fx_b, fy_b = noalloc.force_history()
@@ -71,5 +73,9 @@ def test_noalloc_step_rejects_unprepared_solver(product, oracle_lib):
     assert fn(s.h, spec["tau"], spec["u"], 1) == 5  # LBM2D_ERR_STATE: not prepared yet
     s.step(spec["tau"], spec["u"], 1)
     assert fn(s.h, spec["tau"] * 1.1, spec["u"], 1) == 5  # tau changed: needs the regular path
+    assert fn(s.h, spec["tau"], spec["u"], 1) == 0
+    s.set_profiling(True)
+    assert fn(s.h, spec["tau"], spec["u"], 1) == 5  # profiling events are the regular path's
+    s.set_profiling(False)
     assert fn(s.h, spec["tau"], spec["u"], 1) == 0
     s.close()
