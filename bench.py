@@ -60,7 +60,9 @@ WORKLOAD = workload_name(NX, NY)
 KERNEL_NAMES = {0: ("step_kernel", "one node per thread"),
                 1: ("step_pair_kernel", "two x-neighbours per thread, packed FP32x2, register pulls"),
                 2: ("step_rows_kernel", "row tiles staged by cp.async.bulk into shared memory, persistent grid, "
-                                        "packed FP32x2")}
+                                        "packed FP32x2"),
+                3: ("step_tiles_kernel", "flat tiles of 512 consecutive nodes staged by cp.async.bulk, persistent "
+                                         "grid over one or many instances")}
 
 
 def peaks():
@@ -492,37 +494,47 @@ def batch_block(args, lbm2d, storage, steps):
     in one whole-budget call."""
     import torch
     inst = _c4_instances(args.instances)
-    solvers = [_plain_solver(lbm2d, r, storage) for r in inst]
     nodes = sum(r["nx"] * r["ny"] for r in inst)
-    # sequential: each solver alone, one after the other
+
+    def diverged(solvers):
+        n = 0
+        for s in solvers:
+            try:
+                s.synchronize()
+            except lbm2d.LBMError as ex:  # a solve that diverges does so in both legs alike
+                if ex.code != 4:
+                    raise
+                n += 1
+        return n
+
+    # sequential: each solver alone, one after the other, from the same start
+    solvers = [_plain_solver(lbm2d, r, storage) for r in inst]
     for s in solvers:
         s.step(s._tau, s._ubc, 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in solvers:
         s.step(s._tau, s._ubc, steps)
-    for s in solvers:
-        s.synchronize()
+    torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
-    # batched
+    nan_seq = diverged(solvers)
+    for s in solvers:
+        s.close()
+    # batched: fresh solvers from the same start
+    solvers = [_plain_solver(lbm2d, r, storage) for r in inst]
     b = lbm2d.Batch()
     for s in solvers:
         b.add(s, s._tau, s._ubc)
     if args.autotune:
         bx, by = b.autotune(5)
     b.step(2)
-    b.synchronize()
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     l0 = b.launches
     b.step(steps)
-    b.synchronize()
+    torch.cuda.synchronize()
     t_bat = time.perf_counter() - t0
-    nan = 0
-    for s in solvers:
-        try:
-            s.synchronize()
-        except lbm2d.LBMError:
-            nan += 1
+    nan = diverged(solvers)
     bytes_lu = sum(r["nx"] * r["ny"] * 18 * lbm2d.BYTES_PER_POP[storage] * (2 if r["geometry"] == 4 else 1)
                    for r in inst) / nodes
     peak, peak_kind = peaks()
@@ -530,7 +542,8 @@ def batch_block(args, lbm2d, storage, steps):
     line = {"metric": "batched uneven solves: aggregate GLUPS", "unit": "GLUPS",
             "value": glups, "glups": glups, "sequential_glups": nodes * steps / t_seq / 1e9,
             "speedup_vs_sequential": t_seq / t_bat, "steps": steps, "instances": len(inst), "nodes": nodes,
-            "batch_launches": b.launches - l0, "diverged": nan,
+            "batch_launches": b.launches - l0, "diverged": nan, "diverged_sequential": nan_seq,
+            "kernels": sorted({KERNEL_NAMES[s.info().kernel][0] for s in solvers}),
             "thermal_instances": sum(1 for r in inst if r["geometry"] == 4),
             "alg_bytes_per_update": bytes_lu, "roofline_frac": glups * bytes_lu / peak, "peak_kind": peak_kind,
             "config": {"workload": "256 uneven cavity/step/cylinder solves, sides log-uniform 64-1024, aspect 1-3, "
@@ -936,14 +949,21 @@ def main():
         # the other rows of the metric, on the same GPU after the timed step:
         # storage error against FP64, the thermal step, the C4 batch and the
         # C5 serving stream
-        pe = precision_block(lbm2d, nx, ny, args.precision_steps)
+        def guarded(fn):  # a failing block is reported, never blocks the line
+            try:
+                return fn()
+            except Exception as ex:
+                return {"error": f"{type(ex).__name__}: {ex}"}
+
+        pe = guarded(lambda: precision_block(lbm2d, nx, ny, args.precision_steps))
         line["precision_vs_fp64"] = pe
-        for st, res in pe["results"].items():
+        for st, res in pe.get("results", {}).items():
             if st in prec:
                 prec[st].update({k: res[k] for k in ("velocity_rel_l2_vs_fp64", "drag_rel_err_vs_fp64")})
-        line["thermal"] = thermal_block(lbm2d, torch, args.thermal_n)
-        line["batch"] = {st: batch_block(args, lbm2d, st, args.batch_steps) for st in ("fp32", "fp16")}
-        line["serving"] = serve_block(args, lbm2d)
+        line["thermal"] = guarded(lambda: thermal_block(lbm2d, torch, args.thermal_n))
+        line["batch"] = {st: guarded(lambda st=st: batch_block(args, lbm2d, st, args.batch_steps))
+                         for st in ("fp32", "fp16")}
+        line["serving"] = guarded(lambda: serve_block(args, lbm2d))
     print(json.dumps(line), flush=True)
     reps.close()
     return 0

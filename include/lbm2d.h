@@ -101,6 +101,7 @@ typedef struct lbm2d_info {
 #define LBM2D_KERNEL_SCALAR 0  /* one node per thread */
 #define LBM2D_KERNEL_PAIR 1    /* two x-neighbours per thread, packed FP32x2 */
 #define LBM2D_KERNEL_ROWS 2    /* row tiles staged by bulk copies, persistent grid */
+#define LBM2D_KERNEL_TILES 3   /* flat tiles of consecutive nodes staged by bulk copies (any nx, thermal, batches) */
 
 typedef struct lbm2d_solver lbm2d_solver;
 
@@ -238,16 +239,19 @@ int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
 /* Step-kernel variant.  0 (default): the fastest kernel the configuration
  * allows -- the row pipeline (non-thermal FP32 with nx a multiple of 4, or
  * FP16/BF16 with nx a multiple of 8; in a batch only members of at least
- * 2^20 nodes), else two x-neighbours per thread with packed FP32x2
- * arithmetic (nx even), else one node per thread.  1: one node per thread.
- * 2: two x-neighbours per thread where nx is even.  Same results to
- * rounding; lbm2d_get_info reports the kernel in use. */
+ * 2^20 nodes), else the tile pipeline for the thermal DDF and for batch
+ * members (FP32/FP16/BF16), else two x-neighbours per thread with packed
+ * FP32x2 arithmetic (nx even), else one node per thread.  1: one node per
+ * thread.  2: two x-neighbours per thread where nx is even.  3: the tile
+ * pipeline (FP32/FP16/BF16).  Same results to rounding; lbm2d_get_info
+ * reports the kernel in use. */
 int lbm2d_set_kernel_variant(lbm2d_solver *h, int variant);
-/* Limit, in SM cycles, of the row pipeline's consumer-side waits for its
- * staged tiles (0, the default: about one second).  A wait that runs out
- * makes the kernel stop early and the next lbm2d_synchronize report
- * LBM2D_ERR_TIMEOUT, with the context still usable; a limit of a few cycles
- * exercises that path on purpose (failure-path tests).  The producer's own
+/* Limit, in SM cycles, of the staging pipelines' (row and tile kernels)
+ * consumer-side waits for their staged tiles (0, the default: about one
+ * second).  A wait that runs out makes the kernel stop early and the next
+ * lbm2d_synchronize report LBM2D_ERR_TIMEOUT, with the context still usable.
+ * A negative value is the failure-path test: the producer stages nothing, so
+ * every consumer wait runs out after -cycles cycles.  The producer's own
  * waits keep the default.  No counterpart in the reference. */
 int lbm2d_set_wait_limit(lbm2d_solver *h, long long cycles);
 /* The CUDA stream the handle launches on (cudaStream_t as void*). */

@@ -8,9 +8,10 @@
 //   2. writes the kernel parameters of the next two steps of every member
 //      (ping-pong parity 0 and 1) and the tile-to-instance table (first
 //      launch block of every member) into device arrays,
-//   3. launches, per (storage, thermal) group, one batch_step_kernel that
-//      covers every member's blocks, followed by one batched force reduction,
-//      replaying step pairs from a captured CUDA graph,
+//   3. launches, per (storage, thermal) group, one tile-pipelined kernel
+//      over every member's tiles (FP64 members: one batch_step_kernel over
+//      their blocks), followed by one batched force reduction, replaying step
+//      pairs from a captured CUDA graph,
 //   4. advances every member's state and orders the members' streams after
 //      the batch stream.
 #include <algorithm>
@@ -32,7 +33,14 @@ struct Member {
 
 struct Group {
     int storage = 0, thermal = 0;
-    int kind = 0;  // KERNEL_SCALAR / KERNEL_PAIR (batched launches) or KERNEL_ROWS (solo launches)
+    // KERNEL_TILES / KERNEL_SCALAR / KERNEL_PAIR (batched launches) or
+    // KERNEL_ROWS (solo launches)
+    int kind = 0;
+    // KERNEL_TILES: global tile -> member, first global tile of each member,
+    // and the persistent grid
+    int* d_tile_member = nullptr;
+    int* d_tile_start = nullptr;
+    int ntiles = 0, grid = 0;
     std::vector<KParams> host;  // KERNEL_ROWS: each member's parameters of the call's first step
     std::vector<int> members;  // indices into lbm2d_batch::members
     int nblocks = 0;
@@ -48,6 +56,7 @@ struct Group {
 struct lbm2d_batch {
     int device = 0;
     cudaStream_t stream = nullptr;
+    unsigned int* d_status = nullptr;  // bit 1: a tile-pipeline wait ran out
     cudaEvent_t ev = nullptr;
     std::vector<Member> members;
     std::vector<Group> groups;
@@ -88,6 +97,8 @@ void free_groups(lbm2d_batch* b) {
         cudaFreeAsync(g.d_jobs[0], b->stream);
         cudaFreeAsync(g.d_jobs[1], b->stream);
         cudaFreeAsync(g.d_left, b->stream);
+        if (g.d_tile_member) cudaFreeAsync(g.d_tile_member, b->stream);
+        if (g.d_tile_start) cudaFreeAsync(g.d_tile_start, b->stream);
     }
     b->groups.clear();
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -130,6 +141,29 @@ int build_layout(lbm2d_batch* b) {
         BCK(cudaMallocAsync(&g.d_jobs[1], m * sizeof(ReduceJob), b->stream), "batch jobs");
         BCK(cudaMallocAsync(&g.d_left, 2 * m * sizeof(int), b->stream), "batch budgets");
         g.cap_members = m;
+        if (g.kind == KERNEL_TILES) {
+            // the tile table: member k owns global tiles [start[k], start[k+1])
+            const int tw = tiles_width();
+            std::vector<int> start(m + 1, 0), owner;
+            for (size_t k = 0; k < m; ++k) {
+                const long long nt = ((long long)b->members[g.members[k]].h->N + tw - 1) / tw;
+                if ((long long)start[k] + nt > 0x7FFFFFFF) return bfail(b, LBM2D_ERR_INVALID, "batch: too many tiles");
+                start[k + 1] = start[k] + (int)nt;
+                owner.insert(owner.end(), (size_t)nt, (int)k);
+            }
+            g.ntiles = start[m];
+            g.grid = tiles_grid(g.storage, g.thermal != 0, g.ntiles, b->device);
+            if (g.grid <= 0) return bfail(b, LBM2D_ERR_CUDA, "tile pipeline: no launch configuration");
+            BCK(cudaMallocAsync(&g.d_tile_member, owner.size() * sizeof(int), b->stream), "tile table");
+            BCK(cudaMallocAsync(&g.d_tile_start, start.size() * sizeof(int), b->stream), "tile table");
+            BCK(cudaMemcpyAsync(g.d_tile_member, owner.data(), owner.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                b->stream),
+                "tile table");
+            BCK(cudaMemcpyAsync(g.d_tile_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                b->stream),
+                "tile table");
+            BCK(cudaStreamSynchronize(b->stream), "tile table");  // the host vectors go out of scope
+        }
     }
     b->layout_dirty = false;
     return LBM2D_OK;
@@ -239,8 +273,11 @@ int prepare(lbm2d_batch* b) {
 int launch_one(lbm2d_batch* b, int parity) {
     for (auto& g : b->groups) {
         if (g.kind == KERNEL_ROWS) continue;  // solo members are launched by lbm2d_batch_step
-        int e = launch_batch_step(g.storage, g.d_params[parity], g.d_block_start, (int)g.members.size(), g.nblocks,
-                                  g.thermal, b->bx, b->by, b->stream, g.kind == KERNEL_PAIR ? 1 : 0);
+        int e = g.kind == KERNEL_TILES
+                    ? launch_tiles_batch(g.storage, g.thermal != 0, g.d_params[parity], g.d_tile_member,
+                                         g.d_tile_start, g.ntiles, g.grid, b->d_status, b->stream)
+                    : launch_batch_step(g.storage, g.d_params[parity], g.d_block_start, (int)g.members.size(),
+                                        g.nblocks, g.thermal, b->bx, b->by, b->stream, g.kind == KERNEL_PAIR ? 1 : 0);
         ++b->launches;
         if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
         if (g.njobs > 0) {
@@ -297,7 +334,8 @@ int lbm2d_batch_create(int device, lbm2d_batch** out) {
     auto* b = new lbm2d_batch();
     b->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&b->d_status, 16) != cudaSuccess || cudaMemset(b->d_status, 0, 16) != cudaSuccess) {
         delete b;
         return LBM2D_ERR_CUDA;
     }
@@ -315,6 +353,7 @@ int lbm2d_batch_destroy(lbm2d_batch* b) {
     if (b->h_left) cudaFreeHost(b->h_left);
     cudaEventDestroy(b->ev);
     cudaStreamDestroy(b->stream);
+    cudaFree(b->d_status);
     delete b;
     return LBM2D_OK;
 }
@@ -445,6 +484,12 @@ int lbm2d_batch_synchronize(lbm2d_batch* b) {
     if (!b) return LBM2D_ERR_INVALID;
     cudaSetDevice(b->device);
     BCK(cudaStreamSynchronize(b->stream), "batch sync");
+    unsigned int status = 0;
+    BCK(cudaMemcpy(&status, b->d_status, sizeof(status), cudaMemcpyDeviceToHost), "batch status");
+    if (status) {
+        cudaMemset(b->d_status, 0, sizeof(status));
+        return bfail(b, LBM2D_ERR_TIMEOUT, "a batched tile-pipeline wait exceeded its limit");
+    }
     for (auto& m : b->members) {
         int rc = lbm2d_synchronize(m.h);
         if (rc) return bfail(b, rc, std::string("member: ") + m.h->err);
@@ -515,8 +560,11 @@ int lbm2d_autotune(lbm2d_solver* h, int steps, double tau, double u, int* best_b
     // Candidates: the row pipeline (when the solver would run it), then every
     // block shape of the paired (or scalar) kernel.
     const int v0 = h->variant;
-    const bool rows = kernel_kind(h) == KERNEL_ROWS;
-    const int shape_variant = rows ? 2 : v0;
+    // the persistent kernels (row or tile pipeline) are one candidate; the
+    // block shapes are candidates of the paired (or one-node) kernel
+    const int kind0 = kernel_kind(h);
+    const bool rows = kind0 == KERNEL_ROWS || kind0 == KERNEL_TILES;
+    const int shape_variant = rows ? (use_pair(h) ? 2 : 1) : v0;
     float best = 1e30f;
     int bbx = h->bx, bby = h->by, bvar = v0;
     const int n_cand = (int)(sizeof(kShapes) / sizeof(kShapes[0])) + (rows ? 1 : 0);

@@ -123,6 +123,7 @@ KParams base_params(const lbm2d_solver* h) {
     p.pf.T_ref = float(h->T_ref);
     p.nan_flag = h->d_nan;
     p.consumer_wait = h->consumer_wait;
+    p.inv_nx = 1.0f / float(h->nx);
     p.pair = use_pair(h) ? 1 : 0;
     const int nbw = h->bx * (p.pair ? 2 : 1);  // node width of a block
     p.gx = (h->nx + nbw - 1) / nbw;
@@ -178,7 +179,8 @@ void apply_collide(KParams& p, const CollideParams& c) {
 }
 
 int ensure_populations(lbm2d_solver* h) {
-    const size_t bytes = h->N * 9 * elem_size(h->storage);
+    // 64 bytes of tail padding: the tile pipeline copies whole 16-byte granules
+    const size_t bytes = h->N * 9 * elem_size(h->storage) + 64;
     int rc;
     if ((rc = dalloc(h, &h->P[0], bytes))) return rc;
     if ((rc = dalloc(h, &h->P[1], bytes))) return rc;
@@ -233,7 +235,7 @@ int upload_geometry(lbm2d_solver* h) {
     h->nslots = 0;
     h->slot_bx = h->slot_by = 0;
     int rc;
-    if ((rc = dalloc(h, &h->d_flags, h->N * sizeof(uint32_t)))) return rc;
+    if ((rc = dalloc(h, &h->d_flags, h->N * sizeof(uint32_t) + 64))) return rc;  // granule padding
     CK(cudaMemcpyAsync(h->d_flags, h->geo.flags.data(), h->N * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream),
        "flags H2D");
     const size_t nr = h->geo.rec_info.size();
@@ -259,10 +261,14 @@ bool use_pair(const lbm2d_solver* h) {
 }
 
 int kernel_kind(const lbm2d_solver* h) {
+    const bool tiles_ok = h->storage != ST_FP64;
+    if (h->variant == 3 && tiles_ok) return KERNEL_TILES;
+    if (h->variant == 0 && tiles_ok) {
+        if (rows_eligible(h->storage, h->nx, h->ny, h->thermal) && (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
+            return KERNEL_ROWS;
+        if (h->thermal || h->in_batch) return KERNEL_TILES;
+    }
     if (!use_pair(h)) return KERNEL_SCALAR;
-    if (h->variant == 0 && rows_eligible(h->storage, h->nx, h->ny, h->thermal) &&
-        (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
-        return KERNEL_ROWS;
     return KERNEL_PAIR;
 }
 
@@ -273,15 +279,40 @@ int kernel_kind(const lbm2d_solver* h) {
 int ensure_slots(lbm2d_solver* h) {
     const int kind = kernel_kind(h);
     int grid = 0;
+    const long long ntiles = ((long long)h->N + tiles_width() - 1) / tiles_width();
     if (kind == KERNEL_ROWS) {
         grid = rows_grid(h->storage, h->nx, h->ny, h->device);
         if (grid <= 0) return fail(h, LBM2D_ERR_CUDA, "row pipeline: no launch configuration");
+    } else if (kind == KERNEL_TILES) {
+        grid = tiles_grid(h->storage, h->thermal, ntiles, h->device);
+        if (grid <= 0) return fail(h, LBM2D_ERR_CUDA, "tile pipeline: no launch configuration");
     }
+    const bool persistent = kind == KERNEL_ROWS || kind == KERNEL_TILES;
     if (h->slot_kind == kind && h->d_block_slot &&
-        (kind == KERNEL_ROWS ? h->slot_grid == grid : (h->slot_bx == h->bx && h->slot_by == h->by)))
+        (persistent ? h->slot_grid == grid : (h->slot_bx == h->bx && h->slot_by == h->by)))
         return LBM2D_OK;
     std::vector<int> slots;
-    if (kind == KERNEL_ROWS) {
+    int red_blocks = 0;
+    if (kind == KERNEL_TILES) {
+        // one entry per tile of W consecutive nodes: the first of the tile's
+        // per-warp slots, -1 for a tile without force nodes; then one entry
+        // per CTA of a single-instance launch (tile t runs on CTA t mod
+        // grid): 1 when it holds force tiles, the CTAs the fused second stage
+        // counts
+        const int tw = tiles_width(), warps = tiles_warps();
+        slots.assign((size_t)ntiles + (size_t)grid, -1);
+        for (size_t r = 0; r < h->geo.rec_force.size(); ++r)
+            if (h->geo.rec_force[r]) slots[(size_t)(h->geo.rec_node[r] / tw)] = 0;
+        int k = 0;
+        for (size_t t = 0; t < (size_t)ntiles; ++t)
+            if (slots[t] == 0) {
+                slots[t] = k;
+                k += warps;
+                slots[(size_t)ntiles + t % (size_t)grid] = 1;
+            }
+        for (int c = 0; c < grid; ++c) red_blocks += slots[(size_t)ntiles + c] > 0 ? 1 : 0;
+        h->nslots = k;
+    } else if (kind == KERNEL_ROWS) {
         const int tw = rows_tile_width(), tpr = (h->nx + tw - 1) / tw, warps = rows_warps_per_block();
         slots.assign((size_t)grid, -1);
         for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
@@ -309,9 +340,10 @@ int ensure_slots(lbm2d_solver* h) {
     CK(cudaMemcpyAsync(h->d_block_slot, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream),
        "slots H2D");
     // arrival count of the fused second stage (blocks holding slots)
-    h->red_blocks = 0;
-    for (int s : slots)
-        if (s >= 0) ++h->red_blocks;
+    h->red_blocks = red_blocks;
+    if (kind != KERNEL_TILES)
+        for (int s : slots)
+            if (s >= 0) ++h->red_blocks;
     if (!h->d_red_done) {
         if ((rc = dalloc(h, &h->d_red_done, sizeof(unsigned int)))) return rc;
         CK(cudaMemsetAsync(h->d_red_done, 0, sizeof(unsigned int), h->stream), "reduction count");
@@ -723,7 +755,7 @@ int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0, cudaEvent_t e1)
     // when every block has the 128 threads it needs (the row pipeline has 256
     // consumers); otherwise in its own launch
     const bool fused = h->nslots > 0 && h->red_blocks > 0 &&
-                       (h->slot_kind == KERNEL_ROWS || h->bx * h->by >= 128);
+                       (h->slot_kind == KERNEL_ROWS || h->slot_kind == KERNEL_TILES || h->bx * h->by >= 128);
     p.red_done = fused ? h->d_red_done : nullptr;
     p.red_hist = h->d_hist;
     p.red_counter = h->d_counter;
@@ -732,8 +764,9 @@ int launch_one_step(lbm2d_solver* h, KParams& p, cudaEvent_t e0, cudaEvent_t e1)
     p.red_nslots = h->nslots;
     p.red_cap = h->hist_cap;
     if (e0) CK(cudaEventRecord(e0, h->stream), "event");
-    int e = h->slot_kind == KERNEL_ROWS ? launch_rows(h->storage, p, h->slot_grid, h->stream)
-                                        : launch_step(h->storage, p, h->bx, h->by, h->stream);
+    int e = h->slot_kind == KERNEL_ROWS    ? launch_rows(h->storage, p, h->slot_grid, h->stream)
+            : h->slot_kind == KERNEL_TILES ? launch_tiles_single(h->storage, p, h->slot_grid, h->stream)
+                                           : launch_step(h->storage, p, h->bx, h->by, h->stream);
     if (e1) CK(cudaEventRecord(e1, h->stream), "event");
     ++h->launches;
     if (e) return cuda_fail(h, (cudaError_t)e, "step kernel");
@@ -1169,7 +1202,6 @@ int lbm2d_profile(lbm2d_solver* h, double* ms, long long* n) {
 int lbm2d_set_wait_limit(lbm2d_solver* h, long long cycles) {
     int rc;
     if ((rc = check_handle(h))) return rc;
-    if (cycles < 0) return fail(h, LBM2D_ERR_INVALID, "negative wait limit");
     h->consumer_wait = cycles;
     return LBM2D_OK;
 }
@@ -1177,7 +1209,7 @@ int lbm2d_set_wait_limit(lbm2d_solver* h, long long cycles) {
 int lbm2d_set_kernel_variant(lbm2d_solver* h, int variant) {
     int rc;
     if ((rc = check_handle(h))) return rc;
-    if (variant < 0 || variant > 2) return fail(h, LBM2D_ERR_INVALID, "unknown kernel variant");
+    if (variant < 0 || variant > 3) return fail(h, LBM2D_ERR_INVALID, "unknown kernel variant");
     if (variant == h->variant) return LBM2D_OK;
     if ((rc = before_setting_change(h))) return rc;  // the stored state stays valid; rebuild for safety
     h->variant = variant;

@@ -115,11 +115,16 @@ struct KParams {
     unsigned long long* red_counter;
     double* red_last;
     int red_blocks, red_nslots, red_cap, red_pad;
-    // limit, in SM cycles, of the row pipeline's consumer-side waits on its
-    // staged tiles (0: the default of about one second); the producer's own
-    // waits keep the default
+    // limit, in SM cycles, of the staging pipelines' consumer-side waits on
+    // their staged tiles (0: the default of about one second); the producer's
+    // own waits keep the default.  Negative: failure-path test -- the
+    // producer stages nothing and every consumer wait runs out after
+    // -consumer_wait cycles.
     long long consumer_wait;
-    long long pad_tail;
+    // tile pipeline (lbm2d_tiles.cu): 1 / nx for the node coordinates of a
+    // flat tile, and the per-tile force-slot table is block_slot
+    float inv_nx;
+    int pad_tail;
 };
 static_assert(sizeof(KParams) % 16 == 0, "KParams is staged with 16-byte copies");
 
@@ -205,6 +210,20 @@ int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, dou
                             void* stream);
 int launch_force_reduce(const double* partials, int nslots, double* hist, int hist_cap,
                         unsigned long long* counter, double* last, void* stream);
+
+// Tile-pipelined step (lbm2d_tiles.cu): the lattice of each instance is cut
+// into flat tiles of tiles_width() consecutive nodes (row-major, any nx), whose
+// nine (thermal: eighteen) source windows, flags and -- in a batch -- the
+// instance's parameters are staged by bulk copies; a persistent grid walks
+// the tiles of one instance (single) or of many (tile_member[t] = instance of
+// global tile t, tile_start[k] = its first global tile).  The force slots of
+// an instance are per tile: block_slot[tile] = first of tiles_warps() slots.
+int tiles_width();
+int tiles_warps();
+int tiles_grid(int storage, bool thermal, long long ntiles, int device);  // 0 on error
+int launch_tiles_single(int storage, const KParams& p, int grid, void* stream);
+int launch_tiles_batch(int storage, bool thermal, const KParams* inst, const int* tile_member, const int* tile_start,
+                       int ntiles, int grid, unsigned int* status, void* stream);
 
 // Row-pipelined step (lbm2d_rows.cu): persistent grid of `grid` CTAs, each
 // walking row tiles of rows_tile_width() nodes; p.block_slot has one entry

@@ -88,7 +88,7 @@ extern "C" int lbm2d_step_noalloc(lbm2d_solver* h, double tau, double u_inflow, 
     const int kind = kernel_kind(h);
     double* scratch = scratch_of(h->device);
     if (h->staged || h->geom_dirty || !(c == h->cp_of_P) || h->slot_kind != kind || !h->d_block_slot ||
-        (kind != KERNEL_ROWS && (h->slot_bx != h->bx || h->slot_by != h->by)) || !scratch)
+        (kind != KERNEL_ROWS && kind != KERNEL_TILES && (h->slot_bx != h->bx || h->slot_by != h->by)) || !scratch)
         return fail(h, LBM2D_ERR_STATE,
                     "lbm2d_step_noalloc needs a solver prepared by lbm2d_step with the same tau and settings");
     if (h->nslots > kNoAllocMaxSlots)

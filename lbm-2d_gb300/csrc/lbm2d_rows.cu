@@ -27,7 +27,7 @@
 #include <algorithm>
 #include <atomic>
 
-#include "lbm2d_device.cuh"
+#include "lbm2d_pipeline.cuh"
 
 namespace lbm2d {
 namespace {
@@ -35,7 +35,6 @@ namespace {
 constexpr int kConsumerWarps = 8;
 constexpr int kThreads = 32 * (kConsumerWarps + 1);
 constexpr int kTileW = 2 * 32 * kConsumerWarps;  // nodes per row tile
-constexpr long long kWaitCycles = 2000000000LL;  // about one second at 2 GHz
 
 template <class T>
 struct RowsCfg {
@@ -58,54 +57,6 @@ struct RowsCfg {
     static constexpr int SMEM = ACC_OFF + 32 * kConsumerWarps * 16;
     static_assert(ROW_BYTES % 16 == 0 && FLAGS_OFF % 16 == 0, "bulk-copy alignment");
 };
-
-// ----------------------------------------------------------------- PTX wrappers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase of parity `parity` to complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = kWaitCycles) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > limit) return false;
-    return true;
-}
-
-// Global -> shared bulk copy completing `bytes` on the mbarrier (16-byte
-// aligned addresses, size a multiple of 16).
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-        "l"(src), "r"(bytes), "r"(bar)
-        : "memory");
-}
 
 // ----------------------------------------------------------------- producer
 // Bytes the copies of the tile starting at x0 complete on its mbarrier.
@@ -321,6 +272,7 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
 
     if (warp == kConsumerWarps) {  // producer
         if (lane != 0) return;
+        if (p.consumer_wait < 0) return;  // failure-path test: nothing is staged, every consumer wait runs out
         int k = 0;  // tiles issued
         bool ok = true;
         int y = y_first, seg = seg_first;
@@ -357,7 +309,8 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
         pass_seed(p, s, blockIdx.x == 0 && threadIdx.x == 0);
     }
     const bool force = p.block_slot != nullptr;
-    const long long wait_limit = p.consumer_wait > 0 ? p.consumer_wait : kWaitCycles;
+    const long long wait_limit = p.consumer_wait != 0 ? (p.consumer_wait > 0 ? p.consumer_wait : -p.consumer_wait)
+                                                      : kWaitCycles;
     int y = y_first, seg = seg_first, s = 0;
     uint32_t phase = 0;
     while (y < p.ny) {

@@ -101,8 +101,9 @@ struct lbm2d_solver {
     long long steps_done = 0;
     long long launches = 0;
     int bx = 128, by = 2;
-    // 0: fastest kernel the configuration allows (row pipeline, else paired,
-    // else one node per thread), 1: one node per thread, 2: paired nodes
+    // 0: fastest kernel the configuration allows (row pipeline; the tile
+    // pipeline for the thermal DDF; else paired, else one node per thread),
+    // 1: one node per thread, 2: paired nodes, 3: the tile pipeline
     int variant = 0;
     bool in_batch = false;  // a batch member is stepped by the batched kernels
     bool profiling = false;
@@ -159,12 +160,14 @@ void ibm_release(lbm2d_solver* h);
 // Two x-neighbours per thread (packed FP32x2 collision) when nx is even and
 // the step is non-thermal FP32/FP16/BF16.
 bool use_pair(const lbm2d_solver* h);
-// Step kernel of the next step: KERNEL_SCALAR, KERNEL_PAIR or KERNEL_ROWS
-// (the bulk-copy row pipeline).  Batch members run the batched scalar /
-// paired kernels, except members of at least kBatchSoloNodes nodes that
-// qualify for the row pipeline: those fill the GPU alone and get their own
-// row-pipeline launches inside the batch's step.
-enum KernelKind : int { KERNEL_SCALAR = 0, KERNEL_PAIR = 1, KERNEL_ROWS = 2 };
+// Step kernel of the next step: KERNEL_SCALAR, KERNEL_PAIR, KERNEL_ROWS
+// (the bulk-copy row pipeline) or KERNEL_TILES (the bulk-copy tile pipeline:
+// any nx, the thermal DDF, batches).  Batch members run the batched tile
+// kernel (FP64 storage: the batched one-node kernel), except members of at
+// least kBatchSoloNodes nodes that qualify for the row pipeline: those fill
+// the GPU alone and get their own row-pipeline launches inside the batch's
+// step.
+enum KernelKind : int { KERNEL_SCALAR = 0, KERNEL_PAIR = 1, KERNEL_ROWS = 2, KERNEL_TILES = 3 };
 constexpr long long kBatchSoloNodes = 1LL << 20;
 int kernel_kind(const lbm2d_solver* h);
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the

@@ -1,0 +1,576 @@
+// lbm2d_tiles.cu -- the tile-pipelined step kernel (sm_103a): any grid width,
+// the thermal double distribution, and many instances in one launch.
+//
+// The same step as the row pipeline (pull, rebuild, force, collision, store)
+// with a different unit of work:
+//
+//   * a tile is W = 512 CONSECUTIVE nodes of an instance in row-major order
+//     (it may span several short rows or part of a long one).  In that order
+//     the pull source of direction j is node n - cy_j*nx - cx_j, so the
+//     sources of a whole tile are one contiguous window per direction.  The
+//     producer's elected lane brings each window, rounded out to 16-byte
+//     granules (the window's first element sits `lead` elements into the
+//     staged row), the tile's flags and -- in a batch -- the instance's
+//     parameters into a shared-memory stage with cp.async.bulk copies that
+//     complete on the stage's mbarrier.  No alignment of nx is needed;
+//   * nodes on the lattice border (x = 0, nx-1 or y = 0, ny-1), whose
+//     periodic sources lie outside the window, and nodes that need more than
+//     the plain pull (solid, boundary record, a thermal hook row or column)
+//     are rebuilt from global memory with the per-node functions every step
+//     kernel shares;
+//   * a persistent grid walks the tiles t = blockIdx.x, blockIdx.x + G, ...
+//     of one instance, or of all instances of a batch (tile_member[t] names
+//     the instance).  The producer skips the tiles of an instance whose step
+//     budget is spent and ends the ring with a marker stage;
+//   * consumers: 8 warps, each lane owns two consecutive nodes of the tile.
+//     Non-thermal pairs collide with the packed FP32x2 collision
+//     (collide_pair_dev) and store as pairs (the paired kernels' rounding
+//     noise), thermal nodes collide one at a time (collide_dev<true>) with
+//     the one-node kernel's per-node noise;
+//   * momentum exchange: FP64 per lane in shared memory, an FP64 warp sum per
+//     tile into the instance's per-tile slots (fixed order, so the same
+//     instance gives the same bits alone or in any mix); a single instance
+//     fuses the second stage into its last force CTA.
+// Every wait is bounded (about one second); a wait that runs out sets bit 1
+// of the status word and the CTA leaves after draining its copies.
+#include <algorithm>
+#include <atomic>
+
+#include "lbm2d_pipeline.cuh"
+
+namespace lbm2d {
+namespace {
+
+constexpr int kTWarps = 8;
+constexpr int kTThreads = 32 * (kTWarps + 1);
+constexpr int kTW = 2 * 32 * kTWarps;  // nodes per tile
+
+template <class T, bool TH>
+struct TilesCfg {
+    static constexpr int ES = (int)sizeof(T);
+    static constexpr int EPG = 16 / ES;         // elements per 16-byte granule
+    static constexpr int WIN = kTW + 2 * EPG;   // staged elements per window (lead + W + 2 rounded up)
+    static constexpr int ROWB = WIN * ES;
+    static constexpr int NWIN = TH ? 18 : 9;
+    static constexpr int FLAGS_OFF = NWIN * ROWB;
+    static constexpr int PAR_OFF = FLAGS_OFF + kTW * 4;
+    static constexpr int HDR_OFF = PAR_OFF + (int)sizeof(KParams);
+    static constexpr int STAGE_BYTES = (HDR_OFF + 32 + 127) / 128 * 128;
+    // ring depth and residency: FP32 moves twice the bytes per node of the
+    // 16-bit forms, the thermal form twice again
+    static constexpr int STAGES = TH ? (ES == 4 ? 2 : 3) : (ES == 4 ? 3 : 5);
+    static constexpr int MIN_BLOCKS = ES == 4 ? 2 : 3;
+    static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
+    static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;
+    static constexpr int SMEM = ACC_OFF + 32 * kTWarps * 16;
+    static_assert(ROWB % 16 == 0 && FLAGS_OFF % 16 == 0 && PAR_OFF % 16 == 0, "bulk-copy alignment");
+    static_assert(sizeof(KParams) % 16 == 0, "parameter copy size");
+    static_assert(SMEM <= 227 * 1024, "shared memory");
+};
+
+// Stage header, written by the producer before it arrives on the stage:
+// instance (-1: end of the ring), first node, its (x, y), rounding seed,
+// tile index within the instance, the nine window leads (3 bits each) and the
+// tile's first force slot (-1: none).
+struct TileHdr {
+    int k, n0, x0, y0;
+    uint32_t seed;
+    int tile, leads, slot;
+};
+static_assert(sizeof(TileHdr) == 32, "header size");
+
+// Window j of a tile starting at node n0: global element g = j*N + n0 -
+// cy_j*nx - 1 (the source of the tile's first node for cx = +1), rounded down
+// to a granule: the staged row starts at a = g - lead.
+__device__ __forceinline__ long long win_start(long long N, int nx, int n0, int j, int epg, int& lead) {
+    const long long g = (long long)j * N + n0 - (long long)CYf(j) * nx - 1;
+    const long long a = g >= 0 ? (g / epg) * epg : -((-g + epg - 1) / epg) * epg;
+    lead = (int)(g - a);
+    return a;
+}
+
+// Issue (or, with issue = false, count) the copies of one population set's
+// nine windows into rows [w0, w0 + 9) of the stage.
+template <class T, bool TH>
+__device__ __forceinline__ uint32_t set_copies(const T* __restrict__ P, long long N, int nx, int n0, uint32_t st,
+                                               int w0, uint32_t bar, bool issue, int* leads) {
+    using C = TilesCfg<T, TH>;
+    const long long gend = (9 * N + C::EPG - 1) / C::EPG * C::EPG;  // population buffers are padded to it
+    uint32_t bytes = 0;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        int lead;
+        const long long a = win_start(N, nx, n0, j, C::EPG, lead);
+        const long long cs = max(a, 0LL), ce = min(a + C::WIN, gend);
+        if (leads) *leads |= lead << (3 * j);
+        if (ce > cs) {
+            const uint32_t nb = (uint32_t)((ce - cs) * C::ES);
+            if (issue) bulk_g2s(st + (uint32_t)((w0 + j) * C::ROWB) + (uint32_t)((cs - a) * C::ES), P + cs, nb, bar);
+            bytes += nb;
+        }
+    }
+    return bytes;
+}
+
+// Parameters a consumer reads for the tile: the instance's own copy in the
+// stage (batch) or the kernel parameter (single instance).
+template <bool SINGLE>
+__device__ __forceinline__ const KParams& tile_params(const KParams& single, const unsigned char* stage,
+                                                      int par_off) {
+    if constexpr (SINGLE) return single;
+    else return *reinterpret_cast<const KParams*>(stage + par_off);
+}
+
+// ----------------------------------------------------------------- producer
+template <class T, bool TH, bool SINGLE>
+__device__ void tiles_produce(const KParams& single, const KParams* __restrict__ inst,
+                              const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
+                              unsigned char* smem, uint32_t sbase, uint32_t full0, uint32_t empty0,
+                              unsigned int* status) {
+    using C = TilesCfg<T, TH>;
+    int issued = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int k = 0, tl = t;
+        const KParams* gpp = &single;
+        if constexpr (!SINGLE) {
+            k = __ldg(tile_member + t);
+            tl = t - __ldg(tile_start + k);
+            gpp = inst + k;
+        }
+        const KParams& gp = *gpp;
+        // step budget: an instance whose budget is spent takes no step; the
+        // CTA holding its first tile hands the decremented budget on
+        const int* li = gp.left_in;
+        const int L = li ? *li : 1;
+        if (li && tl == 0) *gp.left_out = L > 0 ? L - 1 : 0;
+        if (L <= 0) continue;
+        // rounding seed, handed on by the CTA holding the first tile
+        const uint32_t seed = gp.seed_in ? *gp.seed_in : gp.seed_host;
+        if (tl == 0 && gp.seed_out) *gp.seed_out = seed + 1u;
+        const int s = issued % C::STAGES, n = issued / C::STAGES;
+        if (n > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1))) {
+            ok = false;
+            break;
+        }
+        const uint32_t st = sbase + (uint32_t)(s * C::STAGE_BYTES);
+        const uint32_t bar = full0 + 8 * s;
+        const long long N = gp.N;
+        const int nx = gp.nx;
+        const int n0 = tl * kTW;
+        const T* Pf = static_cast<const T*>(gp.fin);
+        const T* Pg = static_cast<const T*>(gp.gin);
+        // bytes first (the mbarrier expects them before the copies land)
+        int leads = 0;
+        uint32_t bytes = set_copies<T, TH>(Pf, N, nx, n0, st, 0, bar, false, &leads);
+        if (TH) bytes += set_copies<T, TH>(Pg, N, nx, n0, st, 9, bar, false, nullptr);
+        const uint32_t fbytes = (uint32_t)(((min((long long)kTW, N - n0) * 4) + 15) / 16 * 16);
+        bytes += fbytes;
+        if (!SINGLE) bytes += (uint32_t)sizeof(KParams);
+        TileHdr* h = reinterpret_cast<TileHdr*>(smem + s * C::STAGE_BYTES + C::HDR_OFF);
+        h->k = k;
+        h->n0 = n0;
+        h->x0 = n0 % nx;
+        h->y0 = n0 / nx;
+        h->seed = seed;
+        h->tile = tl;
+        h->leads = leads;
+        h->slot = gp.block_slot ? __ldg(gp.block_slot + tl) : -1;
+        mbar_expect_tx(bar, bytes);  // release: the header is visible with the stage
+        set_copies<T, TH>(Pf, N, nx, n0, st, 0, bar, true, nullptr);
+        if (TH) set_copies<T, TH>(Pg, N, nx, n0, st, 9, bar, true, nullptr);
+        bulk_g2s(st + C::FLAGS_OFF, gp.flags + n0, fbytes, bar);
+        if (!SINGLE) bulk_g2s(st + C::PAR_OFF, &gp, (uint32_t)sizeof(KParams), bar);
+        ++issued;
+    }
+    // end marker: a stage whose header says k = -1, completed by a plain arrival
+    if (ok) {
+        const int s = issued % C::STAGES, n = issued / C::STAGES;
+        if (n > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1))) {
+            ok = false;
+        } else {
+            reinterpret_cast<TileHdr*>(smem + s * C::STAGE_BYTES + C::HDR_OFF)->k = -1;
+            mbar_arrive(full0 + 8 * s);
+        }
+    }
+    // every issued copy completes before the CTA may exit (the stage of tile
+    // issued - STAGES, if any, was refilled or consumed already)
+    bool drained = true;
+    for (int i = max(issued - C::STAGES + 1, 0); i < issued; ++i)
+        drained = mbar_wait(full0 + 8 * (i % C::STAGES), (uint32_t)((i / C::STAGES) & 1)) && drained;
+    if (!ok || !drained) atomicOr(status, 2u);
+}
+
+// ----------------------------------------------------------------- consumer
+// Node coordinates of local node i of a tile whose first node is (x0, y0):
+// a = x0 + i < nx + W, so a single-precision quotient estimate is off by at
+// most one.
+__device__ __forceinline__ void tile_xy(int x0, int y0, int i, int nx, float inv_nx, int& x, int& y) {
+    const int a = x0 + i;
+    int q = (int)(__int2float_rn(a) * inv_nx);
+    int r = a - q * nx;
+    if (r < 0) {
+        --q;
+        r += nx;
+    } else if (r >= nx) {
+        ++q;
+        r -= nx;
+    }
+    x = r;
+    y = y0 + q;
+}
+
+__device__ __forceinline__ bool border(const KParams& p, int x, int y) {
+    return x == 0 || x == p.nx - 1 || y == 0 || y == p.ny - 1;
+}
+
+// Staged value of direction j (window w) for local node i, storage units.
+template <class T, bool TH>
+__device__ __forceinline__ float staged(const unsigned char* stage, int w, int lead, int i, int cx) {
+    using C = TilesCfg<T, TH>;
+    const T* r = reinterpret_cast<const T*>(stage + w * C::ROWB);
+    if constexpr (std::is_same<T, float>::value) return r[lead + i + 1 - cx];
+    else if constexpr (std::is_same<T, __half>::value) return __half2float(r[lead + i + 1 - cx]);
+    else return __bfloat162float(r[lead + i + 1 - cx]);
+}
+
+// Two x-neighbours in storage units stored as a pair, or as two elements
+// (element j*N + n odd for odd N and odd j) with the same rounding bits.
+template <class T>
+__device__ __forceinline__ void store_two(T* __restrict__ base, size_t n, float a, float b, uint32_t rb, bool pair,
+                                          bool vb) {
+    if (pair && vb) {
+        PairStore<T>::st(base, n, a, b, rb);
+        return;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        base[n] = a;
+        if (vb) base[n + 1] = b;
+    } else {
+        const uint32_t w = std::is_same<T, __half>::value ? cvt_rs_f16x2(a, b, rb) : cvt_rs_bf16x2(a, b, rb);
+        reinterpret_cast<unsigned short*>(base)[n] = (unsigned short)(w & 0xFFFFu);
+        if (vb) reinterpret_cast<unsigned short*>(base)[n + 1] = (unsigned short)(w >> 16);
+    }
+}
+
+// Momentum exchange of one fluid boundary node from its post-stream full
+// populations f (FP32 values), added in FP64 to the lane's accumulator.
+__device__ __forceinline__ void add_force(const KParams& p, uint32_t fl, const float f[9], double2* acc) {
+    const uint32_t m = p.rec_force[fl >> 2];
+    if (!m) return;
+    double ax = acc->x, ay = acc->y;
+#pragma unroll
+    for (int j = 1; j < 9; ++j)
+        if (m & (1u << j)) {
+            ax -= double(CXf(j)) * 2.0 * double(f[j]);
+            ay -= double(CYf(j)) * 2.0 * double(f[j]);
+        }
+    *acc = make_double2(ax, ay);
+}
+
+// Non-thermal: nodes i, i+1 of the tile (pair), as consume_pair of the row
+// pipeline with window pulls.
+template <class T>
+__device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char* stage, const TileHdr& h, int i,
+                                          uint32_t skey, double2* acc) {
+    using C = TilesCfg<T, false>;
+    constexpr float iS = Pop<T>::kInvS;
+    const long long N = p.N;
+    const unsigned na = (unsigned)h.n0 + (unsigned)i;
+    const bool vb = (long long)na + 1 < N;
+    int xa, ya, xb, yb;
+    tile_xy(h.x0, h.y0, i, p.nx, p.inv_nx, xa, ya);
+    xb = xa + 1;
+    yb = ya;
+    if (xb == p.nx) {
+        xb = 0;
+        ++yb;
+    }
+    const uint32_t* sfl = reinterpret_cast<const uint32_t*>(stage + C::FLAGS_OFF);
+    const uint32_t fla = sfl[i];
+    const uint32_t flb = vb ? sfl[i + 1] : FLAG_SOLID;
+    const bool oka = !(fla & FLAG_SOLID), okb = vb && !(flb & FLAG_SOLID);
+    const bool sa = border(p, xa, ya) || special_node<false>(p, xa, ya, fla);
+    const bool sb = vb && (border(p, xb, yb) || special_node<false>(p, xb, yb, flb));
+    float da[9], db[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const int lead = (h.leads >> (3 * j)) & 7;
+        da[j] = staged<T, false>(stage, j, lead, i, CXf(j));
+        db[j] = staged<T, false>(stage, j, lead, i + 1, CXf(j));
+    }
+    if (sa) build_dev_s<T>(p, xa, ya, fla, da);
+    if (sb) build_dev_s<T>(p, xb, yb, flb, db);
+    if (h.slot >= 0 && ((fla | flb) & FLAG_BOUNDARY)) {
+        float f[9];
+        if (oka && (fla & FLAG_BOUNDARY)) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) f[j] = fmaf(da[j], iS, p.shf[j]);
+            add_force(p, fla, f, acc);
+        }
+        if (okb && (flb & FLAG_BOUNDARY)) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) f[j] = fmaf(db[j], iS, p.shf[j]);
+            add_force(p, flb, f, acc);
+        }
+    }
+    if (oka || okb) {
+        F2 f[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) f[j] = mk2(da[j], db[j]);
+        collide_pair_dev<T>(p, fla, flb, oka, okb, f);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            da[j] = f[j].v.x;
+            db[j] = f[j].v.y;
+        }
+    }  // solid nodes hold the solid state from build_dev_s
+    const bool settled = p.skip_settled_solids != 0;
+    const bool skip_a = !oka && settled && xa > 0 && xa < p.nx - 1 && ya < p.ny - 1;
+    const bool skip_b = !vb || (!okb && settled && xb > 0 && xb < p.nx - 1 && yb < p.ny - 1);
+    if (!(skip_a && skip_b)) {
+        T* __restrict__ Fo = static_cast<T*>(p.fout);
+        uint32_t rb[9] = {};
+        if constexpr (Pop<T>::kRounds) rand9(skey + na, rb);
+        const bool even_n = (N & 1) == 0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j)
+            store_two<T>(Fo + (size_t)j * (size_t)N, na, da[j], db[j], rb[j], even_n || (j & 1) == 0, vb);
+    }
+}
+
+// Thermal: one node of the tile (local index i), as step_block<T, true>.
+template <class T>
+__device__ __forceinline__ void tile_node_th(const KParams& p, const unsigned char* stage, const TileHdr& h, int i,
+                                             uint32_t skey, double2* acc) {
+    using C = TilesCfg<T, true>;
+    constexpr float iS = Pop<T>::kInvS;
+    const long long N = p.N;
+    const unsigned n = (unsigned)h.n0 + (unsigned)i;
+    int x, y;
+    tile_xy(h.x0, h.y0, i, p.nx, p.inv_nx, x, y);
+    const uint32_t fl = reinterpret_cast<const uint32_t*>(stage + C::FLAGS_OFF)[i];
+    float d[9], e[9];  // deviations
+    if (border(p, x, y) || special_node<true>(p, x, y, fl)) {
+        build_dev<T, true>(p, x, y, fl, d, e);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const int lead = (h.leads >> (3 * j)) & 7;
+            d[j] = staged<T, true>(stage, j, lead, i, CXf(j)) * iS;
+            e[j] = staged<T, true>(stage, 9 + j, lead, i, CXf(j)) * iS;
+        }
+    }
+    const bool ok = !(fl & FLAG_SOLID);
+    if (ok) {
+        if (h.slot >= 0 && (fl & FLAG_BOUNDARY)) {
+            float f[9];
+#pragma unroll
+            for (int j = 0; j < 9; ++j) f[j] = d[j] + p.shf[j];
+            add_force(p, fl, f, acc);
+        }
+        collide_dev<true>(p, fl, d, e);
+    }
+    if (!(!ok && p.skip_settled_solids && x > 0 && x < p.nx - 1 && y < p.ny - 1)) {
+        T* __restrict__ Fo = static_cast<T*>(p.fout);
+        T* __restrict__ Go = static_cast<T*>(p.gout);
+        uint32_t rb[9] = {};
+        if constexpr (Pop<T>::kRounds) rand9(skey + n, rb);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) Pop<T>::std_(Fo + (size_t)j * (size_t)N, n, d[j], rb[j]);
+        if constexpr (Pop<T>::kRounds) rand9((skey + n) ^ 0x6A09E667u, rb);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) Pop<T>::std_(Go + (size_t)j * (size_t)N, n, e[j], rb[j]);
+    }
+}
+
+template <class T, bool TH, bool SINGLE>
+__device__ void tiles_consume(const KParams& single, unsigned char* smem, uint32_t full0, uint32_t empty0,
+                              unsigned int* status) {
+    using C = TilesCfg<T, TH>;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x;  // consumer thread 0..255
+    double2* acc = reinterpret_cast<double2*>(smem + C::ACC_OFF);
+    const long long cw = single.consumer_wait;
+    const long long wait_limit = cw != 0 ? (cw > 0 ? cw : -cw) : kWaitCycles;
+    int s = 0;
+    uint32_t phase = 0;
+    for (;;) {
+        if (!__all_sync(0xffffffffu, mbar_wait(full0 + 8 * s, phase, wait_limit))) {
+            if (lane == 0) atomicOr(status, 2u);
+            break;
+        }
+        const unsigned char* stage = smem + s * C::STAGE_BYTES;
+        const TileHdr h = *reinterpret_cast<const TileHdr*>(stage + C::HDR_OFF);
+        if (h.k < 0) break;
+        const KParams& p = tile_params<SINGLE>(single, stage, C::PAR_OFF);
+        const uint32_t skey = Pop<T>::kRounds ? seed_key(h.seed) : 0u;
+        if (h.slot >= 0) acc[tid] = make_double2(0.0, 0.0);
+        const int i = 2 * tid;
+        if ((long long)h.n0 + i < p.N) {
+            if constexpr (TH) {
+                tile_node_th<T>(p, stage, h, i, skey, acc + tid);
+                if ((long long)h.n0 + i + 1 < p.N) tile_node_th<T>(p, stage, h, i + 1, skey, acc + tid);
+            } else {
+                tile_pair<T>(p, stage, h, i, skey, acc + tid);
+            }
+        }
+        if (h.slot >= 0) {
+            // FP64 warp sum of the tile's link terms into its per-warp slot
+            double a = acc[tid].x, b = acc[tid].y;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_down_sync(0xffffffffu, a, o);
+                b += __shfl_down_sync(0xffffffffu, b, o);
+            }
+            if (lane == 0) {
+                p.partials[2 * (h.slot + warp)] = a;
+                p.partials[2 * (h.slot + warp) + 1] = b;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8 * s);
+        if (++s == C::STAGES) {
+            s = 0;
+            phase ^= 1u;
+        }
+    }
+    if constexpr (SINGLE) {
+        // the drag/lift second stage in the last CTA holding force tiles: the
+        // host marks those CTAs (tile t runs on CTA t mod grid) after the
+        // per-tile entries of the slot table, so every marked CTA counts
+        // itself even when one of its waits ran out
+        const int ntiles = (int)((single.N + kTW - 1) / kTW);
+        if (single.red_done && single.block_slot && __ldg(single.block_slot + ntiles + blockIdx.x) > 0)
+            fused_force_finish(single, tid, [] { asm volatile("bar.sync 1, 256;" ::: "memory"); });
+    }
+}
+
+template <class T, bool TH, bool SINGLE>
+__global__ void __launch_bounds__(kTThreads, TilesCfg<T, TH>::MIN_BLOCKS)
+    step_tiles_kernel(const __grid_constant__ KParams single, const KParams* __restrict__ inst,
+                      const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
+                      unsigned int* status) {
+    using C = TilesCfg<T, TH>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const uint32_t sbase = smem_u32(smem);
+    const uint32_t full0 = sbase + C::BAR_OFF, empty0 = full0 + 8 * C::STAGES;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C::STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, kTWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned int* st = SINGLE ? single.nan_flag : status;
+    if ((threadIdx.x >> 5) == kTWarps) {
+        // (a negative consumer_wait is the failure-path test: nothing is staged)
+        if ((threadIdx.x & 31) == 0 && single.consumer_wait >= 0)
+            tiles_produce<T, TH, SINGLE>(single, inst, tile_member, tile_start, ntiles, smem, sbase, full0, empty0,
+                                         st);
+        return;
+    }
+    tiles_consume<T, TH, SINGLE>(single, smem, full0, empty0, st);
+}
+
+template <class T, bool TH, bool SINGLE>
+int tiles_set_smem(int dev) {
+    static std::atomic<unsigned long long> done{0};
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return 0;
+    const cudaError_t e = cudaFuncSetAttribute(step_tiles_kernel<T, TH, SINGLE>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, TilesCfg<T, TH>::SMEM);
+    if (e != cudaSuccess) return (int)e;
+    done.fetch_or(bit);
+    return 0;
+}
+
+template <class T, bool TH>
+int tiles_per_sm(int dev) {
+    static int cached[2] = {-1, -1};
+    if (cached[TH] < 0) {
+        int b0 = 0, b1 = 0;
+        if (tiles_set_smem<T, TH, true>(dev) || tiles_set_smem<T, TH, false>(dev)) return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, step_tiles_kernel<T, TH, true>, kTThreads,
+                                                          TilesCfg<T, TH>::SMEM) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, step_tiles_kernel<T, TH, false>, kTThreads,
+                                                          TilesCfg<T, TH>::SMEM) != cudaSuccess)
+            return 0;
+        cached[TH] = std::min(b0, b1);
+    }
+    return cached[TH];
+}
+
+template <class T, bool TH>
+int tiles_grid_t(long long ntiles, int dev) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    const int per = tiles_per_sm<T, TH>(dev);
+    if (per <= 0) return 0;
+    return (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)sms * per));
+}
+
+template <class T, bool TH, bool SINGLE>
+int launch_tiles_t(const KParams& p, const KParams* inst, const int* tm, const int* ts, int ntiles, int grid,
+                   unsigned int* status, cudaStream_t s) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (const int r = tiles_set_smem<T, TH, SINGLE>(dev)) return r;
+    if (grid <= 0) return (int)cudaErrorInvalidConfiguration;
+    step_tiles_kernel<T, TH, SINGLE><<<grid, kTThreads, TilesCfg<T, TH>::SMEM, s>>>(p, inst, tm, ts, ntiles, status);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+int tiles_width() { return kTW; }
+int tiles_warps() { return kTWarps; }
+
+int tiles_grid(int storage, bool thermal, long long ntiles, int device) {
+    switch (storage) {
+        case ST_FP32: return thermal ? tiles_grid_t<float, true>(ntiles, device) : tiles_grid_t<float, false>(ntiles, device);
+        case ST_FP16: return thermal ? tiles_grid_t<__half, true>(ntiles, device) : tiles_grid_t<__half, false>(ntiles, device);
+        case ST_BF16:
+            return thermal ? tiles_grid_t<__nv_bfloat16, true>(ntiles, device)
+                           : tiles_grid_t<__nv_bfloat16, false>(ntiles, device);
+    }
+    return 0;
+}
+
+int launch_tiles_single(int storage, const KParams& p, int grid, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nt = (int)((p.N + kTW - 1) / kTW);
+    const bool th = p.thermal != 0;
+#define LBM2D_TILES1(T)                                                                               \
+    return th ? launch_tiles_t<T, true, true>(p, nullptr, nullptr, nullptr, nt, grid, nullptr, s) \
+              : launch_tiles_t<T, false, true>(p, nullptr, nullptr, nullptr, nt, grid, nullptr, s)
+    switch (storage) {
+        case ST_FP32: LBM2D_TILES1(float);
+        case ST_FP16: LBM2D_TILES1(__half);
+        case ST_BF16: LBM2D_TILES1(__nv_bfloat16);
+    }
+#undef LBM2D_TILES1
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_tiles_batch(int storage, bool thermal, const KParams* inst, const int* tile_member, const int* tile_start,
+                       int ntiles, int grid, unsigned int* status, void* stream) {
+    if (ntiles <= 0) return 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    KParams none;
+    memset(&none, 0, sizeof(none));
+#define LBM2D_TILESB(T)                                                                                         \
+    return thermal ? launch_tiles_t<T, true, false>(none, inst, tile_member, tile_start, ntiles, grid, status, s) \
+                   : launch_tiles_t<T, false, false>(none, inst, tile_member, tile_start, ntiles, grid, status, s)
+    switch (storage) {
+        case ST_FP32: LBM2D_TILESB(float);
+        case ST_FP16: LBM2D_TILESB(__half);
+        case ST_BF16: LBM2D_TILESB(__nv_bfloat16);
+    }
+#undef LBM2D_TILESB
+    return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace lbm2d

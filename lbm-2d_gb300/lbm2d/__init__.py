@@ -24,7 +24,7 @@ MRT, BGK = 0, 1
 STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2, "fp64": 3}
 BYTES_PER_POP = {"fp32": 4, "fp16": 2, "bf16": 2, "fp64": 8}
 HOOK_NONE, HOOK_HEATED_CAVITY, HOOK_HEATED_SOLIDS = 0, 1, 2
-KERNEL_SCALAR, KERNEL_PAIR, KERNEL_ROWS = 0, 1, 2
+KERNEL_SCALAR, KERNEL_PAIR, KERNEL_ROWS, KERNEL_TILES = 0, 1, 2, 3
 
 ERRORS = {1: "invalid argument", 2: "out of device memory", 3: "CUDA error", 4: "non-finite density",
           5: "call out of order", 6: "no CUDA device", 7: "device wait timed out"}
@@ -398,10 +398,11 @@ class Solver:
         self._ck(self.L.lbm2d_set_block(self.h, int(bx), int(by)))
 
     def set_kernel_variant(self, variant: int):
-        """0 (default): fastest kernel the configuration allows (row pipeline,
-        else paired nodes, else one node per thread); 1: one node per thread;
-        2: paired nodes per thread.  `info().kernel` reports the kernel in use
-        (KERNEL_SCALAR / KERNEL_PAIR / KERNEL_ROWS)."""
+        """0 (default): fastest kernel the configuration allows (row pipeline;
+        the tile pipeline for the thermal DDF; else paired nodes, else one node
+        per thread); 1: one node per thread; 2: paired nodes per thread; 3: the
+        tile pipeline.  `info().kernel` reports the kernel in use
+        (KERNEL_SCALAR / KERNEL_PAIR / KERNEL_ROWS / KERNEL_TILES)."""
         self._ck(self.L.lbm2d_set_kernel_variant(self.h, int(variant)))
 
     def set_wait_limit(self, cycles: int):

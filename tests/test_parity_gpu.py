@@ -45,12 +45,13 @@ def run(product, O, spec, storage, variant=0):
     return out
 
 
-@pytest.mark.parametrize("storage,variant", [("fp64", 0), ("fp32", 0), ("fp32", 1), ("fp32", 2)])
+@pytest.mark.parametrize("storage,variant", [("fp64", 0), ("fp32", 0), ("fp32", 1), ("fp32", 2), ("fp32", 3)])
 @pytest.mark.parametrize("name", sorted(CS.CASES))
 def test_gpu_matches_reference(product, oracle_lib, name, storage, variant):
     """variant 0: the fastest kernel for the case (row pipeline where nx is a
-    multiple of 4 (FP32), else paired nodes); 1: one node per thread; 2: paired
-    nodes per thread (packed FP32x2) where nx is even."""
+    multiple of 4 (FP32); the tile pipeline for the thermal DDF; else paired
+    nodes); 1: one node per thread; 2: paired nodes per thread (packed FP32x2)
+    where nx is even; 3: the tile pipeline."""
     spec = CS.CASES[name]
     gold = np.load(os.path.join(GOLD, f"{name}.npz"))
     got = run(product, oracle_lib, spec, storage, variant)
@@ -81,7 +82,7 @@ def test_gpu_matches_reference(product, oracle_lib, name, storage, variant):
         assert np.array_equal(got["hist"], got["sums"])
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("storage", ["fp16", "bf16"])
 @pytest.mark.parametrize("name", ["cavity_mrt", "cylinder_mei", "ribs_les", "thermal_cavity", "step"])
 def test_gpu_shifted_storage_bounds(product, oracle_lib, name, storage, variant):

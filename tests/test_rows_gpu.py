@@ -111,18 +111,21 @@ def test_kernel_selection(product):
     s.close()
 
 
-def test_pipeline_wait_timeout_reports_and_recovers(product, oracle_lib):
-    """The row pipeline's bounded waits: with the consumers' wait limit set to
-    one SM cycle, the consumers give up on their first staged tile, the kernel
-    ends (the producer drains the copies it issued) and the next
+@pytest.mark.parametrize("variant", [0, 3])
+def test_pipeline_wait_timeout_reports_and_recovers(product, oracle_lib, variant):
+    """The staging pipelines' bounded waits (row pipeline, tile pipeline): in
+    the failure-path test mode the producer stages nothing -- a stage that
+    never fills, the flag that nothing sets -- so every consumer wait runs
+    out after 2e5 SM cycles (about 0.1 ms); the kernel ends and the next
     synchronisation reports LBM2D_ERR_TIMEOUT (7).  The context stays usable:
     with the default limit restored, a re-uploaded state steps to exactly the
     result of a fresh solver."""
-    spec = CS.CASES["ribs_les"]  # 64 x 40, FP32: the row pipeline
+    spec = CS.CASES["ribs_les"]  # 64 x 40, FP32: the row pipeline, or the tile pipeline
     s = gpu_solver(product, oracle_lib, spec, "fp32")
-    assert s.info().kernel == product.KERNEL_ROWS
+    s.set_kernel_variant(variant)
+    assert s.info().kernel == (product.KERNEL_ROWS if variant == 0 else product.KERNEL_TILES)
     f0 = s.f
-    s.set_wait_limit(1)
+    s.set_wait_limit(-200000)
     s.step(spec["tau"], spec["u"], 1)
     with pytest.raises(product.LBMError) as ex:
         s.synchronize()
@@ -132,6 +135,7 @@ def test_pipeline_wait_timeout_reports_and_recovers(product, oracle_lib):
     s.step(spec["tau"], spec["u"], 5)
     s.synchronize()
     ref = gpu_solver(product, oracle_lib, spec, "fp32")
+    ref.set_kernel_variant(variant)
     ref.step(spec["tau"], spec["u"], 5)
     assert np.array_equal(s.f, ref.f)
     s.close()
