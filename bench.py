@@ -189,12 +189,15 @@ def time_e2e(lbm2d, s, torch, steps, f0_pinned, fout_pinned):
     l0 = s.launches
     t0 = time.perf_counter()
     s.upload_f_ptr(f0_pinned.data_ptr())
+    ta = time.perf_counter()
     for _ in range(steps):
         s.step(TAU, U0, 1)
         s.force_sums()
+    tb = time.perf_counter()
     s.download_f_ptr(fout_pinned.data_ptr())
     t1 = time.perf_counter()
-    return (t1 - t0) * 1e3, s.launches - l0
+    phases = {"upload_ms": (ta - t0) * 1e3, "steps_ms": (tb - ta) * 1e3, "download_ms": (t1 - tb) * 1e3}
+    return (t1 - t0) * 1e3, s.launches - l0, phases
 
 
 def _cpu_impl():
@@ -861,9 +864,9 @@ def main():
             s.synchronize()
             reps.barrier()
             clocks.active = True
-            e2e_ms, e2e_launches = time_e2e(lbm2d, s, torch, e2e_steps, pin, pout)
+            e2e_ms, e2e_launches, phases = time_e2e(lbm2d, s, torch, e2e_steps, pin, pout)
             clocks.active = False
-            results["e2e"] = dict(ms=reps.max(e2e_ms), steps=e2e_steps, launches=e2e_launches)
+            results["e2e"] = dict(ms=reps.max(e2e_ms), steps=e2e_steps, launches=e2e_launches, phases=phases)
             del pin, pout
         s.close()
     clocks.stop()
@@ -909,7 +912,7 @@ def main():
         e = results["e2e"]
         e2e = {"value": world * nodes * e["steps"] / (e["ms"] * 1e-3) / 1e9, "unit": "GLUPS",
                "h2d_bytes_per_step": nodes * 9 * 8 / e["steps"], "d2h_bytes_per_step": 16 + nodes * 9 * 8 / e["steps"],
-               "steps": e["steps"], "launches": e["launches"],
+               "steps": e["steps"], "launches": e["launches"], "phases": e["phases"],
                "note": "initial state H2D from pinned memory + per step (step, drag/lift D2H) + final state D2H"}
     cpu = None
     if not args.no_cpu:

@@ -296,10 +296,11 @@ int ensure_slots(lbm2d_solver* h) {
     if (kind == KERNEL_TILES) {
         // one entry per tile of W consecutive nodes: the first of the tile's
         // per-warp slots, -1 for a tile without force nodes; then one entry
-        // per CTA of a single-instance launch (tile t runs on CTA t mod
-        // grid): 1 when it holds force tiles, the CTAs the fused second stage
-        // counts
+        // per CTA of a single-instance launch (CTA c runs the contiguous tiles
+        // [c*chunk, (c+1)*chunk), chunk = ceil(T / grid)): 1 when it holds
+        // force tiles, the CTAs the fused second stage counts
         const int tw = tiles_width(), warps = tiles_warps();
+        const long long chunk = (ntiles + grid - 1) / grid;
         slots.assign((size_t)ntiles + (size_t)grid, -1);
         for (size_t r = 0; r < h->geo.rec_force.size(); ++r)
             if (h->geo.rec_force[r]) slots[(size_t)(h->geo.rec_node[r] / tw)] = 0;
@@ -308,7 +309,7 @@ int ensure_slots(lbm2d_solver* h) {
             if (slots[t] == 0) {
                 slots[t] = k;
                 k += warps;
-                slots[(size_t)ntiles + t % (size_t)grid] = 1;
+                slots[(size_t)ntiles + (size_t)((long long)t / chunk)] = 1;
             }
         for (int c = 0; c < grid; ++c) red_blocks += slots[(size_t)ntiles + c] > 0 ? 1 : 0;
         h->nslots = k;
@@ -700,8 +701,16 @@ static int upload_common(lbm2d_solver* h, const double* src, bool is_g, cudaMemc
     int rc;
     if ((rc = check_handle(h))) return rc;
     if (!src) return fail(h, LBM2D_ERR_INVALID, "null populations");
-    if ((rc = materialize(h))) return rc;
-    if ((rc = ensure_stage(h, true))) return rc;
+    // the upload replaces one population set; the other one (g for an f
+    // upload of a thermal solver, f for a g upload) is rebuilt first when the
+    // stored populations are the newer state -- a non-thermal f upload
+    // replaces everything and rebuilds nothing
+    if (!h->staged && (h->thermal || is_g)) {
+        if ((rc = materialize(h))) return rc;
+    } else {
+        h->staged = true;
+    }
+    if ((rc = ensure_stage(h, h->thermal || is_g))) return rc;
     double* dst = is_g ? h->d_stage_g : h->d_stage_f;
     CK(cudaMemcpyAsync(dst, src, h->N * 9 * sizeof(double), kind, h->stream), "upload");
     if (kind == cudaMemcpyHostToDevice) CK(cudaStreamSynchronize(h->stream), "upload");

@@ -18,15 +18,16 @@
 //     the plain pull (solid, boundary record, a thermal hook row or column)
 //     are rebuilt from global memory with the per-node functions every step
 //     kernel shares;
-//   * a persistent grid walks the tiles t = blockIdx.x, blockIdx.x + G, ...
-//     of one instance, or of all instances of a batch (tile_member[t] names
-//     the instance).  The producer skips the tiles of an instance whose step
-//     budget is spent and ends the ring with a marker stage;
-//   * consumers: 8 warps, each lane owns two consecutive nodes of the tile.
-//     Non-thermal pairs collide with the packed FP32x2 collision
-//     (collide_pair_dev) and store as pairs (the paired kernels' rounding
-//     noise), thermal nodes collide one at a time (collide_dev<true>) with
-//     the one-node kernel's per-node noise;
+//   * a persistent grid walks the tiles of one instance, or of all instances
+//     of a batch (tile_member[t] names the instance), each CTA a contiguous
+//     chunk of ceil(T / G) tiles.  The producer skips the tiles of an
+//     instance whose step budget is spent and ends the ring with a marker
+//     stage;
+//   * consumers: 8 warps.  Non-thermal: each lane owns two consecutive
+//     nodes, collided with the packed FP32x2 collision (collide_pair_dev) and
+//     stored as pairs (the paired kernels' rounding noise).  Thermal: each
+//     lane owns nodes tid and tid + 256, collided one at a time
+//     (collide_dev<true>) with the one-node kernel's per-node noise;
 //   * momentum exchange: FP64 per lane in shared memory, an FP64 warp sum per
 //     tile into the instance's per-tile slots (fixed order, so the same
 //     instance gives the same bits alone or in any mix); a single instance
@@ -130,24 +131,39 @@ __device__ void tiles_produce(const KParams& single, const KParams* __restrict__
     using C = TilesCfg<T, TH>;
     int issued = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        int k = 0, tl = t;
-        const KParams* gpp = &single;
-        if constexpr (!SINGLE) {
-            k = __ldg(tile_member + t);
-            tl = t - __ldg(tile_start + k);
-            gpp = inst + k;
+    // a contiguous chunk of tiles per CTA: consecutive tiles mostly belong to
+    // the same instance (its parameters, budget and seed are looked up once
+    // per instance, not per tile) and share halo rows in L2
+    const int chunk = (ntiles + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int t_end = min(ntiles, ((int)blockIdx.x + 1) * chunk);
+    int k = -1, k_first = 0, k_next = 0, L = 1;
+    uint32_t seed = 0;
+    const KParams* gpp = &single;
+    for (int t = (int)blockIdx.x * chunk; t < t_end; ++t) {
+        if (SINGLE ? k < 0 : t >= k_next) {
+            // a new instance: its tile range, step budget and rounding seed
+            if constexpr (SINGLE) {
+                k = 0;
+                k_first = 0;
+            } else {
+                k = __ldg(tile_member + t);
+                k_first = __ldg(tile_start + k);
+                k_next = __ldg(tile_start + k + 1);
+                gpp = inst + k;
+            }
+            const KParams& g0 = *gpp;
+            // an instance whose budget is spent takes no step; the CTA holding
+            // its first tile hands the decremented budget and the seed on
+            L = g0.left_in ? *g0.left_in : 1;
+            seed = g0.seed_in ? *g0.seed_in : g0.seed_host;
+            if (t == k_first) {
+                if (g0.left_in) *g0.left_out = L > 0 ? L - 1 : 0;
+                if (L > 0 && g0.seed_out) *g0.seed_out = seed + 1u;
+            }
         }
-        const KParams& gp = *gpp;
-        // step budget: an instance whose budget is spent takes no step; the
-        // CTA holding its first tile hands the decremented budget on
-        const int* li = gp.left_in;
-        const int L = li ? *li : 1;
-        if (li && tl == 0) *gp.left_out = L > 0 ? L - 1 : 0;
         if (L <= 0) continue;
-        // rounding seed, handed on by the CTA holding the first tile
-        const uint32_t seed = gp.seed_in ? *gp.seed_in : gp.seed_host;
-        if (tl == 0 && gp.seed_out) *gp.seed_out = seed + 1u;
+        const KParams& gp = *gpp;
+        const int tl = t - k_first;
         const int s = issued % C::STAGES, n = issued / C::STAGES;
         if (n > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1))) {
             ok = false;
@@ -406,14 +422,14 @@ __device__ void tiles_consume(const KParams& single, unsigned char* smem, uint32
         const KParams& p = tile_params<SINGLE>(single, stage, C::PAR_OFF);
         const uint32_t skey = Pop<T>::kRounds ? seed_key(h.seed) : 0u;
         if (h.slot >= 0) acc[tid] = make_double2(0.0, 0.0);
-        const int i = 2 * tid;
-        if ((long long)h.n0 + i < p.N) {
-            if constexpr (TH) {
-                tile_node_th<T>(p, stage, h, i, skey, acc + tid);
-                if ((long long)h.n0 + i + 1 < p.N) tile_node_th<T>(p, stage, h, i + 1, skey, acc + tid);
-            } else {
-                tile_pair<T>(p, stage, h, i, skey, acc + tid);
-            }
+        if constexpr (TH) {
+            // one node at a time: lanes take consecutive nodes (tid, then
+            // tid + 256), so staged reads and stores are unit-stride
+            if ((long long)h.n0 + tid < p.N) tile_node_th<T>(p, stage, h, tid, skey, acc + tid);
+            if ((long long)h.n0 + tid + kTW / 2 < p.N) tile_node_th<T>(p, stage, h, tid + kTW / 2, skey, acc + tid);
+        } else {
+            const int i = 2 * tid;
+            if ((long long)h.n0 + i < p.N) tile_pair<T>(p, stage, h, i, skey, acc + tid);
         }
         if (h.slot >= 0) {
             // FP64 warp sum of the tile's link terms into its per-warp slot
@@ -437,7 +453,7 @@ __device__ void tiles_consume(const KParams& single, unsigned char* smem, uint32
     }
     if constexpr (SINGLE) {
         // the drag/lift second stage in the last CTA holding force tiles: the
-        // host marks those CTAs (tile t runs on CTA t mod grid) after the
+        // host marks those CTAs (tile t runs on CTA t / ceil(T / grid)) after the
         // per-tile entries of the slot table, so every marked CTA counts
         // itself even when one of its waits ran out
         const int ntiles = (int)((single.N + kTW - 1) / kTW);
