@@ -207,43 +207,83 @@ template <class R>
 __device__ __forceinline__ R clamp_rate(R s) { return s < R(0.5) ? R(0.5) : (s > R(1.99) ? R(1.99) : s); }
 
 // ----------------------------------------------------------------- pull + rebuild
+// Where a rebuild reads the stored (post-collision) populations: plane j of
+// node idx as a full population (the storage shift added back), and the flags
+// of node idx.  GlobalSrc reads device memory; the tile pipeline supplies a
+// source that serves the staged windows from shared memory.
 template <class T>
-__device__ __forceinline__ void pull(const KParams& p, const T* __restrict__ P, const float* sh, int x, int y,
-                                     typename Pop<T>::R f[9]) {
+struct GlobalSrc {
+    const T* __restrict__ P;
+    size_t N;
+    const float* sh;
+    const uint32_t* __restrict__ flags;
+    __device__ __forceinline__ typename Pop<T>::R ld(int j, unsigned idx) const {
+        return Pop<T>::ld(P + (size_t)j * N, idx, sh[j]);
+    }
+    __device__ __forceinline__ uint32_t flag(unsigned idx) const { return __ldg(flags + idx); }
+};
+
+template <class T>
+__device__ __forceinline__ GlobalSrc<T> gsrc_f(const KParams& p) {
+    return {static_cast<const T*>(p.fin), (size_t)p.N, p.shf, p.flags};
+}
+template <class T>
+__device__ __forceinline__ GlobalSrc<T> gsrc_g(const KParams& p) {
+    return {static_cast<const T*>(p.gin), (size_t)p.N, p.shg, p.flags};
+}
+
+template <class S, class R>
+__device__ __forceinline__ void pull_src(const KParams& p, const S& src, int x, int y, R f[9]) {
     const unsigned nx = (unsigned)p.nx, ny = (unsigned)p.ny;
-    const size_t N = (size_t)p.N;
     const unsigned ux = (unsigned)x, uy = (unsigned)y;
     const unsigned xm = ux == 0 ? nx - 1 : ux - 1, xp = ux == nx - 1 ? 0 : ux + 1;
     const unsigned ym = uy == 0 ? ny - 1 : uy - 1, yp = uy == ny - 1 ? 0 : uy + 1;
     const unsigned r0 = uy * nx, rm = ym * nx, rp = yp * nx;  // nx*ny < 2^32 (checked at create)
     // slot j pulls from (x - cx_j, y - cy_j), wrapped; records override the
     // slots whose source is solid or outside the domain.
-    f[0] = Pop<T>::ld(P, r0 + ux, sh[0]);
-    f[1] = Pop<T>::ld(P + N, r0 + xm, sh[1]);
-    f[2] = Pop<T>::ld(P + 2 * N, rm + ux, sh[2]);
-    f[3] = Pop<T>::ld(P + 3 * N, r0 + xp, sh[3]);
-    f[4] = Pop<T>::ld(P + 4 * N, rp + ux, sh[4]);
-    f[5] = Pop<T>::ld(P + 5 * N, rm + xm, sh[5]);
-    f[6] = Pop<T>::ld(P + 6 * N, rm + xp, sh[6]);
-    f[7] = Pop<T>::ld(P + 7 * N, rp + xp, sh[7]);
-    f[8] = Pop<T>::ld(P + 8 * N, rp + xm, sh[8]);
+    f[0] = src.ld(0, r0 + ux);
+    f[1] = src.ld(1, r0 + xm);
+    f[2] = src.ld(2, rm + ux);
+    f[3] = src.ld(3, r0 + xp);
+    f[4] = src.ld(4, rp + ux);
+    f[5] = src.ld(5, rm + xm);
+    f[6] = src.ld(6, rm + xp);
+    f[7] = src.ld(7, rp + xp);
+    f[8] = src.ld(8, rp + xm);
+}
+
+template <class T>
+__device__ __forceinline__ void pull(const KParams& p, const T* __restrict__ P, const float* sh, int x, int y,
+                                     typename Pop<T>::R f[9]) {
+    pull_src(p, GlobalSrc<T>{P, (size_t)p.N, sh, p.flags}, x, y, f);
 }
 
 // Rebuild the non-regular f slots of a boundary node from its record
 // (streaming bounce-back src/lbm.hpp:418-428, :449-452, :470-480 and
-// apply_bouzidi_bb :226-288).
-template <class T>
-__device__ __forceinline__ void fix_f(const KParams& p, const T* __restrict__ P, int x, int y, uint32_t rec,
-                                   typename Pop<T>::R f[9]) {
+// apply_bouzidi_bb :226-288).  With LAZY, the node's own stored values are
+// read only when a slot bounces back (simple or interpolated): a record with
+// "no source" slots alone (inlet and outlet columns) needs none of them.
+template <class T, bool LAZY = false, class S>
+__device__ __forceinline__ void fix_f_src(const KParams& p, const S& src, int x, int y, uint32_t rec,
+                                          typename Pop<T>::R f[9]) {
     using R = typename Pop<T>::R;
     const uint32_t types = p.rec_info[rec] & 0x3FFFFu;
     if (types == 0) return;
-    const size_t N = (size_t)p.N;
-    const size_t n = (size_t)y * p.nx + x;
+    const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
     R own[9];
+    R rho = R(0), u = R(0), v = R(0);
+    if constexpr (LAZY) {
+        // bit 0 of each 2-bit code: SIMPLE_BB (01) or ZERO (11); bit 1: INTERP (10) or ZERO
+        const uint32_t lo = types & 0x15555u, hi = (types >> 1) & 0x15555u;
+        if (lo == hi) {  // "no source" slots only
 #pragma unroll
-    for (int j = 0; j < 9; ++j) own[j] = Pop<T>::ld(P + j * N, n, p.shf[j]);
-    R rho, u, v;
+            for (int j = 0; j < 9; ++j)
+                if (((types >> (2 * j)) & 3u) == SLOT_ZERO) f[j] = R(0);
+            return;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) own[j] = src.ld(j, n);
     macros(own, rho, u, v);
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
@@ -272,7 +312,7 @@ __device__ __forceinline__ void fix_f(const KParams& p, const T* __restrict__ P,
                     const int sx = x - CXf(i), sy = y - CYf(i);
                     R fsrc = own[i];
                     if (sx >= 0 && sx < p.nx && sy >= 0 && sy < p.ny)
-                        fsrc = Pop<T>::ld(P + i * N, (size_t)sy * p.nx + sx, p.shf[i]);
+                        fsrc = src.ld(i, (unsigned)sy * (unsigned)p.nx + (unsigned)sx);
                     fbb = R(2) * q * own[i] + (R(1) - R(2) * q) * fsrc;
                 } else {
                     const R inv2q = R(1) / (R(2) * q);
@@ -286,16 +326,21 @@ __device__ __forceinline__ void fix_f(const KParams& p, const T* __restrict__ P,
 }
 
 template <class T>
-__device__ __forceinline__ void fix_g(const KParams& p, const T* __restrict__ G, int x, int y, uint32_t rec,
-                                   typename Pop<T>::R g[9]) {
+__device__ __forceinline__ void fix_f(const KParams& p, const T* __restrict__ P, int x, int y, uint32_t rec,
+                                      typename Pop<T>::R f[9]) {
+    fix_f_src<T>(p, GlobalSrc<T>{P, (size_t)p.N, p.shf, p.flags}, x, y, rec, f);
+}
+
+template <class T, class S>
+__device__ __forceinline__ void fix_g_src(const KParams& p, const S& src, int x, int y, uint32_t rec,
+                                          typename Pop<T>::R g[9]) {
     using R = typename Pop<T>::R;
     const uint32_t m = (p.rec_info[rec] >> REC_GBB_SHIFT) & 0x1FFu;
     if (m == 0) return;
-    const size_t N = (size_t)p.N;
-    const size_t n = (size_t)y * p.nx + x;
+    const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
     R own[9];
 #pragma unroll
-    for (int j = 0; j < 9; ++j) own[j] = Pop<T>::ld(G + j * N, n, p.shg[j]);
+    for (int j = 0; j < 9; ++j) own[j] = src.ld(j, n);
 #pragma unroll
     for (int j = 0; j < 9; ++j)
         if (m & (1u << j)) g[j] = own[BBf(j)];  // adiabatic bounce-back, src/lbm.hpp:512-520
@@ -333,31 +378,30 @@ __device__ __forceinline__ void apply_bc(const KParams& p, int x, int y, uint32_
 }
 
 // The reference's state after streaming, boundary conditions and (optionally)
-// a driver thermal pass, for node (x, y).  f/g hold it on return.
-template <class T, bool TH>
-__device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint32_t fl, typename Pop<T>::R f[9],
-                                            typename Pop<T>::R g[9]) {
+// a driver thermal pass, for node (x, y), reading the stored populations
+// through sf (f) and sg (g).  f/g hold it on return.
+template <class T, bool TH, bool LAZY = false, class SF, class SG>
+__device__ __forceinline__ void build_state_src(const KParams& p, const SF& sf, const SG& sg, int x, int y,
+                                                uint32_t fl, typename Pop<T>::R f[9], typename Pop<T>::R g[9]) {
     using R = typename Pop<T>::R;
-    const T* __restrict__ Pf = static_cast<const T*>(p.fin);
     const bool outflow_col = (p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x == p.nx - 1;
     // zero-gradient outlet: column NX-1 takes NX-2's post-stream state (src/lbm.hpp:63-73)
     const int sx = outflow_col ? x - 1 : x;
-    const uint32_t sfl = outflow_col ? __ldg(p.flags + (size_t)y * p.nx + sx) : fl;
+    const uint32_t sfl = outflow_col ? sf.flag((unsigned)y * (unsigned)p.nx + (unsigned)sx) : fl;
     if (sfl & FLAG_SOLID) {
 #pragma unroll
         for (int j = 0; j < 9; ++j) f[j] = R(0);
     } else {
-        pull<T>(p, Pf, p.shf, sx, y, f);
-        if (sfl & FLAG_BOUNDARY) fix_f<T>(p, Pf, sx, y, sfl >> 2, f);
+        pull_src(p, sf, sx, y, f);
+        if (sfl & FLAG_BOUNDARY) fix_f_src<T, LAZY>(p, sf, sx, y, sfl >> 2, f);
     }
     if (TH) {
-        const T* __restrict__ Pg = static_cast<const T*>(p.gin);
         if (fl & FLAG_SOLID) {
 #pragma unroll
             for (int j = 0; j < 9; ++j) g[j] = R(0);
         } else {
-            pull<T>(p, Pg, p.shg, x, y, g);
-            if (fl & FLAG_BOUNDARY) fix_g<T>(p, Pg, x, y, fl >> 2, g);
+            pull_src(p, sg, x, y, g);
+            if (fl & FLAG_BOUNDARY) fix_g_src<T>(p, sg, x, y, fl >> 2, g);
         }
     }
     apply_bc<R>(p, x, y, fl, f);
@@ -382,6 +426,12 @@ __device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint
             for (int i = 0; i < 9; ++i) g[i] = R(wgt(i)) * phys<R>(p).hook_a;
         }
     }
+}
+
+template <class T, bool TH>
+__device__ __forceinline__ void build_state(const KParams& p, int x, int y, uint32_t fl, typename Pop<T>::R f[9],
+                                            typename Pop<T>::R g[9]) {
+    build_state_src<T, TH>(p, gsrc_f<T>(p), gsrc_g<T>(p), x, y, fl, f, g);
 }
 
 // LES wall distance of a fluid node: a boundary node's record holds it; any

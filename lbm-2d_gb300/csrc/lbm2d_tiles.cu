@@ -57,10 +57,9 @@ struct TilesCfg {
     static constexpr int PAR_OFF = FLAGS_OFF + kTW * 4;
     static constexpr int HDR_OFF = PAR_OFF + (int)sizeof(KParams);
     static constexpr int STAGE_BYTES = (HDR_OFF + 32 + 127) / 128 * 128;
-    // ring depth and residency: FP32 moves twice the bytes per node of the
-    // 16-bit forms, the thermal form twice again
-    static constexpr int STAGES = TH ? (ES == 4 ? 2 : 3) : (ES == 4 ? 3 : 5);
-    static constexpr int MIN_BLOCKS = ES == 4 ? 2 : 3;
+    // two CTAs per SM (112 registers: the rebuild without spills) with a
+    // ring of about 85 KB each: the deeper, the more bytes in flight per SM
+    static constexpr int STAGES = TH ? (ES == 4 ? 2 : 4) : (ES == 4 ? 4 : 7);
     static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
     static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;
     static constexpr int SMEM = ACC_OFF + 32 * kTWarps * 16;
@@ -124,7 +123,7 @@ __device__ __forceinline__ const KParams& tile_params(const KParams& single, con
 
 // ----------------------------------------------------------------- producer
 template <class T, bool TH, bool SINGLE>
-__device__ void tiles_produce(const KParams& single, const KParams* __restrict__ inst,
+__device__ __forceinline__ void tiles_produce(const KParams& single, const KParams* __restrict__ inst,
                               const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
                               unsigned char* smem, uint32_t sbase, uint32_t full0, uint32_t empty0,
                               unsigned int* status) {
@@ -250,6 +249,73 @@ __device__ __forceinline__ float staged(const unsigned char* stage, int w, int l
     else return __bfloat162float(r[lead + i + 1 - cx]);
 }
 
+// Stored populations of the tile's sources for the rebuild functions: the
+// staged window of direction j when it holds node idx of plane j, else device
+// memory.  Window j starts at global element j*N + n0 - cy_j*nx - 1 - lead_j,
+// so node idx of plane j sits at offset lead_j + 1 + idx - n0 + cy_j*nx; an
+// offset inside the window is an element the producer copied.  Values are
+// converted exactly as Pop<T> converts them from device memory.
+template <class T, bool TH>
+struct TileSrc {
+    const unsigned char* stage;
+    int w0;  // first window of this population set (0: f, 9: g)
+    long long n0;
+    int leads, nx;
+    const T* __restrict__ P;
+    size_t N;
+    const float* sh;
+    const uint32_t* __restrict__ gflags;
+    __device__ __forceinline__ float raw(int j, unsigned idx) const {
+        using C = TilesCfg<T, TH>;
+        const int lead = (leads >> (3 * j)) & 7;
+        const long long o = (long long)lead + 1 + (long long)idx - n0 + (long long)CYf(j) * nx;
+        if (o >= 0 && o < C::WIN) {
+            const T v = reinterpret_cast<const T*>(stage + (w0 + j) * C::ROWB)[o];
+            if constexpr (std::is_same<T, float>::value) return v;
+            else if constexpr (std::is_same<T, __half>::value) return __half2float(v);
+            else return __bfloat162float(v);
+        }
+        return Pop<T>::ldr(P + (size_t)j * N, idx);
+    }
+    // full population (shift added back), as Pop<T>::ld
+    __device__ __forceinline__ float ld(int j, unsigned idx) const {
+        if constexpr (std::is_same<T, __half>::value) return fmaf(raw(j, idx), kF16InvScale, sh[j]);
+        else return raw(j, idx) + sh[j];
+    }
+    // deviation, as Pop<T>::ldd
+    __device__ __forceinline__ float ldd(int j, unsigned idx) const {
+        if constexpr (std::is_same<T, __half>::value) return raw(j, idx) * kF16InvScale;
+        else return raw(j, idx);
+    }
+    __device__ __forceinline__ uint32_t flag(unsigned idx) const {
+        using C = TilesCfg<T, TH>;
+        const long long o = (long long)idx - n0;
+        if (o >= 0 && o < kTW) return reinterpret_cast<const uint32_t*>(stage + C::FLAGS_OFF)[o];
+        return __ldg(gflags + idx);
+    }
+};
+
+template <class T, bool TH>
+__device__ __forceinline__ TileSrc<T, TH> tile_src(const KParams& p, const unsigned char* stage, const TileHdr& h,
+                                                   bool g) {
+    return {stage, g ? 9 : 0, (long long)h.n0, h.leads, p.nx, static_cast<const T*>(g ? p.gin : p.fin),
+            (size_t)p.N, g ? p.shg : p.shf, p.flags};
+}
+
+// Raw (storage-unit) or deviation pulls of node (x, y) through a tile source,
+// with the periodic wrap: the pull_raw / pull_dev of the other kernels.
+template <class S>
+__device__ __forceinline__ void pull_via(const KParams& p, const S& src, int x, int y, float d[9], bool dev) {
+    const unsigned nx = (unsigned)p.nx, ny = (unsigned)p.ny;
+    const unsigned ux = (unsigned)x, uy = (unsigned)y;
+    const unsigned xm = ux == 0 ? nx - 1 : ux - 1, xp = ux == nx - 1 ? 0 : ux + 1;
+    const unsigned ym = uy == 0 ? ny - 1 : uy - 1, yp = uy == ny - 1 ? 0 : uy + 1;
+    const unsigned r0 = uy * nx, rm = ym * nx, rp = yp * nx;
+    const unsigned idx[9] = {r0 + ux, r0 + xm, rm + ux, r0 + xp, rp + ux, rm + xm, rm + xp, rp + xp, rp + xm};
+#pragma unroll
+    for (int j = 0; j < 9; ++j) d[j] = dev ? src.ldd(j, idx[j]) : src.raw(j, idx[j]);
+}
+
 // Two x-neighbours in storage units stored as a pair, or as two elements
 // (element j*N + n odd for odd N and odd j) with the same rounding bits.
 template <class T>
@@ -315,8 +381,30 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
         da[j] = staged<T, false>(stage, j, lead, i, CXf(j));
         db[j] = staged<T, false>(stage, j, lead, i + 1, CXf(j));
     }
-    if (sa) build_dev_s<T>(p, xa, ya, fla, da);
-    if (sb) build_dev_s<T>(p, xb, yb, flb, db);
+    if (sa || sb) {
+        // rebuild through the staged windows (device memory only for
+        // sources outside them): build_dev_s of the other kernels
+        const TileSrc<T, false> src = tile_src<T, false>(p, stage, h, false);
+        float f[9], g[9];
+        if (sa) {
+            if (special_node<false>(p, xa, ya, fla)) {
+                build_state_src<T, false, true>(p, src, src, xa, ya, fla, f, g);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) da[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
+            } else {
+                pull_via(p, src, xa, ya, da, false);
+            }
+        }
+        if (sb) {
+            if (special_node<false>(p, xb, yb, flb)) {
+                build_state_src<T, false, true>(p, src, src, xb, yb, flb, f, g);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) db[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
+            } else {
+                pull_via(p, src, xb, yb, db, false);
+            }
+        }
+    }
     if (h.slot >= 0 && ((fla | flb) & FLAG_BOUNDARY)) {
         float f[9];
         if (oka && (fla & FLAG_BOUNDARY)) {
@@ -367,8 +455,19 @@ __device__ __forceinline__ void tile_node_th(const KParams& p, const unsigned ch
     tile_xy(h.x0, h.y0, i, p.nx, p.inv_nx, x, y);
     const uint32_t fl = reinterpret_cast<const uint32_t*>(stage + C::FLAGS_OFF)[i];
     float d[9], e[9];  // deviations
-    if (border(p, x, y) || special_node<true>(p, x, y, fl)) {
-        build_dev<T, true>(p, x, y, fl, d, e);
+    if (special_node<true>(p, x, y, fl)) {
+        // build_dev<T, true> through the staged windows
+        const TileSrc<T, true> sf = tile_src<T, true>(p, stage, h, false), sg = tile_src<T, true>(p, stage, h, true);
+        float f[9], g[9];
+        build_state_src<T, true, true>(p, sf, sg, x, y, fl, f, g);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            d[j] = f[j] - p.shf[j];
+            e[j] = g[j] - p.shg[j];
+        }
+    } else if (border(p, x, y)) {
+        pull_via(p, tile_src<T, true>(p, stage, h, false), x, y, d, true);
+        pull_via(p, tile_src<T, true>(p, stage, h, true), x, y, e, true);
     } else {
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
@@ -401,7 +500,7 @@ __device__ __forceinline__ void tile_node_th(const KParams& p, const unsigned ch
 }
 
 template <class T, bool TH, bool SINGLE>
-__device__ void tiles_consume(const KParams& single, unsigned char* smem, uint32_t full0, uint32_t empty0,
+__device__ __forceinline__ void tiles_consume(const KParams& single, unsigned char* smem, uint32_t full0, uint32_t empty0,
                               unsigned int* status) {
     using C = TilesCfg<T, TH>;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -463,7 +562,7 @@ __device__ void tiles_consume(const KParams& single, unsigned char* smem, uint32
 }
 
 template <class T, bool TH, bool SINGLE>
-__global__ void __launch_bounds__(kTThreads, TilesCfg<T, TH>::MIN_BLOCKS)
+__global__ void __maxnreg__(112)
     step_tiles_kernel(const __grid_constant__ KParams single, const KParams* __restrict__ inst,
                       const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
                       unsigned int* status) {
