@@ -141,12 +141,12 @@ struct SmemPair<__nv_bfloat16> {
 // reference's post-stream state (pull, bounce-back records, outflow column,
 // boundary conditions), the momentum-exchange force, the collision and the
 // stores -- the body of step_pair_block with shared-memory pulls, on
-// deviations.  The force terms of the two nodes are added in FP64 to the
-// lane's accumulator `acc` in shared memory, so no FP64 value stays live in
-// registers across the collision.
+// deviations.  The link terms of the two nodes (each 2 f, exact in FP32)
+// are summed into (fxs, fys); the caller adds that pair sum to the lane's
+// FP64 running sum.
 template <class T, int KC, int KL>
 __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
-                                             uint32_t skey, double2* acc) {
+                                             uint32_t skey, float& fxs, float& fys) {
     using C = RowsCfg<T>;
     const uint2 fl = *reinterpret_cast<const uint2*>(stage + C::FLAGS_OFF + (x - x0) * 4);
     const int e0 = (x - x0) + C::PAD;
@@ -195,20 +195,16 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
             // accumulated in FP64 (each term 2 f exact in FP64)
             const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
             const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
-            if (ma | mb) {
-                double ax = acc->x, ay = acc->y;
 #pragma unroll
-                for (int j = 1; j < 9; ++j) {
-                    if (ma & (1u << j)) {
-                        ax -= double(CXf(j)) * 2.0 * double(fa[j]);
-                        ay -= double(CYf(j)) * 2.0 * double(fa[j]);
-                    }
-                    if (mb & (1u << j)) {
-                        ax -= double(CXf(j)) * 2.0 * double(fb[j]);
-                        ay -= double(CYf(j)) * 2.0 * double(fb[j]);
-                    }
+            for (int j = 1; j < 9; ++j) {
+                if (ma & (1u << j)) {
+                    fxs -= float(CXf(j)) * 2.0f * fa[j];
+                    fys -= float(CYf(j)) * 2.0f * fa[j];
                 }
-                *acc = make_double2(ax, ay);
+                if (mb & (1u << j)) {
+                    fxs -= float(CXf(j)) * 2.0f * fb[j];
+                    fys -= float(CYf(j)) * 2.0f * fb[j];
+                }
             }
         }
         // back to deviations; a regular neighbour keeps its exact deviations
@@ -323,9 +319,14 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
         }
         const int x0 = seg * kTileW;
         const int x = x0 + 2 * (warp * 32 + lane);
-        if (x < p.nx) consume_pair<T, KC, KL>(p, smem + s * C::STAGE_BYTES, x0, x, y, skey, acc + threadIdx.x);
+        float fxs = 0.0f, fys = 0.0f;
+        if (x < p.nx) consume_pair<T, KC, KL>(p, smem + s * C::STAGE_BYTES, x0, x, y, skey, fxs, fys);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8 * s);
+        if (fxs != 0.0f || fys != 0.0f) {  // the lane's FP64 running sum over its node pairs
+            acc[threadIdx.x].x += double(fxs);
+            acc[threadIdx.x].y += double(fys);
+        }
         if (++s == C::STAGES) {
             s = 0;
             phase ^= 1u;

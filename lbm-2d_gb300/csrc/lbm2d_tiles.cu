@@ -57,8 +57,9 @@ struct TilesCfg {
     static constexpr int PAR_OFF = FLAGS_OFF + kTW * 4;
     static constexpr int HDR_OFF = PAR_OFF + (int)sizeof(KParams);
     static constexpr int STAGE_BYTES = (HDR_OFF + 32 + 127) / 128 * 128;
-    // two CTAs per SM (112 registers: the rebuild without spills) with a
-    // ring of about 85 KB each: the deeper, the more bytes in flight per SM
+    // two CTAs per SM (96 registers: four or five warps per SM sub-partition
+    // fit its 16K registers) with a ring of about 85 KB each: the deeper,
+    // the more bytes in flight per SM
     static constexpr int STAGES = TH ? (ES == 4 ? 2 : 4) : (ES == 4 ? 4 : 7);
     static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
     static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;
@@ -383,25 +384,27 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
     }
     if (sa || sb) {
         // rebuild through the staged windows (device memory only for
-        // sources outside them): build_dev_s of the other kernels
+        // sources outside them): build_dev_s of the other kernels, one node
+        // at a time through a single copy of the (large) rebuild code
         const TileSrc<T, false> src = tile_src<T, false>(p, stage, h, false);
-        float f[9], g[9];
-        if (sa) {
-            if (special_node<false>(p, xa, ya, fla)) {
-                build_state_src<T, false, true>(p, src, src, xa, ya, fla, f, g);
+#pragma unroll 1
+        for (int k = 0; k < 2; ++k) {
+            if (!(k ? sb : sa)) continue;
+            const int xk = k ? xb : xa, yk = k ? yb : ya;
+            const uint32_t flk = k ? flb : fla;
+            float d[9];
+            if (special_node<false>(p, xk, yk, flk)) {
+                float f[9], g[9];
+                build_state_src<T, false, true>(p, src, src, xk, yk, flk, f, g);
 #pragma unroll
-                for (int j = 0; j < 9; ++j) da[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
+                for (int j = 0; j < 9; ++j) d[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
             } else {
-                pull_via(p, src, xa, ya, da, false);
+                pull_via(p, src, xk, yk, d, false);
             }
-        }
-        if (sb) {
-            if (special_node<false>(p, xb, yb, flb)) {
-                build_state_src<T, false, true>(p, src, src, xb, yb, flb, f, g);
 #pragma unroll
-                for (int j = 0; j < 9; ++j) db[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
-            } else {
-                pull_via(p, src, xb, yb, db, false);
+            for (int j = 0; j < 9; ++j) {
+                if (k) db[j] = d[j];
+                else da[j] = d[j];
             }
         }
     }
@@ -523,9 +526,11 @@ __device__ __forceinline__ void tiles_consume(const KParams& single, unsigned ch
         if (h.slot >= 0) acc[tid] = make_double2(0.0, 0.0);
         if constexpr (TH) {
             // one node at a time: lanes take consecutive nodes (tid, then
-            // tid + 256), so staged reads and stores are unit-stride
-            if ((long long)h.n0 + tid < p.N) tile_node_th<T>(p, stage, h, tid, skey, acc + tid);
-            if ((long long)h.n0 + tid + kTW / 2 < p.N) tile_node_th<T>(p, stage, h, tid + kTW / 2, skey, acc + tid);
+            // tid + 256), so staged reads and stores are unit-stride; one
+            // copy of the node code
+#pragma unroll 1
+            for (int i = tid; i < kTW; i += kTW / 2)
+                if ((long long)h.n0 + i < p.N) tile_node_th<T>(p, stage, h, i, skey, acc + tid);
         } else {
             const int i = 2 * tid;
             if ((long long)h.n0 + i < p.N) tile_pair<T>(p, stage, h, i, skey, acc + tid);
@@ -562,7 +567,7 @@ __device__ __forceinline__ void tiles_consume(const KParams& single, unsigned ch
 }
 
 template <class T, bool TH, bool SINGLE>
-__global__ void __maxnreg__(112)
+__global__ void __launch_bounds__(kTThreads, 2)
     step_tiles_kernel(const __grid_constant__ KParams single, const KParams* __restrict__ inst,
                       const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
                       unsigned int* status) {
