@@ -863,7 +863,7 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
         skey = seed_key(s);
         pass_seed(p, s, bxi == 0 && byi == 0 && threadIdx.x == 0 && threadIdx.y == 0);
     }
-    double fxs = 0.0, fys = 0.0;  // momentum exchange, accumulated in FP64
+    double fxs = 0.0, fys = 0.0;  // momentum exchange, summed in FP64 across nodes
     if (x < p.nx && y < p.ny) {
         const unsigned n = (unsigned)y * (unsigned)p.nx + (unsigned)x;
         const uint32_t fl = __ldg(p.flags + n);
@@ -874,15 +874,19 @@ __device__ __forceinline__ void step_block(const KParams& p, int bxi, int byi, i
             build_dev<T, TH>(p, x, y, fl, f, g);
         if (!(fl & FLAG_SOLID)) {
             if (fl & FLAG_BOUNDARY) {
-                // momentum exchange of this node's links (src/lbm.hpp:565-577)
+                // momentum exchange of this node's links (src/lbm.hpp:565-577):
+                // the node's terms 2 f in the compute precision, FP64 across nodes
                 const uint32_t fm = p.rec_force[fl >> 2];
+                R fxn = R(0), fyn = R(0);
 #pragma unroll
                 for (int j = 1; j < 9; ++j)
                     if (fm & (1u << j)) {
-                        const double fj = double(f[j] + R(p.shf[j]));
-                        fxs -= double(CXf(j)) * 2.0 * fj;
-                        fys -= double(CYf(j)) * 2.0 * fj;
+                        const R fj = f[j] + R(p.shf[j]);
+                        fxn -= R(CXf(j)) * R(2) * fj;
+                        fyn -= R(CYf(j)) * R(2) * fj;
                     }
+                fxs = double(fxn);
+                fys = double(fyn);
             }
             if constexpr (std::is_same<T, double>::value)
                 collide<R, TH>(p, fl, f, g);

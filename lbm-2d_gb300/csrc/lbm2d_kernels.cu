@@ -38,7 +38,7 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
         skey = seed_key(s);
         pass_seed(p, s, bxi == 0 && byi == 0 && threadIdx.x == 0 && threadIdx.y == 0);
     }
-    double fxs = 0.0, fys = 0.0;  // momentum exchange, accumulated in FP64
+    double fxs = 0.0, fys = 0.0;  // momentum exchange, FP64 across node pairs
     if (x0 < p.nx && y < p.ny) {
         const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
         const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
@@ -51,19 +51,24 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
             // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
             const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
             const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+            // the pair's link terms in FP32, node x0 then x0 + 1
+            float fxp = 0.0f, fyp = 0.0f;
 #pragma unroll
-            for (int j = 1; j < 9; ++j) {
+            for (int j = 1; j < 9; ++j)
                 if (ma & (1u << j)) {
-                    const double f = double(fmaf(fa[j], iS, p.shf[j]));
-                    fxs -= double(CXf(j)) * 2.0 * f;
-                    fys -= double(CYf(j)) * 2.0 * f;
+                    const float f = fmaf(fa[j], iS, p.shf[j]);
+                    fxp -= float(CXf(j)) * 2.0f * f;
+                    fyp -= float(CYf(j)) * 2.0f * f;
                 }
+#pragma unroll
+            for (int j = 1; j < 9; ++j)
                 if (mb & (1u << j)) {
-                    const double f = double(fmaf(fb[j], iS, p.shf[j]));
-                    fxs -= double(CXf(j)) * 2.0 * f;
-                    fys -= double(CYf(j)) * 2.0 * f;
+                    const float f = fmaf(fb[j], iS, p.shf[j]);
+                    fxp -= float(CXf(j)) * 2.0f * f;
+                    fyp -= float(CYf(j)) * 2.0f * f;
                 }
-            }
+            fxs = double(fxp);
+            fys = double(fyp);
         }
         if (oka || okb) {
             F2 f[9];

@@ -195,17 +195,19 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
             // accumulated in FP64 (each term 2 f exact in FP64)
             const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
             const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+            // node x's links, then node x+1's (the order every pair kernel uses)
 #pragma unroll
-            for (int j = 1; j < 9; ++j) {
+            for (int j = 1; j < 9; ++j)
                 if (ma & (1u << j)) {
                     fxs -= float(CXf(j)) * 2.0f * fa[j];
                     fys -= float(CYf(j)) * 2.0f * fa[j];
                 }
+#pragma unroll
+            for (int j = 1; j < 9; ++j)
                 if (mb & (1u << j)) {
                     fxs -= float(CXf(j)) * 2.0f * fb[j];
                     fys -= float(CYf(j)) * 2.0f * fb[j];
                 }
-            }
         }
         // back to deviations; a regular neighbour keeps its exact deviations
         if (sa) {

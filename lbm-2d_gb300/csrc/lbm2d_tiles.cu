@@ -8,11 +8,12 @@
 //     (it may span several short rows or part of a long one).  In that order
 //     the pull source of direction j is node n - cy_j*nx - cx_j, so the
 //     sources of a whole tile are one contiguous window per direction.  The
-//     producer's elected lane brings each window, rounded out to 16-byte
+//     producer warp brings each window, rounded out to 16-byte
 //     granules (the window's first element sits `lead` elements into the
 //     staged row), the tile's flags and -- in a batch -- the instance's
 //     parameters into a shared-memory stage with cp.async.bulk copies that
-//     complete on the stage's mbarrier.  No alignment of nx is needed;
+//     complete on the stage's mbarrier; the producer warp's lanes compute and
+//     issue one copy each.  No alignment of nx is needed;
 //   * nodes on the lattice border (x = 0, nx-1 or y = 0, ny-1), whose
 //     periodic sources lie outside the window, and nodes that need more than
 //     the plain pull (solid, boundary record, a thermal hook row or column)
@@ -90,29 +91,6 @@ __device__ __forceinline__ long long win_start(long long N, int nx, int n0, int 
     return a;
 }
 
-// Issue (or, with issue = false, count) the copies of one population set's
-// nine windows into rows [w0, w0 + 9) of the stage.
-template <class T, bool TH>
-__device__ __forceinline__ uint32_t set_copies(const T* __restrict__ P, long long N, int nx, int n0, uint32_t st,
-                                               int w0, uint32_t bar, bool issue, int* leads) {
-    using C = TilesCfg<T, TH>;
-    const long long gend = (9 * N + C::EPG - 1) / C::EPG * C::EPG;  // population buffers are padded to it
-    uint32_t bytes = 0;
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        int lead;
-        const long long a = win_start(N, nx, n0, j, C::EPG, lead);
-        const long long cs = max(a, 0LL), ce = min(a + C::WIN, gend);
-        if (leads) *leads |= lead << (3 * j);
-        if (ce > cs) {
-            const uint32_t nb = (uint32_t)((ce - cs) * C::ES);
-            if (issue) bulk_g2s(st + (uint32_t)((w0 + j) * C::ROWB) + (uint32_t)((cs - a) * C::ES), P + cs, nb, bar);
-            bytes += nb;
-        }
-    }
-    return bytes;
-}
-
 // Parameters a consumer reads for the tile: the instance's own copy in the
 // stage (batch) or the kernel parameter (single instance).
 template <bool SINGLE>
@@ -123,12 +101,20 @@ __device__ __forceinline__ const KParams& tile_params(const KParams& single, con
 }
 
 // ----------------------------------------------------------------- producer
+// The producer warp stages one tile at a time, its lanes in parallel: lane w
+// < NWIN computes and issues the copy of window w (f windows, then g), lane
+// NWIN the flags copy and lane NWIN + 1 (batch) the parameter copy; a warp sum
+// gives the bytes lane 0 announces on the stage's mbarrier before any copy is
+// issued.  Per-instance bookkeeping (tile range, budget, seed) is done by all
+// lanes alike when the instance changes; the tile's force slot is loaded ahead
+// of the stage wait, so no dependent global load sits on the per-tile path.
 template <class T, bool TH, bool SINGLE>
 __device__ __forceinline__ void tiles_produce(const KParams& single, const KParams* __restrict__ inst,
-                              const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
-                              unsigned char* smem, uint32_t sbase, uint32_t full0, uint32_t empty0,
-                              unsigned int* status) {
+                                              const int* __restrict__ tile_member, const int* __restrict__ tile_start,
+                                              int ntiles, unsigned char* smem, uint32_t sbase, uint32_t full0,
+                                              uint32_t empty0, unsigned int* status) {
     using C = TilesCfg<T, TH>;
+    const int lane = threadIdx.x & 31;
     int issued = 0;
     bool ok = true;
     // a contiguous chunk of tiles per CTA: consecutive tiles mostly belong to
@@ -138,67 +124,104 @@ __device__ __forceinline__ void tiles_produce(const KParams& single, const KPara
     const int t_end = min(ntiles, ((int)blockIdx.x + 1) * chunk);
     int k = -1, k_first = 0, k_next = 0, L = 1;
     uint32_t seed = 0;
-    const KParams* gpp = &single;
-    for (int t = (int)blockIdx.x * chunk; t < t_end; ++t) {
-        if (SINGLE ? k < 0 : t >= k_next) {
-            // a new instance: its tile range, step budget and rounding seed
-            if constexpr (SINGLE) {
-                k = 0;
-                k_first = 0;
-            } else {
-                k = __ldg(tile_member + t);
-                k_first = __ldg(tile_start + k);
-                k_next = __ldg(tile_start + k + 1);
-                gpp = inst + k;
-            }
-            const KParams& g0 = *gpp;
-            // an instance whose budget is spent takes no step; the CTA holding
-            // its first tile hands the decremented budget and the seed on
-            L = g0.left_in ? *g0.left_in : 1;
-            seed = g0.seed_in ? *g0.seed_in : g0.seed_host;
-            if (t == k_first) {
-                if (g0.left_in) *g0.left_out = L > 0 ? L - 1 : 0;
-                if (L > 0 && g0.seed_out) *g0.seed_out = seed + 1u;
-            }
+    // instance bookkeeping when tile t starts a new instance: its step budget
+    // (an instance whose budget is spent takes no step) and rounding seed; the
+    // CTA holding its first tile hands the decremented budget and the seed on
+    auto begin_instance = [&](const KParams& g0, int t) {
+        L = g0.left_in ? *g0.left_in : 1;
+        seed = g0.seed_in ? *g0.seed_in : g0.seed_host;
+        __syncwarp();
+        if (t == k_first && lane == 0) {
+            if (g0.left_in) *g0.left_out = L > 0 ? L - 1 : 0;
+            if (L > 0 && g0.seed_out) *g0.seed_out = seed + 1u;
         }
-        if (L <= 0) continue;
-        const KParams& gp = *gpp;
-        const int tl = t - k_first;
+    };
+    // stage tile tl of instance gp; false when a wait ran out
+    auto stage_tile = [&](const KParams& gp, int tl) -> bool {
+        // loads that do not depend on the stage, ahead of the wait
+        const int slot = (lane == 0 && gp.block_slot) ? __ldg(gp.block_slot + tl) : -1;
         const int s = issued % C::STAGES, n = issued / C::STAGES;
-        if (n > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1))) {
-            ok = false;
-            break;
-        }
+        if (n > 0 && !__all_sync(0xffffffffu, mbar_wait(empty0 + 8 * s, (uint32_t)((n - 1) & 1)))) return false;
         const uint32_t st = sbase + (uint32_t)(s * C::STAGE_BYTES);
         const uint32_t bar = full0 + 8 * s;
         const long long N = gp.N;
         const int nx = gp.nx;
         const int n0 = tl * kTW;
-        const T* Pf = static_cast<const T*>(gp.fin);
-        const T* Pg = static_cast<const T*>(gp.gin);
-        // bytes first (the mbarrier expects them before the copies land)
-        int leads = 0;
-        uint32_t bytes = set_copies<T, TH>(Pf, N, nx, n0, st, 0, bar, false, &leads);
-        if (TH) bytes += set_copies<T, TH>(Pg, N, nx, n0, st, 9, bar, false, nullptr);
-        const uint32_t fbytes = (uint32_t)(((min((long long)kTW, N - n0) * 4) + 15) / 16 * 16);
-        bytes += fbytes;
-        if (!SINGLE) bytes += (uint32_t)sizeof(KParams);
-        TileHdr* h = reinterpret_cast<TileHdr*>(smem + s * C::STAGE_BYTES + C::HDR_OFF);
-        h->k = k;
-        h->n0 = n0;
-        h->x0 = n0 % nx;
-        h->y0 = n0 / nx;
-        h->seed = seed;
-        h->tile = tl;
-        h->leads = leads;
-        h->slot = gp.block_slot ? __ldg(gp.block_slot + tl) : -1;
-        mbar_expect_tx(bar, bytes);  // release: the header is visible with the stage
-        set_copies<T, TH>(Pf, N, nx, n0, st, 0, bar, true, nullptr);
-        if (TH) set_copies<T, TH>(Pg, N, nx, n0, st, 9, bar, true, nullptr);
-        bulk_g2s(st + C::FLAGS_OFF, gp.flags + n0, fbytes, bar);
-        if (!SINGLE) bulk_g2s(st + C::PAR_OFF, &gp, (uint32_t)sizeof(KParams), bar);
+        // this lane's copy
+        const void* src = nullptr;
+        uint32_t dst = 0, nb = 0;
+        int lead = 0;
+        if (lane < C::NWIN) {
+            const int set = lane / 9, j = lane - 9 * set;
+            const T* P = static_cast<const T*>(set ? gp.gin : gp.fin);
+            const long long a = win_start(N, nx, n0, j, C::EPG, lead);
+            const long long gend = (9 * N + C::EPG - 1) / C::EPG * C::EPG;  // buffers are padded to it
+            const long long cs = max(a, 0LL), ce = min(a + C::WIN, gend);
+            if (ce > cs) {
+                src = P + cs;
+                dst = st + (uint32_t)(lane * C::ROWB) + (uint32_t)((cs - a) * C::ES);
+                nb = (uint32_t)((ce - cs) * C::ES);
+            }
+        } else if (lane == C::NWIN) {
+            src = gp.flags + n0;
+            dst = st + C::FLAGS_OFF;
+            nb = (uint32_t)(((min((long long)kTW, N - n0) * 4) + 15) / 16 * 16);
+        } else if (!SINGLE && lane == C::NWIN + 1) {
+            src = &gp;
+            dst = st + C::PAR_OFF;
+            nb = (uint32_t)sizeof(KParams);
+        }
+        uint32_t bytes = nb;
+        int leads = lane < 9 ? lead << (3 * lane) : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+            leads |= __shfl_xor_sync(0xffffffffu, leads, o);
+        }
+        if (lane == 0) {
+            TileHdr* h = reinterpret_cast<TileHdr*>(smem + s * C::STAGE_BYTES + C::HDR_OFF);
+            h->k = k;
+            h->n0 = n0;
+            h->x0 = n0 % nx;
+            h->y0 = n0 / nx;
+            h->seed = seed;
+            h->tile = tl;
+            h->leads = leads;
+            h->slot = slot;
+            mbar_expect_tx(bar, bytes);  // release: the header is visible with the stage
+        }
+        __syncwarp();
+        if (nb) bulk_g2s(dst, src, nb, bar);
         ++issued;
+        return true;
+    };
+    for (int t = (int)blockIdx.x * chunk; t < t_end; ++t) {
+        if constexpr (SINGLE) {
+            // the kernel parameter is used in place (never through its address)
+            if (k < 0) {
+                k = 0;
+                begin_instance(single, t);
+            }
+            if (L <= 0) continue;
+            if (!stage_tile(single, t)) {
+                ok = false;
+                break;
+            }
+        } else {
+            if (t >= k_next) {
+                k = __ldg(tile_member + t);
+                k_first = __ldg(tile_start + k);
+                k_next = __ldg(tile_start + k + 1);
+                begin_instance(inst[k], t);
+            }
+            if (L <= 0) continue;
+            if (!stage_tile(inst[k], t - k_first)) {
+                ok = false;
+                break;
+            }
+        }
     }
+    if (lane != 0) return;
     // end marker: a stage whose header says k = -1, completed by a plain arrival
     if (ok) {
         const int s = issued % C::STAGES, n = issued / C::STAGES;
@@ -336,19 +359,18 @@ __device__ __forceinline__ void store_two(T* __restrict__ base, size_t n, float 
     }
 }
 
-// Momentum exchange of one fluid boundary node from its post-stream full
-// populations f (FP32 values), added in FP64 to the lane's accumulator.
-__device__ __forceinline__ void add_force(const KParams& p, uint32_t fl, const float f[9], double2* acc) {
+// Momentum exchange of one fluid boundary node (src/lbm.hpp:565-577) from
+// its post-stream full populations f: the link terms 2 f (exact in FP32) are
+// summed in FP32 into (fx, fy), a node pair's sum, which the caller adds to
+// the lane's FP64 accumulator -- the accumulation every pair kernel uses.
+__device__ __forceinline__ void link_terms(const KParams& p, uint32_t fl, const float f[9], float& fx, float& fy) {
     const uint32_t m = p.rec_force[fl >> 2];
-    if (!m) return;
-    double ax = acc->x, ay = acc->y;
 #pragma unroll
     for (int j = 1; j < 9; ++j)
         if (m & (1u << j)) {
-            ax -= double(CXf(j)) * 2.0 * double(f[j]);
-            ay -= double(CYf(j)) * 2.0 * double(f[j]);
+            fx -= float(CXf(j)) * 2.0f * f[j];
+            fy -= float(CYf(j)) * 2.0f * f[j];
         }
-    *acc = make_double2(ax, ay);
 }
 
 // Non-thermal: nodes i, i+1 of the tile (pair), as consume_pair of the row
@@ -357,7 +379,6 @@ template <class T>
 __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char* stage, const TileHdr& h, int i,
                                           uint32_t skey, double2* acc) {
     using C = TilesCfg<T, false>;
-    constexpr float iS = Pop<T>::kInvS;
     const long long N = p.N;
     const unsigned na = (unsigned)h.n0 + (unsigned)i;
     const bool vb = (long long)na + 1 < N;
@@ -375,6 +396,11 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
     const bool oka = !(fla & FLAG_SOLID), okb = vb && !(flb & FLAG_SOLID);
     const bool sa = border(p, xa, ya) || special_node<false>(p, xa, ya, fla);
     const bool sb = vb && (border(p, xb, yb) || special_node<false>(p, xb, yb, flb));
+    // solid nodes whose state can no longer change skip their stores; decided
+    // here so that no coordinate stays live across the collision
+    const bool settled = p.skip_settled_solids != 0;
+    const bool skip = (!oka && settled && xa > 0 && xa < p.nx - 1 && ya < p.ny - 1) &&
+                      (!vb || (!okb && settled && xb > 0 && xb < p.nx - 1 && yb < p.ny - 1));
     float da[9], db[9];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
@@ -387,6 +413,7 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
         // sources outside them): build_dev_s of the other kernels, one node
         // at a time through a single copy of the (large) rebuild code
         const TileSrc<T, false> src = tile_src<T, false>(p, stage, h, false);
+        float fxs = 0.0f, fys = 0.0f;  // the pair's link terms, node a then node b
 #pragma unroll 1
         for (int k = 0; k < 2; ++k) {
             if (!(k ? sb : sa)) continue;
@@ -396,6 +423,7 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
             if (special_node<false>(p, xk, yk, flk)) {
                 float f[9], g[9];
                 build_state_src<T, false, true>(p, src, src, xk, yk, flk, f, g);
+                if (h.slot >= 0 && !(flk & FLAG_SOLID) && (flk & FLAG_BOUNDARY)) link_terms(p, flk, f, fxs, fys);
 #pragma unroll
                 for (int j = 0; j < 9; ++j) d[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
             } else {
@@ -407,18 +435,9 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
                 else da[j] = d[j];
             }
         }
-    }
-    if (h.slot >= 0 && ((fla | flb) & FLAG_BOUNDARY)) {
-        float f[9];
-        if (oka && (fla & FLAG_BOUNDARY)) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) f[j] = fmaf(da[j], iS, p.shf[j]);
-            add_force(p, fla, f, acc);
-        }
-        if (okb && (flb & FLAG_BOUNDARY)) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) f[j] = fmaf(db[j], iS, p.shf[j]);
-            add_force(p, flb, f, acc);
+        if (fxs != 0.0f || fys != 0.0f) {  // FP64 across the lane's node pairs
+            acc->x += double(fxs);
+            acc->y += double(fys);
         }
     }
     if (oka || okb) {
@@ -432,10 +451,7 @@ __device__ __forceinline__ void tile_pair(const KParams& p, const unsigned char*
             db[j] = f[j].v.y;
         }
     }  // solid nodes hold the solid state from build_dev_s
-    const bool settled = p.skip_settled_solids != 0;
-    const bool skip_a = !oka && settled && xa > 0 && xa < p.nx - 1 && ya < p.ny - 1;
-    const bool skip_b = !vb || (!okb && settled && xb > 0 && xb < p.nx - 1 && yb < p.ny - 1);
-    if (!(skip_a && skip_b)) {
+    if (!skip) {
         T* __restrict__ Fo = static_cast<T*>(p.fout);
         uint32_t rb[9] = {};
         if constexpr (Pop<T>::kRounds) rand9(skey + na, rb);
@@ -482,10 +498,13 @@ __device__ __forceinline__ void tile_node_th(const KParams& p, const unsigned ch
     const bool ok = !(fl & FLAG_SOLID);
     if (ok) {
         if (h.slot >= 0 && (fl & FLAG_BOUNDARY)) {
-            float f[9];
+            // the node's link terms in FP32, then FP64 (as the one-node kernel)
+            float f[9], fx = 0.0f, fy = 0.0f;
 #pragma unroll
             for (int j = 0; j < 9; ++j) f[j] = d[j] + p.shf[j];
-            add_force(p, fl, f, acc);
+            link_terms(p, fl, f, fx, fy);
+            acc->x += double(fx);
+            acc->y += double(fy);
         }
         collide_dev<true>(p, fl, d, e);
     }
@@ -519,7 +538,7 @@ __device__ __forceinline__ void tiles_consume(const KParams& single, unsigned ch
             break;
         }
         const unsigned char* stage = smem + s * C::STAGE_BYTES;
-        const TileHdr h = *reinterpret_cast<const TileHdr*>(stage + C::HDR_OFF);
+        const TileHdr& h = *reinterpret_cast<const TileHdr*>(stage + C::HDR_OFF);  // read in place: no registers
         if (h.k < 0) break;
         const KParams& p = tile_params<SINGLE>(single, stage, C::PAR_OFF);
         const uint32_t skey = Pop<T>::kRounds ? seed_key(h.seed) : 0u;
@@ -568,7 +587,7 @@ __device__ __forceinline__ void tiles_consume(const KParams& single, unsigned ch
 
 template <class T, bool TH, bool SINGLE>
 __global__ void __launch_bounds__(kTThreads, 2)
-    step_tiles_kernel(const __grid_constant__ KParams single, const KParams* __restrict__ inst,
+    step_tiles_kernel(const KParams single, const KParams* __restrict__ inst,
                       const int* __restrict__ tile_member, const int* __restrict__ tile_start, int ntiles,
                       unsigned int* status) {
     using C = TilesCfg<T, TH>;
@@ -586,7 +605,7 @@ __global__ void __launch_bounds__(kTThreads, 2)
     unsigned int* st = SINGLE ? single.nan_flag : status;
     if ((threadIdx.x >> 5) == kTWarps) {
         // (a negative consumer_wait is the failure-path test: nothing is staged)
-        if ((threadIdx.x & 31) == 0 && single.consumer_wait >= 0)
+        if (single.consumer_wait >= 0)
             tiles_produce<T, TH, SINGLE>(single, inst, tile_member, tile_start, ntiles, smem, sbase, full0, empty0,
                                          st);
         return;
