@@ -4,7 +4,7 @@
 // The same step as the row pipeline (pull, rebuild, force, collision, store)
 // with a different unit of work:
 //
-//   * a tile is W = 512 CONSECUTIVE nodes of an instance in row-major order
+//   * a tile is W = 448 CONSECUTIVE nodes of an instance in row-major order
 //     (it may span several short rows or part of a long one).  In that order
 //     the pull source of direction j is node n - cy_j*nx - cx_j, so the
 //     sources of a whole tile are one contiguous window per direction.  The
@@ -24,10 +24,10 @@
 //     chunk of ceil(T / G) tiles.  The producer skips the tiles of an
 //     instance whose step budget is spent and ends the ring with a marker
 //     stage;
-//   * consumers: 8 warps.  Non-thermal: each lane owns two consecutive
+//   * consumers: 7 warps.  Non-thermal: each lane owns two consecutive
 //     nodes, collided with the packed FP32x2 collision (collide_pair_dev) and
 //     stored as pairs (the paired kernels' rounding noise).  Thermal: each
-//     lane owns nodes tid and tid + 256, collided one at a time
+//     lane owns nodes tid and tid + W/2, collided one at a time
 //     (collide_dev<true>) with the one-node kernel's per-node noise;
 //   * momentum exchange: FP64 per lane in shared memory, an FP64 warp sum per
 //     tile into the instance's per-tile slots (fixed order, so the same
@@ -43,7 +43,11 @@
 namespace lbm2d {
 namespace {
 
-constexpr int kTWarps = 8;
+// 7 consumer warps + the producer warp, two CTAs per SM: 16 warps per SM,
+// four per SM sub-partition, which leaves each thread 128 registers of the
+// sub-partition's 16K -- the collision plus the tile bookkeeping without
+// spills
+constexpr int kTWarps = 7;
 constexpr int kTThreads = 32 * (kTWarps + 1);
 constexpr int kTW = 2 * 32 * kTWarps;  // nodes per tile
 
@@ -58,9 +62,8 @@ struct TilesCfg {
     static constexpr int PAR_OFF = FLAGS_OFF + kTW * 4;
     static constexpr int HDR_OFF = PAR_OFF + (int)sizeof(KParams);
     static constexpr int STAGE_BYTES = (HDR_OFF + 32 + 127) / 128 * 128;
-    // two CTAs per SM (96 registers: four or five warps per SM sub-partition
-    // fit its 16K registers) with a ring of about 85 KB each: the deeper,
-    // the more bytes in flight per SM
+    // two CTAs per SM with a ring of about 85 KB each: the deeper, the more
+    // bytes in flight per SM
     static constexpr int STAGES = TH ? (ES == 4 ? 2 : 4) : (ES == 4 ? 4 : 7);
     static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
     static constexpr int ACC_OFF = BAR_OFF + 2 * STAGES * 8;
@@ -545,7 +548,7 @@ __device__ __forceinline__ void tiles_consume(const KParams& single, unsigned ch
         if (h.slot >= 0) acc[tid] = make_double2(0.0, 0.0);
         if constexpr (TH) {
             // one node at a time: lanes take consecutive nodes (tid, then
-            // tid + 256), so staged reads and stores are unit-stride; one
+            // tid + W/2), so staged reads and stores are unit-stride; one
             // copy of the node code
 #pragma unroll 1
             for (int i = tid; i < kTW; i += kTW / 2)
@@ -581,7 +584,7 @@ __device__ __forceinline__ void tiles_consume(const KParams& single, unsigned ch
         // itself even when one of its waits ran out
         const int ntiles = (int)((single.N + kTW - 1) / kTW);
         if (single.red_done && single.block_slot && __ldg(single.block_slot + ntiles + blockIdx.x) > 0)
-            fused_force_finish(single, tid, [] { asm volatile("bar.sync 1, 256;" ::: "memory"); });
+            fused_force_finish(single, tid, [] { asm volatile("bar.sync 1, %0;" ::"n"(32 * kTWarps) : "memory"); });
     }
 }
 

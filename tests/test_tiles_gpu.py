@@ -3,9 +3,11 @@ consecutive nodes, any grid width, the thermal DDF, batches).
 
 * Odd and unaligned widths, grids narrower than a tile (tiles span rows) and
   odd node counts (odd plane strides, split pair stores): FP32 populations
-  and the drag/lift series within 1e-5 relative L2 of the oracle, and within
-  1e-6 of the paired / one-node kernels (same arithmetic, separately
-  compiled); FP16 within the shifted-storage bound.
+  and the drag/lift series within 1e-5 relative L2 of the oracle;
+  populations within 1e-6 of the paired / one-node kernels (same arithmetic,
+  separately compiled), the drag/lift series within 1e-6 of the paired
+  kernel (the same FP32 grouping of a node pair's link terms) and 1e-5 of
+  the one-node kernel; FP16 within the shifted-storage bound.
 * The thermal DDF: against the one-node kernel (the same per-node collision
   and rounding noise) within 1e-6 (FP32) and 1e-4 (FP16).
 * Batches: every member of a mixed batch (odd sizes, thermal and not, FP32
@@ -83,7 +85,10 @@ def test_tiles_match_oracle(product, oracle_lib, key):
     assert np.allclose(f_t[~fm], f_ref[~fm], atol=1e-6)
     if spec["case"] != CS.CAVITY:
         assert rel_l2(sums_t, sums_ref) < 1e-5
-        assert rel_l2(sums_t, sums_o) < 1e-6
+        # the paired kernel sums a node pair's link terms in FP32 as the tile
+        # kernel does; the one-node kernel (odd nx) sums one node's, so the two
+        # FP32 groupings round differently (within the oracle bound)
+        assert rel_l2(sums_t, sums_o) < (1e-6 if other == 2 else 1e-5)
 
 
 @pytest.mark.parametrize("storage,tol", [("fp16", 5e-3), ("bf16", 3e-2)])
