@@ -46,7 +46,9 @@ struct Group {
     int nblocks = 0;
     int njobs = 0;
     KParams* d_params[2] = {nullptr, nullptr};
-    int* d_block_start = nullptr;
+    int2* d_block_map = nullptr;  // per launch block: (member, block index within the member)
+    size_t cap_blocks = 0;
+    std::vector<int2> h_block_map;  // the map last uploaded
     ReduceJob* d_jobs[2] = {nullptr, nullptr};  // per launch parity
     int* d_left = nullptr;  // step budgets: [0, m) read by parity-0 launches, [m, 2m) by parity 1
     size_t cap_members = 0;
@@ -93,7 +95,7 @@ void free_groups(lbm2d_batch* b) {
     for (auto& g : b->groups) {
         cudaFreeAsync(g.d_params[0], b->stream);
         cudaFreeAsync(g.d_params[1], b->stream);
-        cudaFreeAsync(g.d_block_start, b->stream);
+        if (g.d_block_map) cudaFreeAsync(g.d_block_map, b->stream);
         cudaFreeAsync(g.d_jobs[0], b->stream);
         cudaFreeAsync(g.d_jobs[1], b->stream);
         cudaFreeAsync(g.d_left, b->stream);
@@ -136,7 +138,6 @@ int build_layout(lbm2d_batch* b) {
         const size_t m = g.members.size();
         BCK(cudaMallocAsync(&g.d_params[0], m * sizeof(KParams), b->stream), "batch params");
         BCK(cudaMallocAsync(&g.d_params[1], m * sizeof(KParams), b->stream), "batch params");
-        BCK(cudaMallocAsync(&g.d_block_start, (m + 1) * sizeof(int), b->stream), "batch table");
         BCK(cudaMallocAsync(&g.d_jobs[0], m * sizeof(ReduceJob), b->stream), "batch jobs");
         BCK(cudaMallocAsync(&g.d_jobs[1], m * sizeof(ReduceJob), b->stream), "batch jobs");
         BCK(cudaMallocAsync(&g.d_left, 2 * m * sizeof(int), b->stream), "batch budgets");
@@ -256,8 +257,28 @@ int prepare(lbm2d_batch* b) {
         BCK(cudaMemcpyAsync(g.d_params[1], p1, m * sizeof(KParams), cudaMemcpyHostToDevice, b->stream), "params");
         // budgets at the start of the call, read by the first (parity-0) launch
         BCK(cudaMemcpyAsync(g.d_left, left, m * sizeof(int), cudaMemcpyHostToDevice, b->stream), "budgets");
-        BCK(cudaMemcpyAsync(g.d_block_start, start.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice, b->stream),
-            "table");
+        // the block map (rebuilt only when the member sizes or the shape change)
+        std::vector<int2> map((size_t)g.nblocks);
+        for (size_t k = 0; k < m; ++k)
+            for (int q = start[k]; q < start[k + 1]; ++q) map[(size_t)q] = make_int2((int)k, q - start[k]);
+        if (map.size() != g.h_block_map.size() ||
+            !std::equal(map.begin(), map.end(), g.h_block_map.begin(),
+                        [](const int2& a, const int2& c) { return a.x == c.x && a.y == c.y; })) {
+            if (map.size() != g.h_block_map.size()) b->graph_valid = false;  // the grid size changed
+            if (map.size() > g.cap_blocks) {
+                if (g.d_block_map) cudaFreeAsync(g.d_block_map, b->stream);
+                g.d_block_map = nullptr;
+                BCK(cudaMallocAsync(&g.d_block_map, std::max<size_t>(map.size(), 1) * sizeof(int2), b->stream),
+                    "batch block map");
+                g.cap_blocks = map.size();
+                b->graph_valid = false;  // captured launches name the old buffer
+            }
+            if (!map.empty())
+                BCK(cudaMemcpyAsync(g.d_block_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                    b->stream),
+                    "batch block map");
+            g.h_block_map.swap(map);
+        }
         for (int par = 0; par < 2; ++par)
             if (!jobs[par].empty())
                 BCK(cudaMemcpyAsync(g.d_jobs[par], jobs[par].data(), jobs[par].size() * sizeof(ReduceJob),
@@ -276,8 +297,8 @@ int launch_one(lbm2d_batch* b, int parity) {
         int e = g.kind == KERNEL_TILES
                     ? launch_tiles_batch(g.storage, g.thermal != 0, g.d_params[parity], g.d_tile_member,
                                          g.d_tile_start, g.ntiles, g.grid, b->d_status, b->stream)
-                    : launch_batch_step(g.storage, g.d_params[parity], g.d_block_start, (int)g.members.size(),
-                                        g.nblocks, g.thermal, b->bx, b->by, b->stream, g.kind == KERNEL_PAIR ? 1 : 0);
+                    : launch_batch_step(g.storage, g.d_params[parity], g.d_block_map, g.nblocks, g.thermal, b->bx,
+                                        b->by, b->stream, g.kind == KERNEL_PAIR ? 1 : 0);
         ++b->launches;
         if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
         if (g.njobs > 0) {

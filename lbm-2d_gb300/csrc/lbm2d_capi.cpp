@@ -256,8 +256,11 @@ int upload_geometry(lbm2d_solver* h) {
     return LBM2D_OK;
 }
 
+// The paired thermal form (step_pair_kernel<T, true>) measured slower than the
+// one-node kernel on heated cavities (2048^2 FP32: 25.7 against 30.2 GLUPS;
+// 124 registers a thread): thermal solves pair only on request (variant 2).
 bool use_pair(const lbm2d_solver* h) {
-    return h->variant != 1 && (h->nx % 2 == 0) && !h->thermal && h->storage != ST_FP64;
+    return h->variant != 1 && (h->nx % 2 == 0) && h->storage != ST_FP64 && (!h->thermal || h->variant == 2);
 }
 
 int kernel_kind(const lbm2d_solver* h) {
@@ -266,7 +269,6 @@ int kernel_kind(const lbm2d_solver* h) {
     if (h->variant == 0 && tiles_ok) {
         if (rows_eligible(h->storage, h->nx, h->ny, h->thermal) && (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
             return KERNEL_ROWS;
-        if (h->thermal || h->in_batch) return KERNEL_TILES;
     }
     if (!use_pair(h)) return KERNEL_SCALAR;
     return KERNEL_PAIR;

@@ -1076,6 +1076,66 @@ __device__ __forceinline__ void collide_pair_dev(const KParams& p, uint32_t fla,
     }
 }
 
+// The thermal double distribution of two nodes at once (FP32x2), in storage
+// units: collide_dev<true>'s thermal part (src/lbm.hpp:357-397,
+// src/thermal.hpp:25-52) after collide_pair_dev has collided f.  u comes from
+// the post-collision f (d); g relaxes with omega_k toward w T (1 + 3 c.u +
+// 4.5 (c.u)^2 - 1.5 u^2) on deviations e = g - w T_ref; the Boussinesq force
+// (0, -beta (T - T_ref) g_y) is added to f as w (3 c.F + 9 (c.u)(c.F)).  A
+// lane that is not collided (solid) keeps its input.
+template <class T>
+__device__ __forceinline__ void thermal_pair_dev(const KParams& p, bool fa_ok, bool fb_ok, F2 d[9], F2 e[9]) {
+    constexpr float S = Pop<T>::kS, iS = Pop<T>::kInvS;
+    const Phys<float>& q = p.pf;
+    const F2 drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+    const F2 mx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
+    const F2 my = (d[2] - d[4]) + (d[5] + d[6]) - (d[7] + d[8]);
+    const F2 k = rcp2(drho + sp2(S));  // 1 / (rho * S)
+    const F2 u = mx * k, v = my * k, usq = fma2(u, u, v * v);
+    const F2 dTS = ((e[0] + e[1]) + (e[2] + e[3])) + ((e[4] + e[5]) + (e[6] + e[7])) + e[8];
+    const F2 dT = dTS * sp2(iS);
+    const F2 TS = fma2(dT, sp2(S), sp2(q.T_ref * S));  // T * S
+    const F2 om = sp2(q.omega_k);
+    F2 o[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const F2 ed = sp2(float(CXf(i))) * u + sp2(float(CYf(i))) * v;
+        const F2 poly = fma2(sp2(4.5f) * ed, ed, fma2(sp2(3.0f), ed, sp2(-1.5f) * usq));
+        const F2 geS = sp2(float(wgt(i))) * fma2(TS, poly, dTS);
+        o[i] = e[i] - om * (e[i] - geS);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) e[i] = mk2(fa_ok ? o[i].v.x : e[i].v.x, fb_ok ? o[i].v.y : e[i].v.y);
+    if (q.beta > 0.0f && q.g_buoy != 0.0f) {
+        const F2 fyb = sp2(-q.beta * q.g_buoy) * dT;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            if (CYf(i) == 0) continue;
+            const F2 eu = sp2(float(CXf(i))) * u + sp2(float(CYf(i))) * v;
+            const F2 Fd = sp2(float(CYf(i))) * fyb;
+            const F2 inc = sp2(float(wgt(i)) * S) * fma2(sp2(9.0f) * eu, Fd, sp2(3.0f) * Fd);
+            d[i] = mk2(fa_ok ? d[i].v.x + inc.v.x : d[i].v.x, fb_ok ? d[i].v.y + inc.v.y : d[i].v.y);
+        }
+    }
+}
+
+// build_dev_s<T> for the thermal DDF: f and g deviations in storage units.
+template <class T>
+__device__ __forceinline__ void build_dev_s_th(const KParams& p, int x, int y, uint32_t fl, float d[9], float e[9]) {
+    if (!special_node<true>(p, x, y, fl)) {
+        pull_raw<T>(p, static_cast<const T*>(p.fin), x, y, d);
+        pull_raw<T>(p, static_cast<const T*>(p.gin), x, y, e);
+        return;
+    }
+    float f[9], g[9];
+    build_state<T, true>(p, x, y, fl, f, g);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        d[j] = (f[j] - p.shf[j]) * Pop<T>::kS;
+        e[j] = (g[j] - p.shg[j]) * Pop<T>::kS;
+    }
+}
+
 template <class T>
 struct PairStore;
 // Two x-neighbours (index i even) in storage units as one 8-byte / 4-byte store.

@@ -18,6 +18,8 @@
 //                 mask, wall distance, and per-slot q / wall velocity for
 //                 interpolated links.
 #pragma once
+#include <vector_types.h>
+
 #include <cstddef>
 #include <cstdint>
 
@@ -196,13 +198,13 @@ int launch_frame(int storage, const KParams& p, const FOut& o, void* stream);
 // Collide an FP64 AoS state S (device) into the stored post-collision state.
 int launch_prologue(int storage, const KParams& p, const double* f_aos, const double* g_aos, void* stream);
 // Step several instances at once: inst[] holds one KParams per instance and
-// block_start[] (ninst+1 entries, device memory) the first launch block of
-// each instance; nblocks = block_start[ninst].  A launch block walks
+// block_map[b] (device memory, nblocks entries) the instance of launch block
+// b and b's index among that instance's blocks.  A launch block walks
 // kBatchTiles consecutive blocks (tiles) of its instance's block grid, so an
 // instance with gx*gy tiles owns ceil(gx*gy / kBatchTiles) launch blocks.
 constexpr int kBatchTiles = 4;
-int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
-                      int bx, int by, void* stream, int pair);
+int launch_batch_step(int storage, const KParams* inst, const int2* block_map, int nblocks, int thermal, int bx,
+                      int by, void* stream, int pair);
 int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream);
 // acc[0..4] += mass, x/y momentum, sum |u - u_prev|^2, sum |u|^2 (FP64).
 int launch_diagnostics(int storage, const KParams& p, double* acc, float* prev_uv, int have_prev, void* stream);

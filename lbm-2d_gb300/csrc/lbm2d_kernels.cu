@@ -27,8 +27,9 @@ namespace lbm2d {
 namespace {
 
 // One step of the paired block (bxi, byi) of an instance whose paired block
-// grid is gx wide (non-thermal, FP32/FP16/BF16 storage, nx even).
-template <class T>
+// grid is gx wide (FP32/FP16/BF16 storage, nx even; TH: with the thermal
+// double distribution, collided by thermal_pair_dev).
+template <class T, bool TH = false>
 __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int byi, int gx) {
     const int x0 = 2 * (bxi * blockDim.x + threadIdx.x);
     const int y = byi * blockDim.y + threadIdx.y;
@@ -44,8 +45,14 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
         const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
         constexpr float iS = Pop<T>::kInvS;
         float fa[9], fb[9];  // deviations in storage units
-        build_dev_s<T>(p, x0, y, fl.x, fa);
-        build_dev_s<T>(p, x0 + 1, y, fl.y, fb);
+        float ea[TH ? 9 : 1], eb[TH ? 9 : 1];  // thermal deviations (TH)
+        if constexpr (TH) {
+            build_dev_s_th<T>(p, x0, y, fl.x, fa, ea);
+            build_dev_s_th<T>(p, x0 + 1, y, fl.y, fb, eb);
+        } else {
+            build_dev_s<T>(p, x0, y, fl.x, fa);
+            build_dev_s<T>(p, x0 + 1, y, fl.y, fb);
+        }
         const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
         if ((fl.x | fl.y) & FLAG_BOUNDARY) {
             // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
@@ -75,12 +82,25 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
 #pragma unroll
             for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
             collide_pair_dev<T>(p, fl.x, fl.y, oka, okb, f);
+            if constexpr (TH) {
+                F2 g[9];
+#pragma unroll
+                for (int j = 0; j < 9; ++j) g[j] = mk2(ea[j], eb[j]);
+                thermal_pair_dev<T>(p, oka, okb, f, g);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) {
+                    ea[j] = g[j].v.x;
+                    eb[j] = g[j].v.y;
+                }
+            }
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
                 fa[j] = f[j].v.x;
                 fb[j] = f[j].v.y;
             }
         }
+        // a solid node's state never changes once settled (the heated
+        // cavity's Dirichlet passes rewrite node states every step)
         const bool settled = p.skip_settled_solids && y < p.ny - 1;
         const bool skip_a = !oka && settled && x0 > 0;
         const bool skip_b = !okb && settled && x0 + 1 < p.nx - 1;
@@ -91,6 +111,12 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
             if constexpr (Pop<T>::kRounds) rand9(skey + n0, rb);
 #pragma unroll
             for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
+            if constexpr (TH) {
+                T* __restrict__ Go = static_cast<T*>(p.gout);
+                if constexpr (Pop<T>::kRounds) rand9((skey + n0) ^ 0x6A09E667u, rb);
+#pragma unroll
+                for (int j = 0; j < 9; ++j) PairStore<T>::st(Go + j * N, n0, ea[j], eb[j], rb[j]);
+            }
         }
     }
     if (p.block_slot) {
@@ -115,9 +141,9 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
     }
 }
 
-template <class T>
+template <class T, bool TH>
 __global__ void __launch_bounds__(512) step_pair_kernel(const KParams p) {
-    step_pair_block<T>(p, blockIdx.x, blockIdx.y, gridDim.x);
+    step_pair_block<T, TH>(p, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 template <class T, bool TH>
@@ -126,40 +152,27 @@ __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
 }
 
 // Many independent instances in one launch (the tile-to-instance table):
-// instance k owns the launch blocks [block_start[k], block_start[k+1]) and
-// walks its own block grid (gx = p.gx blocks wide).  The block finds its
-// instance by binary search and stages that instance's parameters in shared
-// memory once.  An instance with a step budget (left_in set) whose budget is
-// spent does nothing; otherwise its first block hands the decremented budget
-// to the next launch through left_out (the two budget words swap roles
-// between launches, so no launch reads a word it writes).  Returns false
-// when the block has nothing to do.
-__device__ __forceinline__ bool batch_block_begin(const KParams* __restrict__ inst,
-                                                  const int* __restrict__ block_start, int ninst, KParams& sp,
-                                                  int& local) {
-    __shared__ int s_inst, s_left;
+// instance k owns a contiguous range of launch blocks and walks its own block
+// grid (gx = p.gx blocks wide).  block_map[b] = (k, b's index within k), one
+// 8-byte load that every thread of the block makes (a broadcast); the block
+// then stages that instance's parameters in shared memory.  An instance with
+// a step budget (left_in set) whose budget is spent does nothing; otherwise
+// its first block hands the decremented budget to the next launch through
+// left_out (the two budget words swap roles between launches, so no launch
+// reads a word it writes).  Returns false when the block has nothing to do.
+__device__ __forceinline__ bool batch_block_begin(const KParams* __restrict__ inst, const int2* __restrict__ block_map,
+                                                  KParams& sp, int& local) {
+    __shared__ int s_left;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int b = blockIdx.x;
-    if (tid == 0) {
-        int lo = 0, hi = ninst - 1;  // last k with block_start[k] <= b
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (block_start[mid] <= b)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        s_inst = lo;
-    }
-    __syncthreads();
-    const int k = s_inst;
+    const int2 km = __ldg(block_map + blockIdx.x);
+    const int k = km.x;
+    local = km.y;
     {
         const int* src = reinterpret_cast<const int*>(inst + k);
         int* dst = reinterpret_cast<int*>(&sp);
         const int nw = (int)(sizeof(KParams) / sizeof(int));
         for (int w = tid; w < nw; w += blockDim.x * blockDim.y) dst[w] = src[w];
     }
-    local = b - block_start[k];
     if (tid == 0) {
         const int* li = inst[k].left_in;
         const int L = li ? *li : 1;
@@ -172,10 +185,10 @@ __device__ __forceinline__ bool batch_block_begin(const KParams* __restrict__ in
 
 template <class T, bool TH>
 __global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restrict__ inst,
-                                                         const int* __restrict__ block_start, int ninst) {
+                                                         const int2* __restrict__ block_map) {
     __shared__ KParams sp;
     int local;
-    if (!batch_block_begin(inst, block_start, ninst, sp, local)) return;
+    if (!batch_block_begin(inst, block_map, sp, local)) return;
     const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
     for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
         step_block<T, TH>(sp, t % sp.gx, t / sp.gx, sp.gx);
@@ -186,13 +199,25 @@ __global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restri
 // the few spilled values cost (C4 batch +1.6% FP32, +3% FP16).
 template <class T>
 __global__ void __launch_bounds__(512, 2) batch_step_pair_kernel(const KParams* __restrict__ inst,
-                                                              const int* __restrict__ block_start, int ninst) {
+                                                              const int2* __restrict__ block_map) {
     __shared__ KParams sp;
     int local;
-    if (!batch_block_begin(inst, block_start, ninst, sp, local)) return;
+    if (!batch_block_begin(inst, block_map, sp, local)) return;
     const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
     for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
         step_pair_block<T>(sp, t % sp.gx, t / sp.gx, sp.gx);
+}
+
+// The thermal form: twice the populations, so no register cap.
+template <class T>
+__global__ void __launch_bounds__(512) batch_step_pair_th_kernel(const KParams* __restrict__ inst,
+                                                               const int2* __restrict__ block_map) {
+    __shared__ KParams sp;
+    int local;
+    if (!batch_block_begin(inst, block_map, sp, local)) return;
+    const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
+    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+        step_pair_block<T, true>(sp, t % sp.gx, t / sp.gx, sp.gx);
 }
 
 // Post-stream state of node (x, y) in FP64 as the step rebuilds it (before
@@ -635,24 +660,37 @@ __global__ void diagnostics_kernel(const KParams p, double* __restrict__ acc, fl
 // Prologue of a paired solver: the same packed collision as step_pair_block,
 // so a re-collided state (parameter change, autotuner restore) rounds exactly
 // as the steps do.
-template <class T>
-__global__ void prologue_pair_kernel(const KParams p, const double* __restrict__ fa) {
+template <class T, bool TH>
+__global__ void prologue_pair_kernel(const KParams p, const double* __restrict__ fa, const double* __restrict__ ga) {
     const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x0 >= p.nx || y >= p.ny) return;
     const size_t n0 = (size_t)y * p.nx + x0;
     const uint32_t fla = p.flags[n0], flb = p.flags[n0 + 1];
     const bool oka = !(fla & FLAG_SOLID), okb = !(flb & FLAG_SOLID);
-    F2 f[9];
+    F2 f[9], g[9];
     const double S = Pop<T>::kS;
     for (int j = 0; j < 9; ++j)
         f[j] = mk2(float((fa[n0 * 9 + j] - double(p.shf[j])) * S), float((fa[(n0 + 1) * 9 + j] - double(p.shf[j])) * S));
-    if (oka || okb) collide_pair_dev<T>(p, fla, flb, oka, okb, f);
+    if (TH)
+        for (int j = 0; j < 9; ++j)
+            g[j] = mk2(float((ga[n0 * 9 + j] - double(p.shg[j])) * S),
+                       float((ga[(n0 + 1) * 9 + j] - double(p.shg[j])) * S));
+    if (oka || okb) {
+        collide_pair_dev<T>(p, fla, flb, oka, okb, f);
+        if (TH) thermal_pair_dev<T>(p, oka, okb, f, g);
+    }
     T* Fo = static_cast<T*>(p.fout);
     const size_t N = (size_t)p.N;
     uint32_t rb[9] = {};
-    if constexpr (Pop<T>::kRounds) rand9(seed_key(p.seed_host) + (uint32_t)n0, rb);
+    const uint32_t key = seed_key(p.seed_host) + (uint32_t)n0;
+    if constexpr (Pop<T>::kRounds) rand9(key, rb);
     for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, f[j].v.x, f[j].v.y, rb[j]);
+    if (TH) {
+        T* Go = static_cast<T*>(p.gout);
+        if constexpr (Pop<T>::kRounds) rand9(key ^ 0x6A09E667u, rb);
+        for (int j = 0; j < 9; ++j) PairStore<T>::st(Go + j * N, n0, g[j].v.x, g[j].v.y, rb[j]);
+    }
     pass_seed(p, p.seed_host, x0 == 0 && y == 0);
 }
 
@@ -691,21 +729,24 @@ __global__ void batch_force_reduce_kernel(const ReduceJob* __restrict__ jobs) {
 }
 
 template <class T>
-int launch_batch_t(const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal, int bx, int by,
+int launch_batch_t(const KParams* inst, const int2* block_map, int nblocks, int thermal, int bx, int by,
                    cudaStream_t s, int pair) {
-    if (nblocks <= 0 || ninst <= 0) return 0;
+    if (nblocks <= 0) return 0;
     dim3 blk(bx, by);
     if (pair) {
         if constexpr (!std::is_same<T, double>::value) {
-            batch_step_pair_kernel<T><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
+            if (thermal)
+                batch_step_pair_th_kernel<T><<<nblocks, blk, 0, s>>>(inst, block_map);
+            else
+                batch_step_pair_kernel<T><<<nblocks, blk, 0, s>>>(inst, block_map);
             return (int)cudaGetLastError();
         }
         return (int)cudaErrorInvalidValue;
     }
     if (thermal)
-        batch_step_kernel<T, true><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
+        batch_step_kernel<T, true><<<nblocks, blk, 0, s>>>(inst, block_map);
     else
-        batch_step_kernel<T, false><<<nblocks, blk, 0, s>>>(inst, block_start, ninst);
+        batch_step_kernel<T, false><<<nblocks, blk, 0, s>>>(inst, block_map);
     return (int)cudaGetLastError();
 }
 
@@ -714,7 +755,10 @@ int launch_step_t(const KParams& p, int bx, int by, cudaStream_t s) {
     if (p.pair) {
         if constexpr (!std::is_same<T, double>::value) {
             dim3 blk(bx, by), grd((p.nx / 2 + bx - 1) / bx, (p.ny + by - 1) / by);
-            step_pair_kernel<T><<<grd, blk, 0, s>>>(p);
+            if (p.thermal)
+                step_pair_kernel<T, true><<<grd, blk, 0, s>>>(p);
+            else
+                step_pair_kernel<T, false><<<grd, blk, 0, s>>>(p);
             return (int)cudaGetLastError();
         }
         return (int)cudaErrorInvalidValue;
@@ -753,7 +797,10 @@ int launch_prologue_t(const KParams& p, const double* fa, const double* ga, cuda
     if (p.pair) {
         if constexpr (!std::is_same<T, double>::value) {
             dim3 blk(128, 2), grd((p.nx / 2 + 127) / 128, (p.ny + 1) / 2);
-            prologue_pair_kernel<T><<<grd, blk, 0, s>>>(p, fa);
+            if (p.thermal)
+                prologue_pair_kernel<T, true><<<grd, blk, 0, s>>>(p, fa, ga);
+            else
+                prologue_pair_kernel<T, false><<<grd, blk, 0, s>>>(p, fa, nullptr);
             return (int)cudaGetLastError();
         }
         return (int)cudaErrorInvalidValue;
@@ -849,14 +896,14 @@ int launch_prologue(int storage, const KParams& p, const double* fa, const doubl
     return (int)cudaErrorInvalidValue;
 }
 
-int launch_batch_step(int storage, const KParams* inst, const int* block_start, int ninst, int nblocks, int thermal,
-                      int bx, int by, void* stream, int pair) {
+int launch_batch_step(int storage, const KParams* inst, const int2* block_map, int nblocks, int thermal, int bx,
+                      int by, void* stream, int pair) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (storage) {
-        case ST_FP32: return launch_batch_t<float>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
-        case ST_FP16: return launch_batch_t<__half>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
-        case ST_BF16: return launch_batch_t<__nv_bfloat16>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
-        case ST_FP64: return launch_batch_t<double>(inst, block_start, ninst, nblocks, thermal, bx, by, s, pair);
+        case ST_FP32: return launch_batch_t<float>(inst, block_map, nblocks, thermal, bx, by, s, pair);
+        case ST_FP16: return launch_batch_t<__half>(inst, block_map, nblocks, thermal, bx, by, s, pair);
+        case ST_BF16: return launch_batch_t<__nv_bfloat16>(inst, block_map, nblocks, thermal, bx, by, s, pair);
+        case ST_FP64: return launch_batch_t<double>(inst, block_map, nblocks, thermal, bx, by, s, pair);
     }
     return (int)cudaErrorInvalidValue;
 }

@@ -158,17 +158,17 @@ int ibm_from_stage(lbm2d_solver* h, const KParams& p);
 void ibm_state_params(const lbm2d_solver* h, KParams& p);
 void ibm_release(lbm2d_solver* h);
 // Two x-neighbours per thread (packed FP32x2 collision) when nx is even and
-// the step is non-thermal FP32/FP16/BF16.
+// the storage is FP32/FP16/BF16 (for the thermal DDF only with variant 2).
 bool use_pair(const lbm2d_solver* h);
 // Step kernel of the next step: KERNEL_SCALAR, KERNEL_PAIR, KERNEL_ROWS
 // (the bulk-copy row pipeline) or KERNEL_TILES (the bulk-copy tile pipeline:
-// any nx, the thermal DDF, batches).  Batch members run the batched tile
-// kernel (FP64 storage: the batched one-node kernel), except members of at
-// least kBatchSoloNodes nodes that qualify for the row pipeline: those fill
-// the GPU alone and get their own row-pipeline launches inside the batch's
-// step.
+// any nx, the thermal DDF, batches; kernel variant 3 only -- on the measured
+// workloads the other kernels were faster).  Batch members run the batched
+// paired / one-node kernels, except members of at least kBatchSoloNodes nodes
+// that qualify for the row pipeline: those fill the GPU alone and get their
+// own row-pipeline launches inside the batch's step.
 enum KernelKind : int { KERNEL_SCALAR = 0, KERNEL_PAIR = 1, KERNEL_ROWS = 2, KERNEL_TILES = 3 };
-constexpr long long kBatchSoloNodes = 1LL << 20;
+constexpr long long kBatchSoloNodes = 1LL << 21;
 int kernel_kind(const lbm2d_solver* h);
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
 // kernel parameters of the next step (fin = current buffer); returns status.

@@ -148,13 +148,13 @@ def test_member_budgets(product, oracle_lib, storage):
 
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
 def test_large_member_runs_solo(product, oracle_lib, storage):
-    """A member of at least 2^20 nodes that qualifies for the row pipeline is
+    """A member of at least 2^21 nodes that qualifies for the row pipeline is
     stepped with its own row-pipeline launches inside the batch call: it
     reports that kernel, takes exactly its budget, and ends bit-for-bit where
     the same solve stepped alone ends."""
     import copy
     big = copy.deepcopy(CS.CASES["ribs_les"])
-    big["nx"], big["ny"] = 1024, 1024
+    big["nx"], big["ny"] = 2048, 1024
     small = CS.CASES["cylinder_mei"]
     b = product.Batch()
     s_big = gpu_solver(product, oracle_lib, big, storage)

@@ -10,9 +10,9 @@ consecutive nodes, any grid width, the thermal DDF, batches).
   the one-node kernel; FP16 within the shifted-storage bound.
 * The thermal DDF: against the one-node kernel (the same per-node collision
   and rounding noise) within 1e-6 (FP32) and 1e-4 (FP16).
-* Batches: every member of a mixed batch (odd sizes, thermal and not, FP32
-  and FP16) ends with the populations of the same solve stepped alone by the
-  single-instance tile kernel, bit for bit (the same per-node arithmetic);
+* Batches of tile-kernel members (variant 3): every member of a mixed batch
+  (odd sizes, thermal and not, FP32 and FP16) ends with the populations of
+  the same solve stepped alone by the single-instance tile kernel, bit for bit (the same per-node arithmetic);
   drag/lift within 1e-12 (the second stage sums the same FP64 partials in
   another fixed order).
 """
@@ -117,8 +117,8 @@ def thermal_spec(key):
 @pytest.mark.parametrize("key", sorted(THERMAL))
 def test_tiles_thermal_match_one_node_kernel(product, oracle_lib, key, storage, tol):
     spec = thermal_spec(key)
-    kern, f_t, sums_t, g_t = run_gpu(product, oracle_lib, spec, 0, storage)
-    assert kern == product.KERNEL_TILES  # the default for the thermal DDF
+    kern, f_t, sums_t, g_t = run_gpu(product, oracle_lib, spec, 3, storage)
+    assert kern == product.KERNEL_TILES
     k1, f_1, sums_1, g_1 = run_gpu(product, oracle_lib, spec, 1, storage)
     assert k1 == product.KERNEL_SCALAR
     assert rel_l2(f_t, f_1) < tol
@@ -147,6 +147,7 @@ def test_batch_members_equal_single_tiles(product, oracle_lib, steps):
     mem = []
     for spec, st in specs:
         s = gpu_solver(product, oracle_lib, spec, st)
+        s.set_kernel_variant(3)  # batch members run the batched tile kernel
         b.add(s, spec["tau"], spec["u"])
         mem.append(s)
     assert all(s.info().kernel == product.KERNEL_TILES for s in mem)
