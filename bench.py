@@ -217,13 +217,20 @@ def _cpu_impl():
     return "oracle", "port", "oracle/lbm_oracle.c (OpenMP restatement of the reference step)"
 
 
-def _oracle_channel(size, kind="oracle"):
+def _oracle_channel(size, kind="oracle", ny=None):
+    """The channel workload in the oracle: size x size with the circle count
+    scaled by area, or (with ny) exactly the nx x ny workload of the GPU runs."""
     from oracle import oracle as O
     if not os.path.exists(O.LIB_ORACLE):
         O.build()
-    nc = max(1, int(round(N_CIRCLES * (size * size) / (NX * NY))))
-    mask, _ = CS.channel_circles_mask(size, size, nc, RMIN, RMAX, SEED)
-    s = O.Solver(size, size, kind)
+    nx = size
+    if ny is None:
+        ny = size
+        nc = max(1, int(round(N_CIRCLES * (size * size) / (NX * NY))))
+    else:
+        nc = N_CIRCLES
+    mask, _ = CS.channel_circles_mask(nx, ny, nc, RMIN, RMAX, SEED)
+    s = O.Solver(nx, ny, kind)
     s.set_case(O.RIBS, O.MRT, True, CS_LES)
     s.obstacle[:] = mask
     s.set_body_force(BODY_FORCE)
@@ -248,19 +255,39 @@ def cpu_sample(size: int = 1024, budget_s: float = 12.0, max_steps: int = 50):
     return size * size * n / dt / 1e6, dt, nc, n
 
 
+def _cpu_model():
+    """The host CPU's model name and logical core count (lscpu)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        model = next((l.split(":", 1)[1].strip() for l in out.splitlines() if l.startswith("Model name")), "?")
+    except Exception:
+        model = "?"
+    return f"{model}, {os.cpu_count()} logical cores"
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    size = args.cpu_size
     kind, ckind, what = _cpu_impl()
-    s, nc = _oracle_channel(size, kind)
-    for _ in range(min(args.warmup, 1)):
+    # the GPU arm's own workload (nx x ny, the same 64 circles) unless a
+    # square sample is asked for; steps stop at the time budget
+    if args.ref_size > 0:
+        nx = ny = args.ref_size
+        s, nc = _oracle_channel(nx, kind)
+    else:
+        nx, ny = args.nx, args.ny
+        s, nc = _oracle_channel(nx, kind, ny)
+    same = (nx, ny) == (args.nx, args.ny)
+    # a CPU loop needs no warm-up beyond its first touch of the arrays; at the
+    # full size one step takes about a minute (the reference's per-step
+    # wall-distance sweep), so only a sample warms up
+    for _ in range(0 if same else min(args.warmup, 1)):
         s.step(TAU, U0)
     per = []
     t_all = time.perf_counter()
-    for _ in range(args.steps):  # each step is one oracle step over the size x size sample
+    for _ in range(args.steps):  # each step is one oracle step over the whole sample
         t0 = time.perf_counter()
         s.step(TAU, U0)
         per.append(time.perf_counter() - t0)
@@ -268,18 +295,19 @@ def run_reference(args):
             break
     s.close()
     dt = float(np.sum(per))
-    value = size * size * len(per) / dt / 1e9
+    value = nx * ny * len(per) / dt / 1e9
+    size = f"{nx}x{ny}"
     line = {
         "impl": "reference", "metric": "GLUPS (D2Q9 step, lattice updates/s) & %HBM roofline, FP32 vs FP16/BF16 storage",
         "value": value, "unit": "GLUPS", "n_gpus": args.gpus, "steps": len(per), "warmup": args.warmup,
         "ms_per_step": dt / len(per) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args.nx, args.ny),
-                   "sample": f"{size}x{size} with {nc} circles (same generator and physics), "
+        "config": {"workload": workload_name(args.nx, args.ny), "same_config": same,
+                   "sample": f"{size} with {nc} circles (same generator and physics), "
                              f"{len(per)} of {args.steps} requested steps within {args.ref_budget:.0f} s"},
-        "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": ckind,
+        "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": ckind, "cpu": _cpu_model(),
                          "sample": f"{what}, its per-step wall-distance sweep included, {cores} threads, "
-                                   f"{size}x{size}, {len(per)} steps"},
+                                   f"{size}, {len(per)} steps"},
         "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -779,7 +807,9 @@ def main():
     ap.add_argument("--plain", default="fp32,fp16", help="storages also timed without LES (plain MRT)")
     ap.add_argument("--variant", type=int, default=0, help="step kernel: 0 paired nodes per thread, 1 one node")
     ap.add_argument("--cpu-size", type=int, default=1024)
-    ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
+    ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds cap of the reference arm")
+    ap.add_argument("--ref-size", type=int, default=0,
+                    help="reference arm on a size x size sample (0: the GPU arm's own nx x ny workload)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (default: --steps)")
@@ -920,7 +950,7 @@ def main():
             cores = os.cpu_count() or 1
             _, ckind, what = _cpu_impl()
             mlups, dt, nc, n = cpu_sample(args.cpu_size)
-            cpu = {"value": mlups / 1e3, "unit": "GLUPS", "cores": cores, "kind": ckind,
+            cpu = {"value": mlups / 1e3, "unit": "GLUPS", "cores": cores, "kind": ckind, "cpu": _cpu_model(),
                    "sample": f"{what}, per-step wall-distance sweep included, {cores} threads, same generator "
                              f"and physics at {args.cpu_size}x{args.cpu_size} with {nc} circles, {n} steps in "
                              f"{dt:.1f} s"}
