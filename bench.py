@@ -587,7 +587,7 @@ def batch_block(args, lbm2d, storage, steps):
     return line
 
 
-def thermal_block(lbm2d, torch, n=2048, steps=200, storages=("fp32", "fp16")):
+def thermal_block(lbm2d, torch, n=4096, steps=200, storages=("fp32", "fp16")):
     """The thermal double-distribution step on its own: the heated-cavity
     driver's set-up (src/thermal_cavity.cpp: walls all round, hot left and cold
     right columns, adiabatic top and bottom rows, Boussinesq buoyancy at
@@ -616,6 +616,8 @@ def thermal_block(lbm2d, torch, n=2048, steps=200, storages=("fp32", "fp16")):
         except lbm2d.LBMError:
             diverged = True
         kernel = KERNEL_NAMES[s.info().kernel][0]
+        if kernel == "step_kernel" and st != "fp64":
+            kernel = "step_th_kernel"  # the thermal one-node kernel at six blocks per SM
         s.close()
         bpu = 2 * 2 * 9 * lbm2d.BYTES_PER_POP[st]
         glups = n * n * steps / (ms * 1e-3) / 1e9
@@ -829,7 +831,7 @@ def main():
                     help="skip the precision, thermal, batch and serving blocks of the default line")
     ap.add_argument("--precision-steps", type=int, default=1000)
     ap.add_argument("--batch-steps", type=int, default=5000)
-    ap.add_argument("--thermal-n", type=int, default=2048)
+    ap.add_argument("--thermal-n", type=int, default=4096)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

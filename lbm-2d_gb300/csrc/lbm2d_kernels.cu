@@ -151,6 +151,18 @@ __global__ void __launch_bounds__(512) step_kernel(const KParams p) {
     step_block<T, TH>(p, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
+// The thermal one-node step in blocks of at most 256 threads with a register
+// cap that lets MINB of them share an SM: more warps, so more of the 18
+// population loads a node makes in flight per SM.  Six blocks (40 registers,
+// a few bytes spilled) against the uncapped kernel's four (64 registers) on
+// the heated cavity: FP32 4096^2 38.7 against 35.4 GLUPS (0.82 against 0.75
+// of the measured copy bandwidth at 144 B per update), 2048^2 32.1 against
+// 29.9; FP16 +8-10%.
+template <class T, int MINB>
+__global__ void __launch_bounds__(256, MINB) step_th_kernel(const KParams p) {
+    step_block<T, true>(p, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
 // Many independent instances in one launch (the tile-to-instance table):
 // instance k owns a contiguous range of launch blocks and walks its own block
 // grid (gx = p.gx blocks wide).  block_map[b] = (k, b's index within k), one
@@ -192,6 +204,21 @@ __global__ void __launch_bounds__(512) batch_step_kernel(const KParams* __restri
     const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
     for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
         step_block<T, TH>(sp, t % sp.gx, t / sp.gx, sp.gx);
+}
+
+// The thermal batch members' one-node step, five blocks per SM (48
+// registers).  Taken for the 16-bit forms only: on the C4 thermal members
+// FP16 35.5 against 31.0 GLUPS, while FP32 spills more than it gains (28.5
+// against 30.3).
+template <class T, int MINB>
+__global__ void __launch_bounds__(256, MINB) batch_step_th_kernel(const KParams* __restrict__ inst,
+                                                                 const int2* __restrict__ block_map) {
+    __shared__ KParams sp;
+    int local;
+    if (!batch_block_begin(inst, block_map, sp, local)) return;
+    const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
+    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+        step_block<T, true>(sp, t % sp.gx, t / sp.gx, sp.gx);
 }
 
 // Capped at 64 registers (2 x 512 threads per SM): the batched kernel waits
@@ -743,6 +770,12 @@ int launch_batch_t(const KParams* inst, const int2* block_map, int nblocks, int 
         }
         return (int)cudaErrorInvalidValue;
     }
+    if constexpr (sizeof(T) == 2) {
+        if (thermal && bx * by <= 256) {
+            batch_step_th_kernel<T, 5><<<nblocks, blk, 0, s>>>(inst, block_map);
+            return (int)cudaGetLastError();
+        }
+    }
     if (thermal)
         batch_step_kernel<T, true><<<nblocks, blk, 0, s>>>(inst, block_map);
     else
@@ -764,6 +797,12 @@ int launch_step_t(const KParams& p, int bx, int by, cudaStream_t s) {
         return (int)cudaErrorInvalidValue;
     }
     dim3 blk(bx, by), grd((p.nx + bx - 1) / bx, (p.ny + by - 1) / by);
+    if constexpr (!std::is_same<T, double>::value) {
+        if (p.thermal && bx * by <= 256) {
+            step_th_kernel<T, 6><<<grd, blk, 0, s>>>(p);
+            return (int)cudaGetLastError();
+        }
+    }
     if (p.thermal)
         step_kernel<T, true><<<grd, blk, 0, s>>>(p);
     else
