@@ -124,6 +124,11 @@ KParams base_params(const lbm2d_solver* h) {
     p.nan_flag = h->d_nan;
     p.consumer_wait = h->consumer_wait;
     p.inv_nx = 1.0f / float(h->nx);
+    if (h->slot_kind == KERNEL_ROWS) {
+        p.bpairs = h->d_bpairs;
+        p.nbpairs = h->nbpairs;
+        p.bchunk = h->bchunk;
+    }
     p.pair = use_pair(h) ? 1 : 0;
     const int nbw = h->bx * (p.pair ? 2 : 1);  // node width of a block
     p.gx = (h->nx + nbw - 1) / nbw;
@@ -232,6 +237,8 @@ int upload_geometry(lbm2d_solver* h) {
     dfree(h, &h->d_rec_uw);
     dfree(h, &h->d_block_slot);
     dfree(h, &h->d_partials);
+    dfree(h, &h->d_bpairs);
+    h->nbpairs = h->bchunk = 0;
     h->nslots = 0;
     h->slot_bx = h->slot_by = 0;
     int rc;
@@ -293,8 +300,8 @@ int ensure_slots(lbm2d_solver* h) {
     if (h->slot_kind == kind && h->d_block_slot &&
         (persistent ? h->slot_grid == grid : (h->slot_bx == h->bx && h->slot_by == h->by)))
         return LBM2D_OK;
-    std::vector<int> slots;
-    int red_blocks = 0;
+    std::vector<int> slots, bpairs;
+    int red_blocks = 0, bchunk = 0;
     if (kind == KERNEL_TILES) {
         // one entry per tile of W consecutive nodes: the first of the tile's
         // per-warp slots, -1 for a tile without force nodes; then one entry
@@ -315,7 +322,36 @@ int ensure_slots(lbm2d_solver* h) {
             }
         for (int c = 0; c < grid; ++c) red_blocks += slots[(size_t)ntiles + c] > 0 ? 1 : 0;
         h->nslots = k;
+    } else if (kind == KERNEL_ROWS && rows_boundary_pass(h->storage)) {
+        // Every boundary node has a record.  The pairs (x even, x + 1) that
+        // hold one are rebuilt by a CTA before its tiles, CTA c taking the
+        // contiguous chunk [c*bchunk, (c+1)*bchunk) of the ascending list;
+        // force nodes are boundary nodes, so a CTA holds force slots when
+        // its chunk has a pair with a force record.
+        const int warps = rows_warps_per_block();
+        bpairs.reserve(h->geo.rec_node.size());
+        for (int32_t id : h->geo.rec_node) bpairs.push_back(id - (id % h->nx) % 2);
+        std::sort(bpairs.begin(), bpairs.end());
+        bpairs.erase(std::unique(bpairs.begin(), bpairs.end()), bpairs.end());
+        bchunk = bpairs.empty() ? 0 : (int)((bpairs.size() + (size_t)grid - 1) / (size_t)grid);
+        slots.assign((size_t)grid, -1);
+        for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
+            if (!h->geo.rec_force[r]) continue;
+            const int id = h->geo.rec_node[r];
+            const size_t i = (size_t)(std::lower_bound(bpairs.begin(), bpairs.end(), id - (id % h->nx) % 2) -
+                                      bpairs.begin());
+            slots[i / (size_t)bchunk] = 0;
+        }
+        int k = 0;
+        for (auto& s : slots)
+            if (s == 0) {
+                s = k;
+                k += warps;
+            }
+        h->nslots = k;
     } else if (kind == KERNEL_ROWS) {
+        // boundary pairs inline: tile t (row-major over tpr tiles per row)
+        // runs on CTA t mod grid
         const int tw = rows_tile_width(), tpr = (h->nx + tw - 1) / tw, warps = rows_warps_per_block();
         slots.assign((size_t)grid, -1);
         for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
@@ -337,7 +373,17 @@ int ensure_slots(lbm2d_solver* h) {
     }
     dfree(h, &h->d_block_slot);
     dfree(h, &h->d_partials);
+    dfree(h, &h->d_bpairs);
+    h->nbpairs = h->bchunk = 0;
     int rc;
+    if (!bpairs.empty()) {
+        if ((rc = dalloc(h, &h->d_bpairs, bpairs.size() * sizeof(int)))) return rc;
+        CK(cudaMemcpyAsync(h->d_bpairs, bpairs.data(), bpairs.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           h->stream),
+           "boundary pairs H2D");
+        h->nbpairs = (int)bpairs.size();
+        h->bchunk = bchunk;
+    }
     if ((rc = dalloc(h, &h->d_block_slot, slots.size() * sizeof(int)))) return rc;
     if ((rc = dalloc(h, &h->d_partials, (size_t)std::max(h->nslots, 1) * 2 * sizeof(double)))) return rc;
     CK(cudaMemcpyAsync(h->d_block_slot, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream),
@@ -568,7 +614,7 @@ int lbm2d_destroy(lbm2d_solver* h) {
     if (h->pair_graph) cudaGraphExecDestroy(h->pair_graph);
     ibm_release(h);
     void* bufs[] = {h->P[0], h->P[1], h->G[0], h->G[1], h->d_flags, h->d_rec_info, h->d_rec_force,
-                    h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_hist,
+                    h->d_rec_wd, h->d_rec_q, h->d_rec_uw, h->d_partials, h->d_block_slot, h->d_bpairs, h->d_hist,
                     h->d_counter, h->d_nan, h->d_seed, h->d_stage_f, h->d_stage_g, h->d_fx, h->d_fy,
                     h->d_diag, h->d_prev_uv, h->d_red_done};
     for (void* b : bufs)

@@ -126,7 +126,12 @@ struct KParams {
     // tile pipeline (lbm2d_tiles.cu): 1 / nx for the node coordinates of a
     // flat tile, and the per-tile force-slot table is block_slot
     float inv_nx;
-    int pad_tail;
+    // row pipeline: the node pairs (x even, x + 1) holding a boundary node,
+    // first node's index, ascending; CTA c rebuilds pairs [c*bchunk,
+    // (c+1)*bchunk) from device memory before its tiles, which skip them
+    int nbpairs;
+    const int* bpairs;
+    int bchunk, bpad;
 };
 static_assert(sizeof(KParams) % 16 == 0, "KParams is staged with 16-byte copies");
 
@@ -231,6 +236,9 @@ int launch_tiles_batch(int storage, bool thermal, const KParams* inst, const int
 // walking row tiles of rows_tile_width() nodes; p.block_slot has one entry
 // per CTA (first of rows_warps_per_block() per-warp force slots, or -1).
 bool rows_eligible(int storage, int nx, int ny, bool thermal);
+// whether the row pipeline of this storage rebuilds the boundary pairs in a
+// pass of their own (KParams::bpairs) rather than inline in its tiles
+bool rows_boundary_pass(int storage);
 int rows_tile_width();
 int rows_warps_per_block();
 int rows_grid(int storage, int nx, int ny, int device);  // 0 on error

@@ -137,86 +137,87 @@ struct SmemPair<__nv_bfloat16> {
     }
 };
 
-// Nodes (x, x+1) of the tile staged at `stage` (x0 its first node): the
-// reference's post-stream state (pull, bounce-back records, outflow column,
-// boundary conditions), the momentum-exchange force, the collision and the
-// stores -- the body of step_pair_block with shared-memory pulls, on
-// deviations.  The link terms of the two nodes (each 2 f, exact in FP32)
-// are summed into (fxs, fys); the caller adds that pair sum to the lane's
-// FP64 running sum.
-template <class T, int KC, int KL>
-__device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
-                                             uint32_t skey, float& fxs, float& fys) {
-    using C = RowsCfg<T>;
-    const uint2 fl = *reinterpret_cast<const uint2*>(stage + C::FLAGS_OFF + (x - x0) * 4);
-    const int e0 = (x - x0) + C::PAD;
-    float da[9], db[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        const T* r = reinterpret_cast<const T*>(stage + j * C::ROW_BYTES);
-        if (CXf(j) == 0)
-            SmemPair<T>::aligned(r, e0, da[j], db[j]);
-        else
-            SmemPair<T>::any(r, e0 - CXf(j), da[j], db[j]);
-    }
+// Nodes (x, x+1) from their pulled values da, db (storage units, deviation
+// * kS): the reference's post-stream state (bounce-back records, outflow
+// column, boundary conditions), the momentum-exchange force, the collision
+// and the stores -- the body of step_pair_block on deviations.  BND: the
+// pair holds a boundary node and is rebuilt in full, reading device memory;
+// otherwise its only special lanes are solid ones (f = 0).  The link terms of
+// the two nodes (each 2 f, exact in FP32) are summed into (fxs, fys); the
+// caller adds that pair sum to the lane's FP64 running sum.
+template <class T, int KC, int KL, bool BND>
+__device__ __forceinline__ void pair_body(const KParams& p, uint2 fl, int x, int y, float da[9], float db[9],
+                                          uint32_t skey, float& fxs, float& fys) {
     const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
-    const bool sa = special_node<false>(p, x, y, fl.x), sb = special_node<false>(p, x + 1, y, fl.y);
-    if (sa || sb) {
-        // full populations for the special node(s)
-        const T* __restrict__ Pf = static_cast<const T*>(p.fin);
-        constexpr float S = Pop<T>::kS, iS = Pop<T>::kInvS;
-        float fa[9], fb[9];
+    if constexpr (BND) {
+        const bool sa = special_node<false>(p, x, y, fl.x), sb = special_node<false>(p, x + 1, y, fl.y);
+        if (sa || sb) {
+            // full populations for the special node(s)
+            const T* __restrict__ Pf = static_cast<const T*>(p.fin);
+            constexpr float S = Pop<T>::kS, iS = Pop<T>::kInvS;
+            float fa[9], fb[9];
 #pragma unroll
-        for (int j = 0; j < 9; ++j) {
-            fa[j] = fmaf(da[j], iS, p.shf[j]);
-            fb[j] = fmaf(db[j], iS, p.shf[j]);
+            for (int j = 0; j < 9; ++j) {
+                fa[j] = fmaf(da[j], iS, p.shf[j]);
+                fb[j] = fmaf(db[j], iS, p.shf[j]);
+            }
+            if (fl.x & FLAG_SOLID) {
+#pragma unroll
+                for (int j = 0; j < 9; ++j) fa[j] = 0.0f;
+            } else if (fl.x & FLAG_BOUNDARY) {
+                fix_f<T>(p, Pf, x, y, fl.x >> 2, fa);
+            }
+            // zero-gradient outlet: column NX-1 takes NX-2's post-stream state
+            // (src/lbm.hpp:63-73); x + 1 == nx - 1 means x == nx - 2
+            if ((p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x + 1 == p.nx - 1) {
+#pragma unroll
+                for (int j = 0; j < 9; ++j) fb[j] = fa[j];
+            } else if (fl.y & FLAG_SOLID) {
+#pragma unroll
+                for (int j = 0; j < 9; ++j) fb[j] = 0.0f;
+            } else if (fl.y & FLAG_BOUNDARY) {
+                fix_f<T>(p, Pf, x + 1, y, fl.y >> 2, fb);
+            }
+            apply_bc<float>(p, x, y, fl.x, fa);
+            apply_bc<float>(p, x + 1, y, fl.y, fb);
+            if ((fl.x | fl.y) & FLAG_BOUNDARY) {
+                // momentum exchange of the nodes' links (src/lbm.hpp:565-577),
+                // accumulated in FP64 (each term 2 f exact in FP64)
+                const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
+                const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
+                // node x's links, then node x+1's (the order every pair kernel uses)
+#pragma unroll
+                for (int j = 1; j < 9; ++j)
+                    if (ma & (1u << j)) {
+                        fxs -= float(CXf(j)) * 2.0f * fa[j];
+                        fys -= float(CYf(j)) * 2.0f * fa[j];
+                    }
+#pragma unroll
+                for (int j = 1; j < 9; ++j)
+                    if (mb & (1u << j)) {
+                        fxs -= float(CXf(j)) * 2.0f * fb[j];
+                        fys -= float(CYf(j)) * 2.0f * fb[j];
+                    }
+            }
+            // back to deviations; a regular neighbour keeps its exact deviations
+            if (sa) {
+#pragma unroll
+                for (int j = 0; j < 9; ++j) da[j] = (fa[j] - p.shf[j]) * S;
+            }
+            if (sb) {
+#pragma unroll
+                for (int j = 0; j < 9; ++j) db[j] = (fb[j] - p.shf[j]) * S;
+            }
         }
-        if (fl.x & FLAG_SOLID) {
+    } else {
+        constexpr float S = Pop<T>::kS;
+        if (!oka) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) fa[j] = 0.0f;
-        } else if (fl.x & FLAG_BOUNDARY) {
-            fix_f<T>(p, Pf, x, y, fl.x >> 2, fa);
+            for (int j = 0; j < 9; ++j) da[j] = -p.shf[j] * S;
         }
-        // zero-gradient outlet: column NX-1 takes NX-2's post-stream state
-        // (src/lbm.hpp:63-73); x + 1 == nx - 1 means x == nx - 2
-        if ((p.bc_kind == BC_INFLOW || p.bc_kind == BC_STEP) && x + 1 == p.nx - 1) {
+        if (!okb) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) fb[j] = fa[j];
-        } else if (fl.y & FLAG_SOLID) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) fb[j] = 0.0f;
-        } else if (fl.y & FLAG_BOUNDARY) {
-            fix_f<T>(p, Pf, x + 1, y, fl.y >> 2, fb);
-        }
-        apply_bc<float>(p, x, y, fl.x, fa);
-        apply_bc<float>(p, x + 1, y, fl.y, fb);
-        if ((fl.x | fl.y) & FLAG_BOUNDARY) {
-            // momentum exchange of the nodes' links (src/lbm.hpp:565-577),
-            // accumulated in FP64 (each term 2 f exact in FP64)
-            const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
-            const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
-            // node x's links, then node x+1's (the order every pair kernel uses)
-#pragma unroll
-            for (int j = 1; j < 9; ++j)
-                if (ma & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * fa[j];
-                    fys -= float(CYf(j)) * 2.0f * fa[j];
-                }
-#pragma unroll
-            for (int j = 1; j < 9; ++j)
-                if (mb & (1u << j)) {
-                    fxs -= float(CXf(j)) * 2.0f * fb[j];
-                    fys -= float(CYf(j)) * 2.0f * fb[j];
-                }
-        }
-        // back to deviations; a regular neighbour keeps its exact deviations
-        if (sa) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) da[j] = (fa[j] - p.shf[j]) * S;
-        }
-        if (sb) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) db[j] = (fb[j] - p.shf[j]) * S;
+            for (int j = 0; j < 9; ++j) db[j] = -p.shf[j] * S;
         }
     }
     if (oka || okb) {
@@ -241,6 +242,62 @@ __device__ __forceinline__ void consume_pair(const KParams& p, const unsigned ch
         if constexpr (Pop<T>::kRounds) rand9(skey + (uint32_t)n0, rb);
 #pragma unroll
         for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, da[j], db[j], rb[j]);
+    }
+}
+
+// The 16-bit forms, bound by their instructions, leave the pairs that hold a
+// boundary node to a boundary pass at the start of each CTA (boundary_pairs):
+// inline, a warp with one boundary node runs the rebuild with all its lanes
+// waiting (4096^2 LES channel, FP16: 112.0 against 107.5 GLUPS).  FP32,
+// bound by HBM, keeps them inline: there the pass delays the CTA's first
+// tiles, which the ring cannot absorb (75.7 against 77.0 GLUPS).
+template <class T>
+constexpr bool kBoundaryPass = sizeof(T) == 2;
+
+// Nodes (x, x+1) of the tile staged at `stage` (x0 its first node), pulled
+// from shared memory.  A settled solid pair needs no store.
+template <class T, int KC, int KL>
+__device__ __forceinline__ void consume_pair(const KParams& p, const unsigned char* stage, int x0, int x, int y,
+                                             uint32_t skey, float& fxs, float& fys) {
+    using C = RowsCfg<T>;
+    const uint2 fl = *reinterpret_cast<const uint2*>(stage + C::FLAGS_OFF + (x - x0) * 4);
+    if (kBoundaryPass<T> && ((fl.x | fl.y) & FLAG_BOUNDARY)) return;
+    if ((fl.x & fl.y & FLAG_SOLID) && p.skip_settled_solids && y < p.ny - 1 && x > 0 && x + 1 < p.nx - 1) return;
+    const int e0 = (x - x0) + C::PAD;
+    float da[9], db[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const T* r = reinterpret_cast<const T*>(stage + j * C::ROW_BYTES);
+        if (CXf(j) == 0)
+            SmemPair<T>::aligned(r, e0, da[j], db[j]);
+        else
+            SmemPair<T>::any(r, e0 - CXf(j), da[j], db[j]);
+    }
+    pair_body<T, KC, KL, !kBoundaryPass<T>>(p, fl, x, y, da, db, skey, fxs, fys);
+}
+
+// The boundary pass: this CTA's chunk of the boundary pairs, one pair per
+// consumer lane, pulled from device memory (the previous step's stored
+// populations, which no tile of this launch writes) and rebuilt in full.
+// Run before the CTA's first tile, so its device-memory latency overlaps
+// the producer's filling of the ring.
+template <class T, int KC, int KL>
+__device__ __forceinline__ void boundary_pairs(const KParams& p, uint32_t skey, double2* acc) {
+    const int b0 = (int)blockIdx.x * p.bchunk, b1 = min(b0 + p.bchunk, p.nbpairs);
+    const T* __restrict__ P = static_cast<const T*>(p.fin);
+    for (int i = b0 + (int)threadIdx.x; i < b1; i += 32 * kConsumerWarps) {
+        const int n0 = p.bpairs[i];
+        const int y = (int)((unsigned)n0 / (unsigned)p.nx), x = n0 - y * p.nx;
+        const uint2 fl = make_uint2(p.flags[n0], p.flags[n0 + 1]);
+        float da[9], db[9];
+        pull_raw<T>(p, P, x, y, da);
+        pull_raw<T>(p, P, x + 1, y, db);
+        float fxs = 0.0f, fys = 0.0f;
+        pair_body<T, KC, KL, true>(p, fl, x, y, da, db, skey, fxs, fys);
+        if (fxs != 0.0f || fys != 0.0f) {
+            acc[threadIdx.x].x += double(fxs);
+            acc[threadIdx.x].y += double(fys);
+        }
     }
 }
 
@@ -306,6 +363,8 @@ __global__ void __launch_bounds__(kThreads, RowsCfg<T>::MIN_BLOCKS) step_rows_ke
         skey = seed_key(s);
         pass_seed(p, s, blockIdx.x == 0 && threadIdx.x == 0);
     }
+    if constexpr (kBoundaryPass<T>)
+        if (p.nbpairs > 0) boundary_pairs<T, KC, KL>(p, skey, acc);
     const bool force = p.block_slot != nullptr;
     const long long wait_limit = p.consumer_wait != 0 ? (p.consumer_wait > 0 ? p.consumer_wait : -p.consumer_wait)
                                                       : kWaitCycles;
@@ -432,6 +491,8 @@ int launch_rows_t(const KParams& p, int grid, cudaStream_t s) {
 
 // Every staged row must start on a 16-byte boundary: nx a multiple of 4
 // (FP32) or 8 (FP16/BF16).
+bool rows_boundary_pass(int storage) { return storage == ST_FP16 || storage == ST_BF16; }
+
 bool rows_eligible(int storage, int nx, int ny, bool thermal) {
     const int q = storage == ST_FP32 ? 4 : 8;
     return !thermal && (storage == ST_FP32 || storage == ST_FP16 || storage == ST_BF16) && nx % q == 0 && nx >= 16 &&

@@ -72,6 +72,8 @@ struct lbm2d_solver {
     double* d_rec_uw = nullptr;
     double* d_partials = nullptr;
     int* d_block_slot = nullptr;
+    int* d_bpairs = nullptr;  // row pipeline: boundary pairs (KParams::bpairs)
+    int nbpairs = 0, bchunk = 0;
     unsigned int* d_red_done = nullptr;  // arrivals of the fused force reduction
     int red_blocks = 0;                  // blocks (CTAs) that hold force slots
     int nslots = 0, slot_bx = 0, slot_by = 0, slot_kind = -1, slot_grid = 0;
