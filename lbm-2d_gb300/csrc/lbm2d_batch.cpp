@@ -199,7 +199,7 @@ int prepare(lbm2d_batch* b) {
         KParams* p0 = b->h_params + off;
         KParams* p1 = p0 + m;
         int* left = b->h_left + off;
-        std::vector<int> start(m + 1, 0);
+        std::vector<int> start(m + 1, 0), reg(m, 0);
         std::vector<ReduceJob> jobs[2];
         for (size_t k = 0; k < m; ++k) {
             Member& mem = b->members[g.members[k]];
@@ -236,7 +236,11 @@ int prepare(lbm2d_batch* b) {
                 BCK(cudaStreamWaitEvent(b->stream, b->ev, 0), "wait");
             }
             const int gy = (h->ny + b->by - 1) / b->by;
-            start[k + 1] = start[k] + (p.gx * gy + kBatchTiles - 1) / kBatchTiles;
+            // tile blocks, then the member's boundary blocks (nbpairs set only
+            // when its slots are laid out for them)
+            const int nbb = p.nbpairs > 0 ? (p.nbpairs + p.bchunk - 1) / p.bchunk : 0;
+            reg[k] = (p.gx * gy + kBatchTiles - 1) / kBatchTiles;
+            start[k + 1] = start[k] + reg[k] + nbb;
             if (h->nslots > 0) {
                 jobs[0].push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last,
                                    budgeted ? g.d_left + k : nullptr});
@@ -259,8 +263,12 @@ int prepare(lbm2d_batch* b) {
         BCK(cudaMemcpyAsync(g.d_left, left, m * sizeof(int), cudaMemcpyHostToDevice, b->stream), "budgets");
         // the block map (rebuilt only when the member sizes or the shape change)
         std::vector<int2> map((size_t)g.nblocks);
+        // (member, tile block index), or (member, -(i + 1)) for boundary block i
         for (size_t k = 0; k < m; ++k)
-            for (int q = start[k]; q < start[k + 1]; ++q) map[(size_t)q] = make_int2((int)k, q - start[k]);
+            for (int q = start[k]; q < start[k + 1]; ++q) {
+                const int local = q - start[k];
+                map[(size_t)q] = make_int2((int)k, local < reg[k] ? local : -(local - reg[k] + 1));
+            }
         if (map.size() != g.h_block_map.size() ||
             !std::equal(map.begin(), map.end(), g.h_block_map.begin(),
                         [](const int2& a, const int2& c) { return a.x == c.x && a.y == c.y; })) {

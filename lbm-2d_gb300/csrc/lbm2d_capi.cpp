@@ -124,7 +124,7 @@ KParams base_params(const lbm2d_solver* h) {
     p.nan_flag = h->d_nan;
     p.consumer_wait = h->consumer_wait;
     p.inv_nx = 1.0f / float(h->nx);
-    if (h->slot_kind == KERNEL_ROWS) {
+    if (h->slot_kind == KERNEL_ROWS || h->slot_bpass) {
         p.bpairs = h->d_bpairs;
         p.nbpairs = h->nbpairs;
         p.bchunk = h->bchunk;
@@ -285,8 +285,21 @@ int kernel_kind(const lbm2d_solver* h) {
 // kernels: one table entry per launch block (blocks without a force node get
 // -1).  Row pipeline: one entry per persistent CTA, marking the CTAs whose
 // tiles (tile t goes to CTA t mod grid) hold a force node.
+// The node pairs (x even, x + 1) that hold a boundary node (every boundary
+// node has a record), first node's index, ascending.
+void boundary_pair_list(const lbm2d_solver* h, std::vector<int>& out) {
+    out.clear();
+    out.reserve(h->geo.rec_node.size());
+    for (int32_t id : h->geo.rec_node) out.push_back(id - (id % h->nx) % 2);
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
 int ensure_slots(lbm2d_solver* h) {
     const int kind = kernel_kind(h);
+    // a batch member on the paired kernel: its boundary pairs run in boundary
+    // blocks appended after its tile blocks
+    const bool bpass = kind == KERNEL_PAIR && h->in_batch && !h->thermal;
     int grid = 0;
     const long long ntiles = ((long long)h->N + tiles_width() - 1) / tiles_width();
     if (kind == KERNEL_ROWS) {
@@ -297,7 +310,7 @@ int ensure_slots(lbm2d_solver* h) {
         if (grid <= 0) return fail(h, LBM2D_ERR_CUDA, "tile pipeline: no launch configuration");
     }
     const bool persistent = kind == KERNEL_ROWS || kind == KERNEL_TILES;
-    if (h->slot_kind == kind && h->d_block_slot &&
+    if (h->slot_kind == kind && h->d_block_slot && h->slot_bpass == bpass &&
         (persistent ? h->slot_grid == grid : (h->slot_bx == h->bx && h->slot_by == h->by)))
         return LBM2D_OK;
     std::vector<int> slots, bpairs;
@@ -329,10 +342,7 @@ int ensure_slots(lbm2d_solver* h) {
         // force nodes are boundary nodes, so a CTA holds force slots when
         // its chunk has a pair with a force record.
         const int warps = rows_warps_per_block();
-        bpairs.reserve(h->geo.rec_node.size());
-        for (int32_t id : h->geo.rec_node) bpairs.push_back(id - (id % h->nx) % 2);
-        std::sort(bpairs.begin(), bpairs.end());
-        bpairs.erase(std::unique(bpairs.begin(), bpairs.end()), bpairs.end());
+        boundary_pair_list(h, bpairs);
         bchunk = bpairs.empty() ? 0 : (int)((bpairs.size() + (size_t)grid - 1) / (size_t)grid);
         slots.assign((size_t)grid, -1);
         for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
@@ -359,6 +369,30 @@ int ensure_slots(lbm2d_solver* h) {
             const int id = h->geo.rec_node[r];
             const long long t = (long long)(id / h->nx) * tpr + (id % h->nx) / tw;
             slots[(size_t)(t % grid)] = 0;
+        }
+        int k = 0;
+        for (auto& s : slots)
+            if (s == 0) {
+                s = k;
+                k += warps;
+            }
+        h->nslots = k;
+    } else if (bpass) {
+        // tile blocks own no slots; boundary block i (pairs [i*B, (i+1)*B),
+        // B = bx*by, one per thread) owns one per warp when it holds a force
+        // pair, at block_slot[ntiles + i]
+        const int B = h->bx * h->by, warps = (B + 31) / 32;
+        const size_t gx = (size_t)((h->nx + 2 * h->bx - 1) / (2 * h->bx)), gy = (size_t)((h->ny + h->by - 1) / h->by);
+        boundary_pair_list(h, bpairs);
+        bchunk = B;
+        const size_t ntl = gx * gy, nbb = (bpairs.size() + (size_t)B - 1) / (size_t)B;
+        slots.assign(ntl + nbb, -1);
+        for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
+            if (!h->geo.rec_force[r]) continue;
+            const int id = h->geo.rec_node[r];
+            const size_t i = (size_t)(std::lower_bound(bpairs.begin(), bpairs.end(), id - (id % h->nx) % 2) -
+                                      bpairs.begin());
+            slots[ntl + i / (size_t)B] = 0;
         }
         int k = 0;
         for (auto& s : slots)
@@ -402,6 +436,7 @@ int ensure_slots(lbm2d_solver* h) {
     h->slot_by = h->by;
     h->slot_kind = kind;
     h->slot_grid = grid;
+    h->slot_bpass = bpass;
     return LBM2D_OK;
 }
 

@@ -74,6 +74,7 @@ struct lbm2d_solver {
     int* d_block_slot = nullptr;
     int* d_bpairs = nullptr;  // row pipeline: boundary pairs (KParams::bpairs)
     int nbpairs = 0, bchunk = 0;
+    bool slot_bpass = false;  // slots laid out for a batch member's boundary blocks
     unsigned int* d_red_done = nullptr;  // arrivals of the fused force reduction
     int red_blocks = 0;                  // blocks (CTAs) that hold force slots
     int nslots = 0, slot_bx = 0, slot_by = 0, slot_kind = -1, slot_grid = 0;
