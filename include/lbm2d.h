@@ -368,6 +368,16 @@ typedef struct lbm2d_server_stats_t {
 
 typedef struct lbm2d_server lbm2d_server;
 int lbm2d_server_create(int device, double budget_bytes, int max_active, int steps_per_tick, lbm2d_server **out);
+/* flags of lbm2d_server_create_ex.  LBM2D_SERVE_RESIDENT: the solves are
+ * stepped by a device-resident loop (a CUDA graph WHILE loop over a device
+ * table of solves): a solve joins at the next step boundary after it is set
+ * up and retires at its budget with no host round trip between steps;
+ * steps_per_tick bounds the iterations of one launch of the loop (it
+ * relaunches while solves are active).  max_active <= 1024.  Without it:
+ * ticks of steps_per_tick batched steps (lbm2d_server_create). */
+#define LBM2D_SERVE_RESIDENT 1
+int lbm2d_server_create_ex(int device, double budget_bytes, int max_active, int steps_per_tick, int flags,
+                           lbm2d_server **out);
 int lbm2d_server_submit(lbm2d_server *s, const lbm2d_request *r, long long *id);
 /* lbm2d_server_submit with caller state: f_init (may be NULL) is the
  * request's initial population field, FP64 AoS [nx*ny*9], copied before the

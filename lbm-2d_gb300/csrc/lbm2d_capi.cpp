@@ -274,7 +274,8 @@ int kernel_kind(const lbm2d_solver* h) {
     const bool tiles_ok = h->storage != ST_FP64;
     if (h->variant == 3 && tiles_ok) return KERNEL_TILES;
     if (h->variant == 0 && tiles_ok) {
-        if (rows_eligible(h->storage, h->nx, h->ny, h->thermal) && (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
+        if (rows_eligible(h->storage, h->nx, h->ny, h->thermal) && !h->resident &&
+            (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
             return KERNEL_ROWS;
     }
     if (!use_pair(h)) return KERNEL_SCALAR;

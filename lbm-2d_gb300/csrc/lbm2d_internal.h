@@ -211,6 +211,44 @@ constexpr int kBatchTiles = 4;
 int launch_batch_step(int storage, const KParams* inst, const int2* block_map, int nblocks, int thermal, int bx,
                       int by, void* stream, int pair);
 int launch_batch_force_reduce(const ReduceJob* jobs, int njobs, void* stream);
+
+// Resident serving loop (lbm2d_resident.cu): a CUDA graph whose WHILE node
+// steps every member of a device table once per iteration, with a scheduler
+// kernel that admits and retires members at every step boundary through a
+// mailbox in mapped host memory.  A member's kind ("combo") is its storage
+// and kernel: combo = 3 * storage + {0 paired, 1 one node, 2 one node thermal}.
+constexpr int kResCombos = 12;
+constexpr int kResMaxSlots = 1024;  // one scheduler thread per slot
+struct ResEntry {
+    KParams p[2];      // the member's step parameters at parity 0 and 1 (p[1]: buffers and seeds swapped)
+    ReduceJob job;     // its per-step force reduction (job.nslots == 0: none)
+    int combo;         // kernel of the member
+    int units;         // work units of one step (launch blocks of the batched kernels)
+    int left;          // step budget
+    int settle_after;  // steps after which its settled solids are no longer stored (-1: never)
+};
+// Host <-> device words, in mapped pinned memory.  join[k]: the host writes 1
+// once entry k is in the table; the scheduler answers 2 when it admits it.
+// done[k]: the scheduler writes the steps taken + 1 when member k retires
+// (its last step and force reduction complete); the host clears it when it
+// reuses the slot.  stop: the host asks the loop to end at the next step
+// boundary.
+struct ResMailbox {
+    int join[kResMaxSlots];
+    long long done[kResMaxSlots];
+    int stop;
+    int pad;
+    long long iterations;  // iterations of all launches so far (device)
+};
+struct ResLoop;
+int res_create(int device, int cap, int bx, int by, ResLoop** out);
+void res_destroy(ResLoop* r);
+ResEntry* res_table(ResLoop* r);          // device array of cap entries
+volatile ResMailbox* res_mailbox(ResLoop* r);  // host view
+// Launch the loop on stream s (graph rebuilt first when the set of combos in
+// use changed); it ends by itself when no member is active, after
+// max_iters iterations, or at the host's stop word.
+int res_launch(ResLoop* r, unsigned combo_mask, int max_iters, void* stream);
 // acc[0..4] += mass, x/y momentum, sum |u - u_prev|^2, sum |u|^2 (FP64).
 int launch_diagnostics(int storage, const KParams& p, double* acc, float* prev_uv, int have_prev, void* stream);
 int launch_fill_equilibrium(double* fa, double* ga, long long N, double rho, double u, double v, double T,

@@ -26,176 +26,6 @@
 namespace lbm2d {
 namespace {
 
-// One step of the node pair (x0, x0 + 1), x0 even (FP32/FP16/BF16 storage;
-// TH: with the thermal double distribution, collided by thermal_pair_dev):
-// pull with the rebuild of special nodes, momentum exchange (the pair's
-// link terms summed in FP32, node x0 then x0 + 1, returned in fxs/fys),
-// collision and stores.  PLAIN: the pair holds no boundary node (those are
-// stepped by a boundary block), so a solid lane (f = 0) is its only special
-// case and the pulls need no rebuild.
-template <class T, bool TH, bool PLAIN>
-__device__ __forceinline__ void pair_step(const KParams& p, int x0, int y, uint32_t skey, uint2 fl, double& fxs,
-                                          double& fys) {
-    const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
-    constexpr float iS = Pop<T>::kInvS;
-    float fa[9], fb[9];  // deviations in storage units
-    float ea[TH ? 9 : 1], eb[TH ? 9 : 1];  // thermal deviations (TH)
-    const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
-    if constexpr (PLAIN) {
-        const T* __restrict__ P = static_cast<const T*>(p.fin);
-        pull_raw<T>(p, P, x0, y, fa);
-        pull_raw<T>(p, P, x0 + 1, y, fb);
-        constexpr float S = Pop<T>::kS;
-        if (!oka) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) fa[j] = -p.shf[j] * S;
-        }
-        if (!okb) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) fb[j] = -p.shf[j] * S;
-        }
-    } else if constexpr (TH) {
-        build_dev_s_th<T>(p, x0, y, fl.x, fa, ea);
-        build_dev_s_th<T>(p, x0 + 1, y, fl.y, fb, eb);
-    } else {
-        build_dev_s<T>(p, x0, y, fl.x, fa);
-        build_dev_s<T>(p, x0 + 1, y, fl.y, fb);
-    }
-    if (!PLAIN && ((fl.x | fl.y) & FLAG_BOUNDARY)) {
-        // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
-        const uint32_t ma = (oka && (fl.x & FLAG_BOUNDARY)) ? p.rec_force[fl.x >> 2] : 0u;
-        const uint32_t mb = (okb && (fl.y & FLAG_BOUNDARY)) ? p.rec_force[fl.y >> 2] : 0u;
-        // the pair's link terms in FP32, node x0 then x0 + 1
-        float fxp = 0.0f, fyp = 0.0f;
-#pragma unroll
-        for (int j = 1; j < 9; ++j)
-            if (ma & (1u << j)) {
-                const float f = fmaf(fa[j], iS, p.shf[j]);
-                fxp -= float(CXf(j)) * 2.0f * f;
-                fyp -= float(CYf(j)) * 2.0f * f;
-            }
-#pragma unroll
-        for (int j = 1; j < 9; ++j)
-            if (mb & (1u << j)) {
-                const float f = fmaf(fb[j], iS, p.shf[j]);
-                fxp -= float(CXf(j)) * 2.0f * f;
-                fyp -= float(CYf(j)) * 2.0f * f;
-            }
-        fxs = double(fxp);
-        fys = double(fyp);
-    }
-    if (oka || okb) {
-        F2 f[9];
-#pragma unroll
-        for (int j = 0; j < 9; ++j) f[j] = mk2(fa[j], fb[j]);
-        collide_pair_dev<T>(p, fl.x, fl.y, oka, okb, f);
-        if constexpr (TH) {
-            F2 g[9];
-#pragma unroll
-            for (int j = 0; j < 9; ++j) g[j] = mk2(ea[j], eb[j]);
-            thermal_pair_dev<T>(p, oka, okb, f, g);
-#pragma unroll
-            for (int j = 0; j < 9; ++j) {
-                ea[j] = g[j].v.x;
-                eb[j] = g[j].v.y;
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 9; ++j) {
-            fa[j] = f[j].v.x;
-            fb[j] = f[j].v.y;
-        }
-    }
-    // a solid node's state never changes once settled (the heated
-    // cavity's Dirichlet passes rewrite node states every step)
-    const bool settled = p.skip_settled_solids && y < p.ny - 1;
-    const bool skip_a = !oka && settled && x0 > 0;
-    const bool skip_b = !okb && settled && x0 + 1 < p.nx - 1;
-    if (!(skip_a && skip_b)) {
-        T* __restrict__ Fo = static_cast<T*>(p.fout);
-        const size_t N = (size_t)p.N;
-        uint32_t rb[9] = {};
-        if constexpr (Pop<T>::kRounds) rand9(skey + n0, rb);
-#pragma unroll
-        for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
-        if constexpr (TH) {
-            T* __restrict__ Go = static_cast<T*>(p.gout);
-            if constexpr (Pop<T>::kRounds) rand9((skey + n0) ^ 0x6A09E667u, rb);
-#pragma unroll
-            for (int j = 0; j < 9; ++j) PairStore<T>::st(Go + j * N, n0, ea[j], eb[j], rb[j]);
-        }
-    }
-}
-
-// The block's per-warp force partials: FP64 warp sums into the slots that
-// block_slot[idx] opens (none when -1), then the fused second stage.
-__device__ __forceinline__ void pair_block_slots(const KParams& p, int idx, double fxs, double fys) {
-    if (p.block_slot) {
-        const int base = p.block_slot[idx];
-        if (base >= 0) {
-            double a = fxs, b = fys;  // FP64 warp sum
-            if (__any_sync(0xffffffffu, a != 0.0 || b != 0.0)) {
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    a += __shfl_down_sync(0xffffffffu, a, o);
-                    b += __shfl_down_sync(0xffffffffu, b, o);
-                }
-            }
-            const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-            if ((tid & 31) == 0) {
-                const int slot = base + (tid >> 5);
-                p.partials[2 * slot] = a;
-                p.partials[2 * slot + 1] = b;
-            }
-            if (p.red_done) fused_force_finish(p, tid, [] { __syncthreads(); });
-        }
-    }
-}
-
-__device__ __forceinline__ uint32_t pair_seed_key(const KParams& p, bool first) {
-    const uint32_t s = seed_of(p);
-    pass_seed(p, s, first);
-    return seed_key(s);
-}
-
-// One step of the paired block (bxi, byi) of an instance whose paired block
-// grid is gx wide.  PLAIN: the instance's boundary pairs are stepped by its
-// boundary blocks (pair_boundary_block); this block skips them.
-template <class T, bool TH = false, bool PLAIN = false>
-__device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int byi, int gx) {
-    const int x0 = 2 * (bxi * blockDim.x + threadIdx.x);
-    const int y = byi * blockDim.y + threadIdx.y;
-    uint32_t skey = 0;
-    if constexpr (Pop<T>::kRounds)
-        skey = pair_seed_key(p, bxi == 0 && byi == 0 && threadIdx.x == 0 && threadIdx.y == 0);
-    double fxs = 0.0, fys = 0.0;  // momentum exchange, FP64 across node pairs
-    if (x0 < p.nx && y < p.ny) {
-        const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
-        const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
-        if (!PLAIN || !((fl.x | fl.y) & FLAG_BOUNDARY)) pair_step<T, TH, PLAIN>(p, x0, y, skey, fl, fxs, fys);
-    }
-    if (!PLAIN) pair_block_slots(p, byi * gx + bxi, fxs, fys);
-}
-
-// Boundary block i of an instance: its boundary pairs [i*B, (i+1)*B), B the
-// block's threads, one pair per thread (bpairs, ascending); the force slots
-// of boundary block i are block_slot[ntiles + i], ntiles = gx * gy.
-template <class T>
-__device__ __forceinline__ void pair_boundary_block(const KParams& p, int i, int ntiles) {
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int j = i * (int)(blockDim.x * blockDim.y) + tid;
-    uint32_t skey = 0;
-    if constexpr (Pop<T>::kRounds) skey = pair_seed_key(p, false);
-    double fxs = 0.0, fys = 0.0;
-    if (j < p.nbpairs) {
-        const int n0 = p.bpairs[j];
-        const int y = (int)((unsigned)n0 / (unsigned)p.nx), x0 = n0 - y * p.nx;
-        const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
-        pair_step<T, false, false>(p, x0, y, skey, fl, fxs, fys);
-    }
-    pair_block_slots(p, ntiles + i, fxs, fys);
-}
-
 template <class T, bool TH>
 __global__ void __launch_bounds__(512) step_pair_kernel(const KParams p) {
     step_pair_block<T, TH>(p, blockIdx.x, blockIdx.y, gridDim.x);
@@ -290,12 +120,11 @@ __global__ void __launch_bounds__(512, 2) batch_step_pair_kernel(const KParams* 
         pair_boundary_block<T>(sp, -(local + 1), tiles);
         return;
     }
-    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t) {
-        if (sp.nbpairs > 0)
-            step_pair_block<T, false, true>(sp, t % sp.gx, t / sp.gx, sp.gx);
-        else
-            step_pair_block<T>(sp, t % sp.gx, t / sp.gx, sp.gx);
-    }
+    // a member's boundary pairs are all in its boundary blocks (a batch
+    // member on this kernel always has its slots laid out for them; none
+    // when it has no boundary node)
+    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+        step_pair_block<T, false, true>(sp, t % sp.gx, t / sp.gx, sp.gx);
 }
 
 // The thermal form: twice the populations, so no register cap.

@@ -109,6 +109,7 @@ struct lbm2d_solver {
     // 1: one node per thread, 2: paired nodes, 3: the tile pipeline
     int variant = 0;
     bool in_batch = false;  // a batch member is stepped by the batched kernels
+    bool resident = false;  // a member of the resident serving loop (never the row pipeline)
     bool profiling = false;
     long long consumer_wait = 0;  // row pipeline's consumer wait limit in cycles (0: default)
     // immersed boundary (lbm2d_set_ibm); ibm_np == 0: none.  F and the

@@ -17,8 +17,20 @@
 //     stops exactly at its budget without shortening the tick;
 //   * it then retires finished solves (non-finite check, drag/lift read back,
 //     memory freed) and records arrival, admission and completion times.
+//
+// Resident mode (LBM2D_SERVE_RESIDENT) replaces the ticks with the device
+// loop of lbm2d_resident.cu: the set-up threads also prepare each solve's
+// table entry (its step parameters, work units and force reduction); the
+// stepping thread copies it into a free slot of the device table and raises
+// the slot's join word in mapped memory, and the loop admits the solve at its
+// next step boundary, steps it with the others and retires it at its budget
+// by writing the steps it took to the slot's done word, which the stepping
+// thread polls.  The loop relaunches itself only when it ends (no active
+// solve, a new kind of solve, or a bounded number of iterations).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <cstring>
 #include <cmath>
 #include <condition_variable>
 #include <deque>
@@ -63,6 +75,7 @@ struct Active {
     size_t footprint = 0;
     double tau = 0.0, u_bc = 0.0;
     StateIO io;
+    std::shared_ptr<ResEntry> entry;  // resident mode: the solve's table entry
 };
 
 size_t footprint_bytes(const lbm2d_request& r) {
@@ -77,6 +90,7 @@ size_t footprint_bytes(const lbm2d_request& r) {
 
 struct lbm2d_server {
     int device = 0;
+    bool resident = false;
     size_t budget = 0;
     int max_active = 0;
     int steps_per_tick = 0;
@@ -102,12 +116,60 @@ struct lbm2d_server {
     long long ticks = 0, member_ticks = 0;
     double gpu_s = 0.0;  // device time of the ticks (CUDA events on the batch stream)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // resident mode (stepping thread): the device loop, its streams, the
+    // solve in each table slot and the slot's state (0 free, 1 entry written,
+    // join not yet raised, 2 joined), the combos in use
+    ResLoop* loop = nullptr;
+    cudaStream_t loop_stream = nullptr, copy_stream = nullptr;
+    ResEntry* h_entry = nullptr;  // pinned staging of one entry
+    std::vector<Active> slot;
+    std::vector<int> slot_state;
+    unsigned mask_used = 0, mask_running = 0;
+    bool running = false;
     // stepping-thread time split: step call (prepare + enqueue), wait for the
     // device, retirement, joining ready solves
     double call_s = 0.0, wait_s = 0.0, retire_s = 0.0, join_s = 0.0;
 };
 
 namespace {
+
+// Resident mode: the solve's step parameters at both parities (the batched
+// kernels' launch shape, 32x4), its kind, work units, force reduction and
+// budget, as lbm2d_batch_step would launch it.
+int prepare_entry(Active& a) {
+    lbm2d_solver* h = a.h;
+    h->bx = 32;
+    h->by = 4;
+    h->in_batch = true;
+    h->resident = true;
+    KParams p;
+    int rc = rt::prepare_steps(h, a.tau, a.u_bc, p);
+    if (rc) return rc;
+    if (h->thermal && p.pair) return LBM2D_ERR_INVALID;  // the loop has no paired thermal kernel
+    auto e = std::make_shared<ResEntry>();
+    std::memset(e.get(), 0, sizeof(ResEntry));
+    const int kind = h->thermal ? 2 : (p.pair ? 0 : 1);
+    e->combo = 3 * h->storage + kind;
+    const int gy = (h->ny + h->by - 1) / h->by;
+    long long units = ((long long)p.gx * gy + kBatchTiles - 1) / kBatchTiles;
+    if (kind == 0 && p.nbpairs > 0) units += (p.nbpairs + p.bchunk - 1) / p.bchunk;
+    e->units = (int)units;
+    e->p[0] = p;
+    e->p[1] = p;
+    e->p[1].fin = p.fout;
+    e->p[1].fout = const_cast<void*>(p.fin);
+    e->p[1].gin = p.gout;
+    e->p[1].gout = const_cast<void*>(p.gin);
+    e->p[1].seed_in = p.seed_out;
+    e->p[1].seed_out = const_cast<uint32_t*>(p.seed_in);
+    if (h->nslots > 0) e->job = {h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last, nullptr};
+    e->left = (int)std::min<long long>(std::max(a.left, 0LL), 0x7FFFFFFF);
+    // settled solids are skipped from the solve's third step since its last
+    // re-collision on (never with the heated cavity's per-step passes)
+    e->settle_after = h->hook == 1 ? -1 : (int)std::max<long long>(0, 2 - h->steps_since_collide);
+    a.entry = e;
+    return LBM2D_OK;
+}
 
 // Build one solve the way the reference's drivers do.
 int setup_request(lbm2d_server* s, Active& a) {
@@ -193,9 +255,10 @@ int setup_request(lbm2d_server* s, Active& a) {
     a.io.f_init.reset();  // the copy is on the device now
     lbm2d_info info;  // builds and uploads the geometry here, off the stepping thread
     if ((rc = lbm2d_get_info(a.h, &info))) return rc;
-    if ((rc = lbm2d_synchronize(a.h))) return rc;
     a.tau = tau;
     a.u_bc = u_bc;
+    if (s->resident && (rc = prepare_entry(a))) return rc;
+    if ((rc = lbm2d_synchronize(a.h))) return rc;
     return LBM2D_OK;
 }
 
@@ -361,14 +424,165 @@ void worker_loop(lbm2d_server* s) {
     }
 }
 
+// ---------------------------------------------------------------- resident
+// Retire the solves the loop has finished (their done word holds the steps
+// they took + 1).  Returns whether any was.
+bool res_retire_done(lbm2d_server* s) {
+    volatile ResMailbox* mb = res_mailbox(s->loop);
+    bool any = false;
+    for (size_t k = 0; k < s->slot.size(); ++k) {
+        if (s->slot_state[k] != 2) continue;
+        const long long d = mb->done[k];
+        if (d == 0) continue;
+        mb->done[k] = 0;
+        mb->join[k] = 0;
+        Active a = s->slot[k];
+        s->slot[k] = Active();
+        s->slot_state[k] = 0;
+        const long long taken = d - 1;
+        rt::advance(a.h, taken);
+        if (taken > 0) a.h->u_last = a.u_bc;  // the boundary velocity the state was stepped with
+        s->lattice_updates += taken * (long long)a.req.nx * a.req.ny;
+        ++s->member_ticks;
+        const double t0 = now_s();
+        // the solve's own non-finite flag: LBM2D_ERR_NAN
+        release(s, a, taken < a.left ? LBM2D_ERR_STATE : lbm2d_synchronize(a.h));
+        s->retire_s += now_s() - t0;
+        any = true;
+    }
+    return any;
+}
+
+// Put the solves that are set up into free table slots.  A slot's join word
+// is raised now when the running loop has its kind, else at the next launch
+// (the running loop is asked to end so that it is rebuilt with it).
+bool res_join_ready(lbm2d_server* s) {
+    std::deque<Active> r;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        r.swap(s->ready);
+    }
+    if (r.empty()) return false;
+    volatile ResMailbox* mb = res_mailbox(s->loop);
+    ResEntry* table = res_table(s->loop);
+    const double t0 = now_s();
+    for (auto& a : r) {
+        size_t k = 0;
+        while (k < s->slot.size() && s->slot_state[k] != 0) ++k;
+        if (k == s->slot.size()) {  // admission keeps the live solves within the slots
+            release(s, a, LBM2D_ERR_STATE);
+            continue;
+        }
+        *s->h_entry = *a.entry;
+        a.entry.reset();
+        if (cudaMemcpyAsync(table + k, s->h_entry, sizeof(ResEntry), cudaMemcpyHostToDevice, s->copy_stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s->copy_stream) != cudaSuccess) {
+            release(s, a, LBM2D_ERR_CUDA);
+            continue;
+        }
+        const unsigned bit = 1u << s->h_entry->combo;
+        s->mask_used |= bit;
+        s->slot[k] = a;
+        mb->done[k] = 0;
+        if (s->running && (s->mask_running & bit)) {
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+            mb->join[k] = 1;
+            s->slot_state[k] = 2;
+        } else {
+            s->slot_state[k] = 1;
+            if (s->running) mb->stop = 1;
+        }
+    }
+    s->join_s += now_s() - t0;
+    return true;
+}
+
+void resident_loop(lbm2d_server* s) {
+    cudaSetDevice(s->device);
+    volatile ResMailbox* mb = res_mailbox(s->loop);
+    const int max_iters = s->steps_per_tick;
+    double t_launch = 0.0;
+    for (;;) {
+        bool did = res_retire_done(s);
+        if (s->running && cudaEventQuery(s->ev1) != cudaErrorNotReady) {
+            s->running = false;
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) s->gpu_s += 1e-3 * ms;
+            s->busy_s += now_s() - t_launch;
+            did = res_retire_done(s) || did;
+        }
+        bool stop;
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            stop = s->stop;
+        }
+        if (stop) {
+            if (s->running) {
+                mb->stop = 1;
+                cudaStreamSynchronize(s->loop_stream);
+                s->running = false;
+                res_retire_done(s);
+            }
+            return;
+        }
+        did = res_join_ready(s) || did;
+        if (!s->running) {
+            bool any = false;
+            for (int st : s->slot_state) any = any || st != 0;
+            if (any) {
+                mb->stop = 0;
+                for (size_t k = 0; k < s->slot.size(); ++k)
+                    if (s->slot_state[k] == 1) {
+                        mb->join[k] = 1;
+                        s->slot_state[k] = 2;
+                    }
+                std::atomic_thread_fence(std::memory_order_seq_cst);
+                const double t0 = now_s();
+                cudaEventRecord(s->ev0, s->loop_stream);
+                const int e = res_launch(s->loop, s->mask_used, max_iters, s->loop_stream);
+                cudaEventRecord(s->ev1, s->loop_stream);
+                s->call_s += now_s() - t0;
+                if (e) {
+                    // nothing runs: fail the solves waiting in the table
+                    for (size_t k = 0; k < s->slot.size(); ++k)
+                        if (s->slot_state[k] != 0) {
+                            Active a = s->slot[k];
+                            s->slot[k] = Active();
+                            s->slot_state[k] = 0;
+                            mb->join[k] = 0;
+                            release(s, a, LBM2D_ERR_CUDA);
+                        }
+                    continue;
+                }
+                s->mask_running = s->mask_used;
+                s->running = true;
+                t_launch = t0;
+                ++s->ticks;
+                did = true;
+            }
+        }
+        if (!did) {
+            // nothing changed: wait a little for a set-up solve or the device
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait_for(lock, std::chrono::microseconds(s->running ? 50 : 2000),
+                           [&] { return s->stop || !s->ready.empty(); });
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
 
-int lbm2d_server_create(int device, double budget_bytes, int max_active, int steps_per_tick, lbm2d_server** out) {
+int lbm2d_server_create_ex(int device, double budget_bytes, int max_active, int steps_per_tick, int flags,
+                           lbm2d_server** out) {
     if (!out || max_active < 1 || steps_per_tick < 1) return LBM2D_ERR_INVALID;
+    const bool resident = (flags & LBM2D_SERVE_RESIDENT) != 0;
+    if (resident && max_active > kResMaxSlots) return LBM2D_ERR_INVALID;
     auto* s = new lbm2d_server();
     s->device = device;
+    s->resident = resident;
     s->budget = budget_bytes > 0 ? (size_t)budget_bytes : (size_t)64 << 30;
     s->max_active = max_active;
     s->steps_per_tick = steps_per_tick;
@@ -376,18 +590,40 @@ int lbm2d_server_create(int device, double budget_bytes, int max_active, int ste
     // narrow blocks: a serving mix holds many small grids, and a block that
     // overhangs a grid's right edge idles its overhanging threads
     if (!rc) rc = lbm2d_batch_set_block(s->batch, 32, 4);
+    if (!rc && resident) {
+        if (res_create(device, max_active, 32, 4, &s->loop) != 0 ||
+            cudaStreamCreateWithFlags(&s->loop_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaMallocHost(&s->h_entry, sizeof(ResEntry)) != cudaSuccess)
+            rc = LBM2D_ERR_CUDA;
+        s->slot.assign((size_t)max_active, Active());
+        s->slot_state.assign((size_t)max_active, 0);
+    }
     if (rc) {
+        if (s->loop) res_destroy(s->loop);
+        if (s->loop_stream) cudaStreamDestroy(s->loop_stream);
+        if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+        if (s->h_entry) cudaFreeHost(s->h_entry);
+        if (s->batch) lbm2d_batch_destroy(s->batch);
         delete s;
         return rc;
     }
     cudaSetDevice(device);
     if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) s->ev0 = s->ev1 = nullptr;
-    s->worker = std::thread(worker_loop, s);
+    if (resident && !s->ev0) {
+        lbm2d_server_destroy(s);
+        return LBM2D_ERR_CUDA;
+    }
+    s->worker = std::thread(resident ? resident_loop : worker_loop, s);
     const unsigned hw = std::thread::hardware_concurrency();
     const int n_setup = (int)std::max(1u, std::min(hw > 2 ? hw - 2 : 1u, 6u));
     for (int k = 0; k < n_setup; ++k) s->setup_threads.emplace_back(setup_loop, s);
     *out = s;
     return LBM2D_OK;
+}
+
+int lbm2d_server_create(int device, double budget_bytes, int max_active, int steps_per_tick, lbm2d_server** out) {
+    return lbm2d_server_create_ex(device, budget_bytes, max_active, steps_per_tick, 0, out);
 }
 
 int lbm2d_server_submit_state(lbm2d_server* s, const lbm2d_request* r, const double* f_init, double* f_out,
@@ -465,8 +701,25 @@ int lbm2d_server_destroy(lbm2d_server* s) {
     for (auto& t : s->setup_threads)
         if (t.joinable()) t.join();
     for (size_t k = s->active.size(); k-- > 0;) retire(s, k, LBM2D_ERR_STATE);
-    join_ready(s);  // set up but never stepped
+    if (s->resident) {
+        // solves still in the table (the loop has ended), then the ready ones
+        for (size_t k = 0; k < s->slot.size(); ++k)
+            if (s->slot_state[k] != 0) {
+                Active a = s->slot[k];
+                s->slot_state[k] = 0;
+                release(s, a, LBM2D_ERR_STATE);
+            }
+        std::deque<Active> r;
+        r.swap(s->ready);
+        for (auto& a : r) release(s, a, LBM2D_ERR_STATE);
+    } else {
+        join_ready(s);  // set up but never stepped
+    }
     for (size_t k = s->active.size(); k-- > 0;) retire(s, k, LBM2D_ERR_STATE);
+    if (s->loop) res_destroy(s->loop);
+    if (s->loop_stream) cudaStreamDestroy(s->loop_stream);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->h_entry) cudaFreeHost(s->h_entry);
     lbm2d_batch_destroy(s->batch);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);

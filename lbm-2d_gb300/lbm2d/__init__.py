@@ -139,6 +139,7 @@ _SIGS = {
     "lbm2d_batch_launch_count": ([_P], C.c_longlong),
     "lbm2d_autotune": ([_P, _I, _D, _D, C.POINTER(_I), C.POINTER(_I)], _I),
     "lbm2d_server_create": ([_I, _D, _I, _I, C.POINTER(_P)], _I),
+    "lbm2d_server_create_ex": ([_I, _D, _I, _I, _I, C.POINTER(_P)], _I),
     "lbm2d_server_submit": ([_P, C.POINTER(Request), C.POINTER(C.c_longlong)], _I),
     "lbm2d_server_submit_state": ([_P, C.POINTER(Request), _DP, _DP, _DP, C.POINTER(C.c_longlong)], _I),
     "lbm2d_server_wait": ([_P, C.c_longlong, _D], _I),
@@ -639,11 +640,14 @@ class Server:
     """Serving loop: concurrent solves admitted by device-memory footprint and
     stepped together (see include/lbm2d.h, lbm2d_server_*)."""
 
-    def __init__(self, device=0, budget_bytes=64 << 30, max_active=512, steps_per_tick=200):
+    def __init__(self, device=0, budget_bytes=64 << 30, max_active=512, steps_per_tick=200, resident=False):
+        """resident: step the solves with the device-resident loop
+        (LBM2D_SERVE_RESIDENT; steps_per_tick then bounds one launch of the
+        loop) instead of host ticks of steps_per_tick batched steps."""
         L = lib()
         h = _P()
-        rc = L.lbm2d_server_create(int(device), float(budget_bytes), int(max_active), int(steps_per_tick),
-                                   C.byref(h))
+        rc = L.lbm2d_server_create_ex(int(device), float(budget_bytes), int(max_active), int(steps_per_tick),
+                                      1 if resident else 0, C.byref(h))
         if rc:
             raise LBMError(rc, "server create")
         self.L, self.h = L, h

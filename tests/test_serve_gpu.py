@@ -16,7 +16,10 @@ admitted, stepped together and retired exactly at their budgets.
 * Failure isolation: a request whose initial state carries a NaN (seeded on
   the host) retires with LBM2D_ERR_NAN while every other request of its mix
   stays bit-identical to its solo run.
-* Admission respects the device-memory budget."""
+* Admission respects the device-memory budget.
+* The device-resident loop (resident=True) serves every request with
+  bit-for-bit the same final state and drag/lift as the tick loop; each
+  test above runs in both modes."""
 import time
 
 import numpy as np
@@ -49,9 +52,13 @@ def _alone(product, r, storage):
     return fx, fy, f
 
 
+MODES = [pytest.param(False, id="ticks"), pytest.param(True, id="resident")]
+
+
+@pytest.mark.parametrize("resident", MODES)
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
-def test_served_results_match_alone(product, storage):
-    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=64)
+def test_served_results_match_alone(product, storage, resident):
+    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=64, resident=resident)
     ids = []
     for r in REQS:
         ids.append(srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"],
@@ -76,8 +83,8 @@ def test_served_results_match_alone(product, storage):
         assert abs(x["fx"] - fx) <= tol * scale and abs(x["fy"] - fy) <= tol * scale, (r, x, fx, fy)
 
 
-def _serve(product, reqs, storage, tick, f_inits=None):
-    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=tick)
+def _serve(product, reqs, storage, tick, f_inits=None, resident=False):
+    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=tick, resident=resident)
     f_inits = f_inits or [None] * len(reqs)
     ids = [srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"], f_init=fi,
                       keep_state=True) for r, fi in zip(reqs, f_inits)]
@@ -95,21 +102,23 @@ def _same_state(x, a):
     assert x["fx"] == a["fx"] and x["fy"] == a["fy"]
 
 
+@pytest.mark.parametrize("resident", MODES)
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
-def test_mix_equals_alone_bit_for_bit(product, storage):
+def test_mix_equals_alone_bit_for_bit(product, storage, resident):
     """Every request alone in a serving loop and the same request among the
     others (different tick boundaries, other solves in the same launches)
     end with identical populations and drag/lift."""
-    mixed = _serve(product, REQS, storage, 64)
+    mixed = _serve(product, REQS, storage, 64, resident=resident)
     for r, x in zip(REQS, mixed):
-        (a,) = _serve(product, [r], storage, 64)
+        (a,) = _serve(product, [r], storage, 64, resident=resident)
         assert x["status"] == 0 and a["status"] == 0
         assert x["steps"] == a["steps"] == r["steps"]
         _same_state(x, a)
 
 
+@pytest.mark.parametrize("resident", MODES)
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
-def test_nan_request_fails_alone(product, storage):
+def test_nan_request_fails_alone(product, storage, resident):
     """A request started from a state with one NaN population (seeded on the
     host) diverges and retires with LBM2D_ERR_NAN (4); its mix-mates, stepped
     in the same launches, end bit-identical to their solo runs."""
@@ -120,19 +129,58 @@ def test_nan_request_fails_alone(product, storage):
     s.close()
     f0[(32 * bad["nx"] + 64) * 9 + 3] = np.nan
     reqs = REQS[:3] + [bad] + REQS[3:]
-    mixed = _serve(product, reqs, storage, 64, f_inits=[None, None, None, f0, None, None, None])
+    mixed = _serve(product, reqs, storage, 64, f_inits=[None, None, None, f0, None, None, None],
+                   resident=resident)
     assert mixed[3]["status"] == 4, mixed[3]
     for k, (r, x) in enumerate(zip(reqs, mixed)):
         if k == 3:
             continue
-        (a,) = _serve(product, [r], storage, 64)
+        (a,) = _serve(product, [r], storage, 64, resident=resident)
         assert x["status"] == 0 and a["status"] == 0, (r, x)
         _same_state(x, a)
 
 
-def test_admission_respects_memory_budget(product):
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_resident_equals_ticks(product, storage):
+    """The device-resident loop and the tick loop run the same kernels on the
+    same launch shape: every request of the mix ends bit-identical, and its
+    budget is met exactly, though the resident loop admits and retires at
+    step boundaries and relaunches every 37 iterations."""
+    ticks = _serve(product, REQS, storage, 64)
+    res = _serve(product, REQS, storage, 37, resident=True)
+    for r, x, a in zip(REQS, res, ticks):
+        assert x["status"] == 0 and a["status"] == 0
+        assert x["steps"] == a["steps"] == r["steps"]
+        _same_state(x, a)
+
+
+def test_resident_late_joins(product):
+    """Requests submitted while the resident loop is stepping others join it
+    without waiting for the running ones: a short request submitted after a
+    long one is running finishes first, with the state of its solo run."""
+    long_r = dict(nx=256, ny=96, geometry=2, re=800.0, steps=40000, param=0.0)
+    short_r = dict(nx=128, ny=64, geometry=2, re=100.0, steps=100, param=0.0)
+    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=5000, resident=True)
+    i_long = srv.submit(long_r["nx"], long_r["ny"], long_r["geometry"], long_r["re"], long_r["steps"], "fp16",
+                        keep_state=True)
+    time.sleep(0.1)
+    i_short = srv.submit(short_r["nx"], short_r["ny"], short_r["geometry"], short_r["re"], short_r["steps"], "fp16",
+                         keep_state=True)
+    assert srv.wait(2, 120)
+    res = {x["id"]: x for x in srv.results()}
+    srv.close()
+    xs, xl = res[i_short], res[i_long]
+    assert xs["status"] == 0 and xl["status"] == 0
+    assert xs["steps"] == 100 and xl["steps"] == 40000
+    assert xs["t_done"] < xl["t_done"]
+    (a,) = _serve(product, [short_r], "fp16", 64, resident=True)
+    _same_state(xs, a)
+
+
+@pytest.mark.parametrize("resident", MODES)
+def test_admission_respects_memory_budget(product, resident):
     # a budget that fits about one 512x512 FP32 solve at a time
-    srv = product.Server(0, budget_bytes=70 << 20, max_active=64, steps_per_tick=50)
+    srv = product.Server(0, budget_bytes=70 << 20, max_active=64, steps_per_tick=50, resident=resident)
     for _ in range(4):
         srv.submit(512, 512, 0, 100.0, 100, "fp32")
     assert srv.wait(4, 120)
