@@ -370,35 +370,48 @@ def serve_block(args, lbm2d):
     rng = np.random.default_rng(5)
     gaps = rng.exponential(1.0 / args.rate, len(reqs))
     storage = args.serve_storage
-    # --- serving loop
-    srv = lbm2d.Server(0, budget_bytes=args.serve_budget_gb * (1 << 30), max_active=args.max_active,
-                       steps_per_tick=args.tick)
-    t0 = time.perf_counter()
-    next_t = t0
-    for r, gap in zip(reqs, gaps):
-        next_t += gap
-        while time.perf_counter() < next_t:
-            time.sleep(min(0.001, max(0.0, next_t - time.perf_counter())))
-        srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"])
-    srv.wait(len(reqs), timeout_s=3600)
-    t_end = time.perf_counter()
-    res = srv.results()
-    st = srv.stats()
-    srv.close()
-    lat = np.array([x["t_done"] - x["t_submit"] for x in res])
-    lu = sum(x["steps"] * x["nodes"] for x in res)
-    span = max(x["t_done"] for x in res) - min(x["t_submit"] for x in res)
-    status = {}
-    for x in res:
-        status[str(x["status"])] = status.get(str(x["status"]), 0) + 1
-    serve = {"requests": len(res), "failed": int(sum(1 for x in res if x["status"] != 0)), "status": status,
-             "ticks": st["ticks"], "mean_solves_per_tick": st["member_ticks"] / max(st["ticks"], 1),
-             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-             "mean_s": float(lat.mean()), "makespan_s": span, "glups": lu / span / 1e9,
-             "busy_glups": st["lattice_updates"] / max(st["busy_s"], 1e-9) / 1e9, "lattice_updates": lu,
-             "setup_s": st["setup_s"], "gpu_s": st["gpu_s"],
-             "stepping_thread_s": {k: st[k] for k in ("call_s", "wait_s", "retire_s", "join_s")},
-             "gpu_glups": st["lattice_updates"] / max(st["gpu_s"], 1e-9) / 1e9}
+
+    def leg(resident):
+        # resident: the device loop (steps_per_tick bounds one launch of it);
+        # else host ticks of args.tick batched steps
+        srv = lbm2d.Server(0, budget_bytes=args.serve_budget_gb * (1 << 30), max_active=args.max_active,
+                           steps_per_tick=args.resident_launch if resident else args.tick, resident=resident)
+        t0 = time.perf_counter()
+        next_t = t0
+        for r, gap in zip(reqs, gaps):
+            next_t += gap
+            while time.perf_counter() < next_t:
+                time.sleep(min(0.001, max(0.0, next_t - time.perf_counter())))
+            srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"])
+        srv.wait(len(reqs), timeout_s=3600)
+        res = srv.results()
+        st = srv.stats()
+        srv.close()
+        lat = np.array([x["t_done"] - x["t_submit"] for x in res])
+        lu = sum(x["steps"] * x["nodes"] for x in res)
+        span = max(x["t_done"] for x in res) - min(x["t_submit"] for x in res)
+        status = {}
+        for x in res:
+            status[str(x["status"])] = status.get(str(x["status"]), 0) + 1
+        out = {"loop": "resident" if resident else "ticks",
+               "requests": len(res), "failed": int(sum(1 for x in res if x["status"] != 0)), "status": status,
+               "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+               "mean_s": float(lat.mean()), "makespan_s": span, "glups": lu / span / 1e9,
+               "busy_glups": st["lattice_updates"] / max(st["busy_s"], 1e-9) / 1e9, "lattice_updates": lu,
+               "setup_s": st["setup_s"], "gpu_s": st["gpu_s"],
+               "stepping_thread_s": {k: st[k] for k in ("call_s", "wait_s", "retire_s", "join_s")},
+               "gpu_glups": st["lattice_updates"] / max(st["gpu_s"], 1e-9) / 1e9}
+        if resident:
+            out["launches"] = st["ticks"]
+        else:
+            out["ticks"] = st["ticks"]
+            out["mean_solves_per_tick"] = st["member_ticks"] / max(st["ticks"], 1)
+        return out
+
+    # the tick loop is the headline (the faster of the two on this mix); the
+    # device-resident loop is measured beside it
+    serve = leg(False)
+    serve_resident = leg(True) if not args.no_resident_leg else None
     # --- sequential plain solves, FIFO, same arrival times:
     #   "dropin": the reference drivers' loop through the per-solve API, one
     #             lbm2d_step call per time step followed by the drag/lift
@@ -444,12 +457,13 @@ def serve_block(args, lbm2d):
         seq["bulk"]["note"] = "same, but one lbm2d_step call for each request's whole budget"
     line = {"metric": "serving: p50/p99 time-to-solution and aggregate GLUPS", "unit": "GLUPS",
             "value": serve["glups"], "p50_s": serve["p50_s"], "p99_s": serve["p99_s"], "glups": serve["glups"],
-            "budget_scale": scale, "serve": serve, "sequential": seq or None,
+            "budget_scale": scale, "serve": serve, "serve_resident": serve_resident, "sequential": seq or None,
             "speedup_vs_sequential_dropin": (serve["glups"] / seq["dropin"]["glups"]) if seq else None,
             "speedup_vs_sequential_bulk": (serve["glups"] / seq["bulk"]["glups"]) if seq else None,
             "config": {"workload": f"{len(reqs)} requests, Poisson {args.rate}/s, grids 128x64..2048x768, "
                                    f"{{cavity, step, cylinder, side-by-side}}, Re 50-2000, budgets 1k-50k x {scale}",
-                       "storage": storage, "tick": args.tick, "budget_gb": args.serve_budget_gb}}
+                       "storage": storage, "loop": "ticks", "resident_launch": args.resident_launch,
+                       "tick": args.tick, "budget_gb": args.serve_budget_gb}}
     return line
 
 
@@ -826,6 +840,10 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--max-active", type=int, default=512)
     ap.add_argument("--tick", type=int, default=200)
+    ap.add_argument("--resident-launch", type=int, default=1000,
+                    help="serving: iterations of one launch of the resident loop")
+    ap.add_argument("--no-resident-leg", action="store_true",
+                    help="serving: skip the device-resident loop's comparison leg")
     ap.add_argument("--no-sequential", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the precision, thermal, batch and serving blocks of the default line")

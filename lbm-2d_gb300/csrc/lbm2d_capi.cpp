@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -50,6 +51,42 @@ int cuda_fail(lbm2d_solver* h, cudaError_t e, const char* what) {
 // Device buffers come from the stream-ordered allocator on the handle's
 // stream: creating and destroying solves (the serving loop does it for every
 // request) then neither synchronizes the device nor stalls other streams.
+// Mapped pinned (fx, fy) pairs of the solvers, cut from chunks that live as
+// long as the process: freeing pinned memory waits for the whole device, so
+// a solver destroyed while other work runs (a serving loop retiring a solve
+// while its device loop steps the others) would stall on it.
+struct PinnedPairs {
+    std::mutex mu;
+    std::vector<double*> free_slots;
+};
+PinnedPairs& pinned_pairs() {
+    static PinnedPairs* p = new PinnedPairs();  // never destroyed: solvers may outlive static destructors
+    return *p;
+}
+int pinned_pair_get(double** host, double** dev) {
+    PinnedPairs& P = pinned_pairs();
+    std::lock_guard<std::mutex> lock(P.mu);
+    if (P.free_slots.empty()) {
+        constexpr int kChunk = 4096;
+        double* c = nullptr;
+        if (cudaHostAlloc(&c, kChunk * 2 * sizeof(double), cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
+            return 1;
+        for (int i = kChunk; i-- > 0;) P.free_slots.push_back(c + 2 * i);
+    }
+    double* h = P.free_slots.back();
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) return 1;
+    P.free_slots.pop_back();
+    *host = h;
+    *dev = static_cast<double*>(d);
+    return 0;
+}
+void pinned_pair_put(double* host) {
+    PinnedPairs& P = pinned_pairs();
+    std::lock_guard<std::mutex> lock(P.mu);
+    P.free_slots.push_back(host);
+}
+
 template <class T>
 int dalloc(lbm2d_solver* h, T** p, size_t bytes) {
     if (*p) return LBM2D_OK;
@@ -620,10 +657,7 @@ int lbm2d_create(const lbm2d_config* cfg, lbm2d_solver** out) {
     if (!rc) rc = dalloc(h, &h->d_counter, 16);
     // The last step's drag/lift lives in mapped pinned memory: the kernel that
     // records it writes straight to the host, so a read needs no copy.
-    if (!rc && (cudaHostAlloc(&h->h_last, 2 * sizeof(double), cudaHostAllocMapped | cudaHostAllocPortable) !=
-                    cudaSuccess ||
-                cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->d_last), h->h_last, 0) != cudaSuccess))
-        rc = fail(h, LBM2D_ERR_CUDA, "mapped force buffer");
+    if (!rc && pinned_pair_get(&h->h_last, &h->d_last)) rc = fail(h, LBM2D_ERR_CUDA, "mapped force buffer");
     if (!rc) h->h_last[0] = h->h_last[1] = 0.0;
     if (!rc) rc = dalloc(h, &h->d_hist, (size_t)h->hist_cap * 2 * sizeof(double));
     if (!rc) rc = ensure_stage(h, false);
@@ -657,7 +691,7 @@ int lbm2d_destroy(lbm2d_solver* h) {
         if (b) cudaFreeAsync(b, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
-    if (h->h_last) cudaFreeHost(h->h_last);  // d_last is its device alias
+    if (h->h_last) pinned_pair_put(h->h_last);  // d_last is its device alias
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LBM2D_OK;

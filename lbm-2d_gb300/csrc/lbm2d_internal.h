@@ -231,14 +231,14 @@ struct ResEntry {
 // once entry k is in the table; the scheduler answers 2 when it admits it.
 // done[k]: the scheduler writes the steps taken + 1 when member k retires
 // (its last step and force reduction complete); the host clears it when it
-// reuses the slot.  stop: the host asks the loop to end at the next step
-// boundary.
+// reuses the slot.  join_gen: the host increments it after raising join
+// words, so the scheduler reads the join words only when it changed.  stop:
+// the host asks the loop to end at the next step boundary.
 struct ResMailbox {
     int join[kResMaxSlots];
     long long done[kResMaxSlots];
     int stop;
-    int pad;
-    long long iterations;  // iterations of all launches so far (device)
+    int join_gen;
 };
 struct ResLoop;
 int res_create(int device, int cap, int bx, int by, ResLoop** out);

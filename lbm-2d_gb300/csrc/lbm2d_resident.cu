@@ -55,14 +55,23 @@ struct ResDev {
     int* start;             // [2][kResCombos][cap + 1] first unit of each listed member
     const KParams** params; // [2][kResCombos][cap] the listed members' step parameters
     ReduceJob* jobs;        // [2][cap]
+    int* ctr;               // [2][kResCombos] units taken by the step kernels
     int* njobs;             // [2]
-    long long* it;          // [0] last committed iteration, [1] iterations of this launch, [2] halted
+    long long* it;          // [0] last committed iteration, [1] iterations of this launch, [2] halted,
+                            // [3] the join_gen last acted on
     int cap;
     int max_iters;
+    unsigned combo_mask;  // combos with a step kernel in the graph
     cudaGraphConditionalHandle cond;
 };
 
 __device__ __forceinline__ int ld_vol(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+// acquire load at system scope: the host's writes before it are visible after it
+__device__ __forceinline__ int ld_acquire_sys(const int* p) {
+    int v;
+    asm volatile("ld.acquire.sys.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 // Exclusive block scan of a 64-bit value (kTailThreads threads); total in *tot.
 __device__ __forceinline__ long long block_scan64(long long v, long long* tot) {
@@ -90,12 +99,16 @@ __device__ __forceinline__ long long block_scan64(long long v, long long* tot) {
 // Schedule the iteration whose lists go to buffer b.  pre: at the start of a
 // launch (every earlier kernel is complete).
 __device__ void res_schedule(const ResDev& d, int b, bool pre) {
-    __shared__ int s_active, s_njobs;
+    __shared__ int s_active, s_njobs, s_joins;
     __shared__ long long s_last, s_cont;
     const int t = threadIdx.x;
     if (t == 0) {
         s_active = 0;
         s_njobs = 0;
+        // one read of mapped memory per step unless the host announced joins
+        const int gen = ld_acquire_sys(&d.mb->join_gen);
+        s_joins = gen != (int)d.it[3];
+        d.it[3] = gen;
         if (pre) {
             d.it[1] = 0;
             d.it[2] = 0;
@@ -117,7 +130,7 @@ __device__ void res_schedule(const ResDev& d, int b, bool pre) {
         listed[r] = false;
         if (k >= d.cap) continue;
         int st = d.state[k];
-        if (st == 0 && ld_vol(&d.mb->join[k]) == 1) {
+        if (st == 0 && s_joins && ld_vol(&d.mb->join[k]) == 1) {
             // the host wrote the entry (copy complete) before the join word
             st = 1;
             d.state[k] = 1;
@@ -140,9 +153,11 @@ __device__ void res_schedule(const ResDev& d, int b, bool pre) {
                 continue;
             }
         } else {
-            listed[r] = true;
             combo[r] = __ldcg(&e->combo);
             units[r] = __ldcg(&e->units);
+            // a kind this graph has no kernel for waits (the host relaunches
+            // the loop with it)
+            listed[r] = (d.combo_mask >> combo[r]) & 1u;
         }
         atomicAdd(&s_active, 1);
     }
@@ -159,7 +174,9 @@ __device__ void res_schedule(const ResDev& d, int b, bool pre) {
     const bool cont = s_cont != 0;
     // pass 2: per-combo lists in slot order (empty when the loop ends)
     const int cap = d.cap;
+    if (t < kResCombos) d.ctr[b * kResCombos + t] = 0;
     for (int c = 0; c < kResCombos; ++c) {
+        if (!(d.combo_mask & (1u << c))) continue;  // no kernel reads its list
         long long v = 0;
 #pragma unroll
         for (int r = 0; r < kSlotsPerThread; ++r)
@@ -247,62 +264,99 @@ __global__ void __launch_bounds__(kTailThreads) res_tail_kernel(ResDev d, int b)
 // buffer b, one unit per block at a time.  KIND 0: paired (tile blocks, then
 // the member's boundary blocks); 1: one node per thread; 2: one node per
 // thread with the thermal DDF.
-// The launch bounds are the batched kernels' (batch_step_pair_kernel,
-// batch_step_th_kernel for the 16-bit thermal forms, batch_step_kernel), so
-// each kind compiles as the tick loop's kernel does.
+// Launch bounds: the register budgets of the batched kernels
+// (batch_step_pair_kernel 64, batch_step_th_kernel for the 16-bit thermal
+// forms 48; batch_step_kernel's one-node forms need at most 80 and keep 6
+// blocks of 128 threads per SM), so the unit loop's own state does not cost
+// occupancy.
 template <class T, int KIND>
-constexpr int kResMaxThreads = (KIND == 2 && sizeof(T) == 2) ? 256 : 512;
+constexpr int kResMaxThreads = (KIND == 2 && sizeof(T) == 2) ? 256 : (KIND == 0 ? 128 : 128);
 template <class T, int KIND>
-constexpr int kResMinBlocks = KIND == 0 ? 2 : ((KIND == 2 && sizeof(T) == 2) ? 5 : 1);
+constexpr int kResMinBlocks = KIND == 0 ? 6 : ((KIND == 2 && sizeof(T) == 2) ? 5 : (KIND == 1 ? 6 : 1));
 
 template <class T, int KIND>
 __global__ void __launch_bounds__(kResMaxThreads<T, KIND>, kResMinBlocks<T, KIND>)
     res_step_kernel(ResDev d, int b, int c) {
-    __shared__ KParams sp;
-    __shared__ int s_m, s_local;
+    __shared__ __align__(16) KParams sp[2];
+    __shared__ int s_st[kResMaxSlots + 1];
+    __shared__ int s_u[2];
     const int n = d.count[b * kResCombos + c];
     if (n == 0) return;
     const int* st = d.start + (size_t)(b * kResCombos + c) * (d.cap + 1);
-    const KParams* const* pp = d.params + (size_t)(b * kResCombos + c) * d.cap;
     const int total = st[n];
+    // block k starts with unit k; a block without one has nothing to do
+    if ((int)blockIdx.x >= total) return;
+    const int first = min((int)gridDim.x, total);  // units handed out by block index
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int u = blockIdx.x; u < total; u += gridDim.x) {
-        if (tid == 0) {
-            int lo = 0, hi = n - 1;  // last member whose first unit is <= u
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (st[mid] <= u) lo = mid;
-                else hi = mid - 1;
+    for (int i = tid; i <= n; i += nt) s_st[i] = st[i];
+    const KParams* const* pp = d.params + (size_t)(b * kResCombos + c) * d.cap;
+    int* ctr = d.ctr + b * kResCombos + c;
+    // the others are taken one at a time from the combo's counter (the block
+    // scheduler's dynamic balance); the next one is taken, and its member's
+    // parameters staged into the other buffer, while the current one runs
+    if (tid == 0) {
+        s_u[0] = (int)blockIdx.x;
+        s_u[1] = first + atomicAdd(ctr, 1);
+    }
+    __syncthreads();
+    auto member_of = [&](int u) {  // last member whose first unit is <= u
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_st[mid] <= u) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
+    constexpr int kChunks = (int)(sizeof(KParams) / 16);
+    auto stage = [&](int m, int buf) {  // 16-byte asynchronous copies
+        if (tid < kChunks) {
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char*>(&sp[buf]) + 16 * tid);
+            const char* src = reinterpret_cast<const char*>(pp[m]) + 16 * tid;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    int u = s_u[0], cb = 0;
+    if (u >= total) return;
+    int staged[2] = {member_of(u), -1};
+    stage(staged[0], 0);
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    for (;;) {
+        const int un = s_u[cb ^ 1];
+        if (un < total) {
+            const int mn = member_of(un);
+            if (mn != staged[cb ^ 1]) {
+                staged[cb ^ 1] = mn;
+                stage(mn, cb ^ 1);
             }
-            s_m = lo;
-            s_local = u - st[lo];
         }
-        __syncthreads();
-        {
-            const int* src = reinterpret_cast<const int*>(pp[s_m]);
-            int* dst = reinterpret_cast<int*>(&sp);
-            for (int w = tid; w < (int)(sizeof(KParams) / sizeof(int)); w += nt) dst[w] = src[w];
-        }
-        __syncthreads();
-        const int local = s_local;
-        const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
+        if (tid == 0) s_u[cb] = un < total ? first + atomicAdd(ctr, 1) : total;
+        const KParams& p = sp[cb];
+        const int local = u - s_st[staged[cb]];
+        const int tiles = p.gx * ((p.ny + (int)blockDim.y - 1) / (int)blockDim.y);
         if constexpr (KIND == 0) {
             if constexpr (!std::is_same<T, double>::value) {
                 const int reg = (tiles + kBatchTiles - 1) / kBatchTiles;
                 if (local >= reg) {
-                    pair_boundary_block<T>(sp, local - reg, tiles);
+                    pair_boundary_block<T>(p, local - reg, tiles);
                 } else {
                     // a paired member's boundary pairs are all in its
                     // boundary blocks (none when it has no boundary node)
                     for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
-                        step_pair_block<T, false, true>(sp, t % sp.gx, t / sp.gx, sp.gx);
+                        step_pair_block<T, false, true>(p, t % p.gx, t / p.gx, p.gx);
                 }
             }
         } else {
             for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
-                step_block<T, KIND == 2>(sp, t % sp.gx, t / sp.gx, sp.gx);
+                step_block<T, KIND == 2>(p, t % p.gx, t / p.gx, p.gx);
         }
-        __syncthreads();  // sp and s_m are rewritten for the next unit
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();  // the next unit's id and parameters are in place
+        if (un >= total) break;
+        u = un;
+        cb ^= 1;
     }
 }
 
@@ -351,6 +405,7 @@ int build_graph(ResLoop* r, unsigned mask, int max_iters) {
     e = cudaGraphConditionalHandleCreate(&r->d.cond, r->graph, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) return (int)e;
     r->d.max_iters = max_iters;
+    r->d.combo_mask = mask;
     ResDev d = r->d;
     int zero = 0, one = 1;
     void* pre_args[] = {&d};
@@ -447,7 +502,8 @@ int res_create(int device, int cap, int bx, int by, ResLoop** out) {
     const size_t o_table = take(C * sizeof(ResEntry)), o_state = take(C * 4), o_par = take(C * 4),
                  o_taken = take(C * 4), o_last = take(C * 8), o_count = take(2 * kResCombos * 4),
                  o_start = take(2 * kResCombos * (C + 1) * 4), o_params = take(2 * kResCombos * C * sizeof(void*)),
-                 o_jobs = take(2 * C * sizeof(ReduceJob)), o_njobs = take(2 * 4), o_it = take(3 * 8);
+                 o_jobs = take(2 * C * sizeof(ReduceJob)), o_njobs = take(2 * 4), o_it = take(4 * 8),
+                 o_ctr = take(2 * kResCombos * 4);
     if ((e = cudaMalloc(&r->dev_block, off)) != cudaSuccess || (e = cudaMemset(r->dev_block, 0, off)) != cudaSuccess) {
         if (r->dev_block) cudaFree(r->dev_block);
         cudaFreeHost(r->mb_host);
@@ -468,6 +524,7 @@ int res_create(int device, int cap, int bx, int by, ResLoop** out) {
     d.jobs = reinterpret_cast<ReduceJob*>(base + o_jobs);
     d.njobs = reinterpret_cast<int*>(base + o_njobs);
     d.it = reinterpret_cast<long long*>(base + o_it);
+    d.ctr = reinterpret_cast<int*>(base + o_ctr);
     d.cap = cap;
     *out = r;
     return 0;

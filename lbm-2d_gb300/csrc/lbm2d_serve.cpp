@@ -488,6 +488,8 @@ bool res_join_ready(lbm2d_server* s) {
         if (s->running && (s->mask_running & bit)) {
             std::atomic_thread_fence(std::memory_order_seq_cst);
             mb->join[k] = 1;
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+            mb->join_gen = mb->join_gen + 1;
             s->slot_state[k] = 2;
         } else {
             s->slot_state[k] = 1;
@@ -537,6 +539,8 @@ void resident_loop(lbm2d_server* s) {
                         mb->join[k] = 1;
                         s->slot_state[k] = 2;
                     }
+                std::atomic_thread_fence(std::memory_order_seq_cst);
+                mb->join_gen = mb->join_gen + 1;
                 std::atomic_thread_fence(std::memory_order_seq_cst);
                 const double t0 = now_s();
                 cudaEventRecord(s->ev0, s->loop_stream);

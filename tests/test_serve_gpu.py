@@ -34,7 +34,8 @@ REQS = [dict(nx=128, ny=64, geometry=2, re=100.0, steps=300, param=0.0),
         dict(nx=160, ny=60, geometry=1, re=200.0, steps=200, param=0.0),
         dict(nx=200, ny=80, geometry=3, re=150.0, steps=350, param=3.0),
         dict(nx=64, ny=64, geometry=4, re=0.0, steps=250, param=1e4),
-        dict(nx=256, ny=96, geometry=2, re=800.0, steps=120, param=0.0)]
+        dict(nx=256, ny=96, geometry=2, re=800.0, steps=120, param=0.0),
+        dict(nx=131, ny=50, geometry=2, re=150.0, steps=180, param=0.0)]  # odd width: one node per thread
 
 
 # final populations, served in the mix vs the plain per-solve API
@@ -129,7 +130,7 @@ def test_nan_request_fails_alone(product, storage, resident):
     s.close()
     f0[(32 * bad["nx"] + 64) * 9 + 3] = np.nan
     reqs = REQS[:3] + [bad] + REQS[3:]
-    mixed = _serve(product, reqs, storage, 64, f_inits=[None, None, None, f0, None, None, None],
+    mixed = _serve(product, reqs, storage, 64, f_inits=[None, None, None, f0, None, None, None, None],
                    resident=resident)
     assert mixed[3]["status"] == 4, mixed[3]
     for k, (r, x) in enumerate(zip(reqs, mixed)):
