@@ -60,6 +60,11 @@ struct lbm2d_batch {
     cudaStream_t stream = nullptr;
     unsigned int* d_status = nullptr;  // bit 1: a tile-pipeline wait ran out
     cudaEvent_t ev = nullptr;
+    // groups after the first run on side streams forked from the batch
+    // stream at every step and joined back before the next
+    cudaEvent_t ev_fork = nullptr;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev_join;
     std::vector<Member> members;
     std::vector<Group> groups;
     bool layout_dirty = true;
@@ -299,20 +304,54 @@ int prepare(lbm2d_batch* b) {
     return LBM2D_OK;
 }
 
+// One step of every batched group.  The groups' members are independent, so
+// the groups run concurrently: the first on the batch stream, each other one
+// on a side stream forked from it and joined back (a paired and a one-node
+// group overlap: 16 + 16 FP16 cylinders 512x256 / 511x256, 104-118 against
+// 98 us per step).
+// Side streams and join events for every batched group but the first
+// (created outside any stream capture).
+int ensure_side(lbm2d_batch* b) {
+    size_t n = 0;
+    for (auto& g : b->groups)
+        if (g.kind != KERNEL_ROWS) ++n;
+    while (b->side.size() + 1 < n) {
+        cudaStream_t s = nullptr;
+        cudaEvent_t e = nullptr;
+        BCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "side stream");
+        b->side.push_back(s);
+        BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "join event");
+        b->ev_join.push_back(e);
+    }
+    return LBM2D_OK;
+}
+
 int launch_one(lbm2d_batch* b, int parity) {
-    for (auto& g : b->groups) {
-        if (g.kind == KERNEL_ROWS) continue;  // solo members are launched by lbm2d_batch_step
+    std::vector<Group*> gs;
+    for (auto& g : b->groups)
+        if (g.kind != KERNEL_ROWS) gs.push_back(&g);  // solo members are launched by lbm2d_batch_step
+    const size_t nside = gs.empty() ? 0 : gs.size() - 1;
+    if (b->side.size() < nside) return bfail(b, LBM2D_ERR_STATE, "batch side streams missing");
+    if (nside > 0) BCK(cudaEventRecord(b->ev_fork, b->stream), "fork");
+    for (size_t i = 0; i < gs.size(); ++i) {
+        Group& g = *gs[i];
+        cudaStream_t s = i == 0 ? b->stream : b->side[i - 1];
+        if (i > 0) BCK(cudaStreamWaitEvent(s, b->ev_fork, 0), "fork wait");
         int e = g.kind == KERNEL_TILES
                     ? launch_tiles_batch(g.storage, g.thermal != 0, g.d_params[parity], g.d_tile_member,
-                                         g.d_tile_start, g.ntiles, g.grid, b->d_status, b->stream)
+                                         g.d_tile_start, g.ntiles, g.grid, b->d_status, s)
                     : launch_batch_step(g.storage, g.d_params[parity], g.d_block_map, g.nblocks, g.thermal, b->bx,
-                                        b->by, b->stream, g.kind == KERNEL_PAIR ? 1 : 0);
+                                        b->by, s, g.kind == KERNEL_PAIR ? 1 : 0);
         ++b->launches;
         if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)e));
         if (g.njobs > 0) {
-            e = launch_batch_force_reduce(g.d_jobs[parity], g.njobs, b->stream);
+            e = launch_batch_force_reduce(g.d_jobs[parity], g.njobs, s);
             ++b->launches;
             if (e) return bfail(b, LBM2D_ERR_CUDA, std::string("batch reduce: ") + cudaGetErrorString((cudaError_t)e));
+        }
+        if (i > 0) {
+            BCK(cudaEventRecord(b->ev_join[i - 1], s), "join");
+            BCK(cudaStreamWaitEvent(b->stream, b->ev_join[i - 1], 0), "join wait");
         }
     }
     return LBM2D_OK;
@@ -323,6 +362,8 @@ int capture_pair(lbm2d_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     cudaGraph_t g = nullptr;
+    int rs = ensure_side(b);
+    if (rs) return rs;
     BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     const long long l0 = b->launches;
     int rc = launch_one(b, 0);
@@ -364,6 +405,7 @@ int lbm2d_batch_create(int device, lbm2d_batch** out) {
     b->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&b->d_status, 16) != cudaSuccess || cudaMemset(b->d_status, 0, 16) != cudaSuccess) {
         delete b;
         return LBM2D_ERR_CUDA;
@@ -381,6 +423,9 @@ int lbm2d_batch_destroy(lbm2d_batch* b) {
     if (b->h_params) cudaFreeHost(b->h_params);
     if (b->h_left) cudaFreeHost(b->h_left);
     cudaEventDestroy(b->ev);
+    cudaEventDestroy(b->ev_fork);
+    for (cudaStream_t s : b->side) cudaStreamDestroy(s);
+    for (cudaEvent_t e : b->ev_join) cudaEventDestroy(e);
     cudaStreamDestroy(b->stream);
     cudaFree(b->d_status);
     delete b;
@@ -489,6 +534,7 @@ int lbm2d_batch_step(lbm2d_batch* b, int nsteps) {
             }
         }
         if (nsteps & 1) {
+            if ((rc = ensure_side(b))) return rc;
             if ((rc = launch_one(b, 0))) return rc;
         }
     }
