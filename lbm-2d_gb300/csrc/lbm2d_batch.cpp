@@ -126,7 +126,7 @@ int build_layout(lbm2d_batch* b) {
     std::map<std::tuple<int, int, int>, int> gi;
     for (size_t k = 0; k < b->members.size(); ++k) {
         lbm2d_solver* h = b->members[k].h;
-        const auto key = std::make_tuple(h->storage, h->thermal ? 1 : 0, kernel_kind(h));
+        const auto key = std::make_tuple(h->storage, h->thermal ? 1 : 0, kernel_kind(h, true));
         auto it = gi.find(key);
         if (it == gi.end()) {
             gi[key] = (int)b->groups.size();
@@ -216,7 +216,7 @@ int prepare(lbm2d_batch* b) {
             }
             KParams p;
             const long long l0 = h->launches;
-            if ((rc = prepare_steps(h, mem.tau, mem.u, p))) return bfail(b, rc, std::string("member: ") + h->err);
+            if ((rc = prepare_steps(h, mem.tau, mem.u, p, true))) return bfail(b, rc, std::string("member: ") + h->err);
             const bool budgeted = mem.budget >= 0;
             left[k] = (int)std::min<long long>(std::max(mem.budget, 0LL), 0x7FFFFFFF);
             if (budgeted) {
@@ -244,7 +244,7 @@ int prepare(lbm2d_batch* b) {
             // tile blocks, then the member's boundary blocks (nbpairs set only
             // when its slots are laid out for them)
             const int nbb = p.nbpairs > 0 ? (p.nbpairs + p.bchunk - 1) / p.bchunk : 0;
-            reg[k] = (p.gx * gy + kBatchTiles - 1) / kBatchTiles;
+            reg[k] = ((p.ftiles > 0 ? p.ftiles : p.gx * gy) + kBatchTiles - 1) / kBatchTiles;
             start[k + 1] = start[k] + reg[k] + nbb;
             if (h->nslots > 0) {
                 jobs[0].push_back({h->d_partials, h->nslots, h->hist_cap, h->d_hist, h->d_counter, h->d_last,

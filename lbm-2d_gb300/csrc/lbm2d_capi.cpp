@@ -133,6 +133,12 @@ CollideParams collide_params(const lbm2d_solver* h, double tau) {
     return c;
 }
 
+// Flat tiles of a batched paired member: ceil(N / 2) pairs, bx*by per tile.
+int flat_tiles(const lbm2d_solver* h) {
+    const long long pairs = ((long long)h->N + 1) / 2, B = (long long)h->bx * h->by;
+    return (int)((pairs + B - 1) / B);
+}
+
 KParams base_params(const lbm2d_solver* h) {
     KParams p;
     std::memset(&p, 0, sizeof(p));
@@ -166,6 +172,7 @@ KParams base_params(const lbm2d_solver* h) {
         p.nbpairs = h->nbpairs;
         p.bchunk = h->bchunk;
     }
+    if (h->slot_bpass) p.ftiles = flat_tiles(h);
     p.pair = use_pair(h) ? 1 : 0;
     const int nbw = h->bx * (p.pair ? 2 : 1);  // node width of a block
     p.gx = (h->nx + nbw - 1) / nbw;
@@ -307,17 +314,26 @@ bool use_pair(const lbm2d_solver* h) {
     return h->variant != 1 && (h->nx % 2 == 0) && h->storage != ST_FP64 && (!h->thermal || h->variant == 2);
 }
 
-int kernel_kind(const lbm2d_solver* h) {
+// The kernel a step of h runs.  batch: stepped by a batch (or the resident
+// serving loop), whose paired kernel walks flat pairs (2k, 2k + 1) of the
+// node index, so any width with an even node count pairs there; a plain step
+// of the same solver runs the single-solve kernels.
+int kernel_kind(const lbm2d_solver* h, bool batch) {
     const bool tiles_ok = h->storage != ST_FP64;
     if (h->variant == 3 && tiles_ok) return KERNEL_TILES;
     if (h->variant == 0 && tiles_ok) {
-        if (rows_eligible(h->storage, h->nx, h->ny, h->thermal) && !h->resident &&
-            (!h->in_batch || (long long)h->N >= kBatchSoloNodes))
+        if (rows_eligible(h->storage, h->nx, h->ny, h->thermal) && !(batch && h->resident) &&
+            (!batch || (long long)h->N >= kBatchSoloNodes))
             return KERNEL_ROWS;
     }
-    if (!use_pair(h)) return KERNEL_SCALAR;
+    // flat pairs store 8-byte (FP32) / 4-byte (16-bit) pairs at node index
+    // j*N + 2k of plane j: aligned only when the node count N is even
+    const bool flat = batch && !h->thermal && h->storage != ST_FP64 && h->variant != 1 && h->N % 2 == 0;
+    if (!use_pair(h) && !flat) return KERNEL_SCALAR;
     return KERNEL_PAIR;
 }
+
+int kernel_kind(const lbm2d_solver* h) { return kernel_kind(h, false); }
 
 // Per-warp force slots of the kernel that will run.  Scalar / paired
 // kernels: one table entry per launch block (blocks without a force node get
@@ -325,19 +341,20 @@ int kernel_kind(const lbm2d_solver* h) {
 // tiles (tile t goes to CTA t mod grid) hold a force node.
 // The node pairs (x even, x + 1) that hold a boundary node (every boundary
 // node has a record), first node's index, ascending.
-void boundary_pair_list(const lbm2d_solver* h, std::vector<int>& out) {
+// flat: the pairs (2k, 2k + 1) of the node index instead.
+void boundary_pair_list(const lbm2d_solver* h, std::vector<int>& out, bool flat) {
     out.clear();
     out.reserve(h->geo.rec_node.size());
-    for (int32_t id : h->geo.rec_node) out.push_back(id - (id % h->nx) % 2);
+    for (int32_t id : h->geo.rec_node) out.push_back(flat ? (id & ~1) : id - (id % h->nx) % 2);
     std::sort(out.begin(), out.end());
     out.erase(std::unique(out.begin(), out.end()), out.end());
 }
 
-int ensure_slots(lbm2d_solver* h) {
-    const int kind = kernel_kind(h);
-    // a batch member on the paired kernel: its boundary pairs run in boundary
-    // blocks appended after its tile blocks
-    const bool bpass = kind == KERNEL_PAIR && h->in_batch && !h->thermal;
+int ensure_slots(lbm2d_solver* h, bool batch) {
+    const int kind = kernel_kind(h, batch);
+    // a batch member on the paired kernel: flat pair tiles, and its boundary
+    // pairs in boundary blocks appended after them
+    const bool bpass = kind == KERNEL_PAIR && batch && !h->thermal;
     int grid = 0;
     const long long ntiles = ((long long)h->N + tiles_width() - 1) / tiles_width();
     if (kind == KERNEL_ROWS) {
@@ -380,7 +397,7 @@ int ensure_slots(lbm2d_solver* h) {
         // force nodes are boundary nodes, so a CTA holds force slots when
         // its chunk has a pair with a force record.
         const int warps = rows_warps_per_block();
-        boundary_pair_list(h, bpairs);
+        boundary_pair_list(h, bpairs, false);
         bchunk = bpairs.empty() ? 0 : (int)((bpairs.size() + (size_t)grid - 1) / (size_t)grid);
         slots.assign((size_t)grid, -1);
         for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
@@ -416,20 +433,18 @@ int ensure_slots(lbm2d_solver* h) {
             }
         h->nslots = k;
     } else if (bpass) {
-        // tile blocks own no slots; boundary block i (pairs [i*B, (i+1)*B),
-        // B = bx*by, one per thread) owns one per warp when it holds a force
-        // pair, at block_slot[ntiles + i]
+        // ntiles flat tiles of B = bx*by pairs own no slots; boundary block
+        // i (pairs [i*B, (i+1)*B), one per thread) owns one per warp when it
+        // holds a force pair, at block_slot[ntiles + i]
         const int B = h->bx * h->by, warps = (B + 31) / 32;
-        const size_t gx = (size_t)((h->nx + 2 * h->bx - 1) / (2 * h->bx)), gy = (size_t)((h->ny + h->by - 1) / h->by);
-        boundary_pair_list(h, bpairs);
+        boundary_pair_list(h, bpairs, true);
         bchunk = B;
-        const size_t ntl = gx * gy, nbb = (bpairs.size() + (size_t)B - 1) / (size_t)B;
+        const size_t ntl = (size_t)flat_tiles(h), nbb = (bpairs.size() + (size_t)B - 1) / (size_t)B;
         slots.assign(ntl + nbb, -1);
         for (size_t r = 0; r < h->geo.rec_force.size(); ++r) {
             if (!h->geo.rec_force[r]) continue;
             const int id = h->geo.rec_node[r];
-            const size_t i = (size_t)(std::lower_bound(bpairs.begin(), bpairs.end(), id - (id % h->nx) % 2) -
-                                      bpairs.begin());
+            const size_t i = (size_t)(std::lower_bound(bpairs.begin(), bpairs.end(), id & ~1) - bpairs.begin());
             slots[ntl + i / (size_t)B] = 0;
         }
         int k = 0;
@@ -556,7 +571,7 @@ int check_handle(lbm2d_solver* h) {
 // Prepare a handle for steps with (tau, u): re-collide on parameter change,
 // push geometry, force slots and the prologue, then fill the kernel
 // parameters of the next step.
-int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p) {
+int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p, bool batch) {
     int rc;
     if (!(tau > 0.0)) return fail(h, LBM2D_ERR_INVALID, "tau must be positive");
     const CollideParams c = collide_params(h, tau);
@@ -564,7 +579,7 @@ int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p) {
         if ((rc = materialize(h))) return rc;
     }
     if ((rc = upload_geometry(h))) return rc;
-    if ((rc = ensure_slots(h))) return rc;
+    if ((rc = ensure_slots(h, batch))) return rc;
     // set-up of the allocation-free entry point on this device (once); a
     // failure here is reported by that entry point, not by this step
     noalloc_bind_device(h->device);
@@ -1285,7 +1300,7 @@ int lbm2d_get_info(lbm2d_solver* h, lbm2d_info* info) {
     info->steps_done = h->steps_done;
     info->block_x = h->bx;
     info->block_y = h->by;
-    info->kernel = kernel_kind(h);
+    info->kernel = kernel_kind(h, h->in_batch);  // a batch member: the kernel its batch steps it with
     return LBM2D_OK;
 }
 

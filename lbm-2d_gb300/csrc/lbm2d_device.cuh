@@ -1146,11 +1146,16 @@ struct PairStore<float> {
     static __device__ __forceinline__ void st(float* p, size_t i, float a, float b, uint32_t) {
         __stcs(reinterpret_cast<float2*>(p + i), make_float2(a, b));
     }
+    // one node (the last of a lattice with an odd node count)
+    static __device__ __forceinline__ void st1(float* p, size_t i, float a, uint32_t) { __stcs(p + i, a); }
 };
 template <>
 struct PairStore<__half> {
     static __device__ __forceinline__ void st(__half* p, size_t i, float a, float b, uint32_t rb) {
         *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_f16x2(a, b, rb);
+    }
+    static __device__ __forceinline__ void st1(__half* p, size_t i, float a, uint32_t rb) {
+        p[i] = __ushort_as_half((unsigned short)(cvt_rs_f16x2(a, a, rb) & 0xFFFFu));
     }
 };
 template <>
@@ -1158,27 +1163,33 @@ struct PairStore<__nv_bfloat16> {
     static __device__ __forceinline__ void st(__nv_bfloat16* p, size_t i, float a, float b, uint32_t rb) {
         *reinterpret_cast<uint32_t*>(p + i) = cvt_rs_bf16x2(a, b, rb);
     }
+    static __device__ __forceinline__ void st1(__nv_bfloat16* p, size_t i, float a, uint32_t rb) {
+        p[i] = __ushort_as_bfloat16((unsigned short)(cvt_rs_bf16x2(a, a, rb) & 0xFFFFu));
+    }
 };
 
-// One step of the node pair (x0, x0 + 1), x0 even (FP32/FP16/BF16 storage;
-// TH: with the thermal double distribution, collided by thermal_pair_dev):
-// pull with the rebuild of special nodes, momentum exchange (the pair's
-// link terms summed in FP32, node x0 then x0 + 1, returned in fxs/fys),
-// collision and stores.  PLAIN: the pair holds no boundary node (those are
-// stepped by a boundary block), so a solid lane (f = 0) is its only special
-// case and the pulls need no rebuild.
+// One step of the node pair a = (xa, ya), b = (xb, yb), stored at node
+// indices n0 and n0 + 1, n0 even: two x-neighbours of a row (b = a + x), or
+// a flat pair of the node index, which may end one row and start the next
+// (FP32/FP16/BF16 storage; TH: with the thermal double distribution, collided
+// by thermal_pair_dev): pull with the rebuild of special nodes, momentum
+// exchange (the pair's link terms summed in FP32, node a then b, returned in
+// fxs/fys), collision and stores.  PLAIN: the pair holds no boundary node
+// (those are stepped by a boundary block), so a solid lane (f = 0) is its
+// only special case and the pulls need no rebuild.  has_b false: n0 is the
+// last node of a lattice with an odd node count (b is absent: the caller
+// marks it solid, and only a is stored).
 template <class T, bool TH, bool PLAIN>
-__device__ __forceinline__ void pair_step(const KParams& p, int x0, int y, uint32_t skey, uint2 fl, double& fxs,
-                                          double& fys) {
-    const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
+__device__ __forceinline__ void pair_step(const KParams& p, unsigned n0, int xa, int ya, int xb, int yb, bool has_b,
+                                          uint32_t skey, uint2 fl, double& fxs, double& fys) {
     constexpr float iS = Pop<T>::kInvS;
     float fa[9], fb[9];  // deviations in storage units
     float ea[TH ? 9 : 1], eb[TH ? 9 : 1];  // thermal deviations (TH)
     const bool oka = !(fl.x & FLAG_SOLID), okb = !(fl.y & FLAG_SOLID);
     if constexpr (PLAIN) {
         const T* __restrict__ P = static_cast<const T*>(p.fin);
-        pull_raw<T>(p, P, x0, y, fa);
-        pull_raw<T>(p, P, x0 + 1, y, fb);
+        pull_raw<T>(p, P, xa, ya, fa);
+        if (has_b) pull_raw<T>(p, P, xb, yb, fb);
         constexpr float S = Pop<T>::kS;
         if (!oka) {
 #pragma unroll
@@ -1189,11 +1200,16 @@ __device__ __forceinline__ void pair_step(const KParams& p, int x0, int y, uint3
             for (int j = 0; j < 9; ++j) fb[j] = -p.shf[j] * S;
         }
     } else if constexpr (TH) {
-        build_dev_s_th<T>(p, x0, y, fl.x, fa, ea);
-        build_dev_s_th<T>(p, x0 + 1, y, fl.y, fb, eb);
+        build_dev_s_th<T>(p, xa, ya, fl.x, fa, ea);
+        build_dev_s_th<T>(p, xb, yb, fl.y, fb, eb);
     } else {
-        build_dev_s<T>(p, x0, y, fl.x, fa);
-        build_dev_s<T>(p, x0 + 1, y, fl.y, fb);
+        build_dev_s<T>(p, xa, ya, fl.x, fa);
+        if (has_b) {
+            build_dev_s<T>(p, xb, yb, fl.y, fb);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) fb[j] = -p.shf[j] * Pop<T>::kS;
+        }
     }
     if (!PLAIN && ((fl.x | fl.y) & FLAG_BOUNDARY)) {
         // momentum exchange of the nodes' links (src/lbm.hpp:565-577)
@@ -1242,16 +1258,20 @@ __device__ __forceinline__ void pair_step(const KParams& p, int x0, int y, uint3
     }
     // a solid node's state never changes once settled (the heated
     // cavity's Dirichlet passes rewrite node states every step)
-    const bool settled = p.skip_settled_solids && y < p.ny - 1;
-    const bool skip_a = !oka && settled && x0 > 0;
-    const bool skip_b = !okb && settled && x0 + 1 < p.nx - 1;
+    const bool skip_a = !oka && p.skip_settled_solids && ya < p.ny - 1 && xa > 0;
+    const bool skip_b = !has_b || (!okb && p.skip_settled_solids && yb < p.ny - 1 && xb < p.nx - 1);
     if (!(skip_a && skip_b)) {
         T* __restrict__ Fo = static_cast<T*>(p.fout);
         const size_t N = (size_t)p.N;
         uint32_t rb[9] = {};
         if constexpr (Pop<T>::kRounds) rand9(skey + n0, rb);
+        if (has_b) {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
+            for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) PairStore<T>::st1(Fo + j * N, n0, fa[j], rb[j]);
+        }
         if constexpr (TH) {
             T* __restrict__ Go = static_cast<T*>(p.gout);
             if constexpr (Pop<T>::kRounds) rand9((skey + n0) ^ 0x6A09E667u, rb);
@@ -1306,14 +1326,58 @@ __device__ __forceinline__ void step_pair_block(const KParams& p, int bxi, int b
     if (x0 < p.nx && y < p.ny) {
         const unsigned n0 = (unsigned)y * (unsigned)p.nx + (unsigned)x0;
         const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
-        if (!PLAIN || !((fl.x | fl.y) & FLAG_BOUNDARY)) pair_step<T, TH, PLAIN>(p, x0, y, skey, fl, fxs, fys);
+        if (!PLAIN || !((fl.x | fl.y) & FLAG_BOUNDARY))
+            pair_step<T, TH, PLAIN>(p, n0, x0, y, x0 + 1, y, true, skey, fl, fxs, fys);
     }
     if (!PLAIN) pair_block_slots(p, byi * gx + bxi, fxs, fys);
 }
 
+// The nodes of the flat pair (n0, n0 + 1), n0 even: coordinates, flags and
+// whether n0 + 1 exists.  The flags' second word past the last node is
+// padding; an absent node is marked solid.
+__device__ __forceinline__ void flat_pair(const KParams& p, unsigned n0, int& xa, int& ya, int& xb, int& yb,
+                                          bool& has_b, uint2& fl) {
+    ya = (int)(n0 / (unsigned)p.nx);
+    xa = (int)n0 - ya * p.nx;
+    xb = xa + 1;
+    yb = ya;
+    if (xb == p.nx) {
+        xb = 0;
+        ++yb;
+    }
+    has_b = (long long)n0 + 1 < p.N;
+    fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
+    if (!has_b) fl.y = FLAG_SOLID;
+}
+
+// Flat tile t of a batched paired instance: its pairs [t*B, (t+1)*B), B the
+// block's threads, one pair (2k, 2k + 1) of the node index per thread, so
+// any width pairs (the node count N is even: a pair store at j*N + 2k is
+// aligned in every plane j).  The instance's boundary pairs are stepped by its
+// boundary blocks (pair_boundary_block); this tile skips them.
+template <class T>
+__device__ __forceinline__ void step_flat_pair_block(const KParams& p, int t) {
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const long long q = (long long)t * (blockDim.x * blockDim.y) + tid;
+    uint32_t skey = 0;
+    if constexpr (Pop<T>::kRounds) skey = pair_seed_key(p, t == 0 && tid == 0);
+    if (2 * q < p.N) {
+        const unsigned n0 = (unsigned)(2 * q);
+        int xa, ya, xb, yb;
+        bool has_b;
+        uint2 fl;
+        flat_pair(p, n0, xa, ya, xb, yb, has_b, fl);
+        if (!((fl.x | fl.y) & FLAG_BOUNDARY)) {
+            double fxs = 0.0, fys = 0.0;
+            pair_step<T, false, true>(p, n0, xa, ya, xb, yb, has_b, skey, fl, fxs, fys);
+        }
+    }
+}
+
 // Boundary block i of an instance: its boundary pairs [i*B, (i+1)*B), B the
-// block's threads, one pair per thread (bpairs, ascending); the force slots
-// of boundary block i are block_slot[ntiles + i], ntiles = gx * gy.
+// block's threads, one flat pair per thread (bpairs, ascending); the force
+// slots of boundary block i are block_slot[ntiles + i], ntiles its flat
+// tiles.
 template <class T>
 __device__ __forceinline__ void pair_boundary_block(const KParams& p, int i, int ntiles) {
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -1322,10 +1386,12 @@ __device__ __forceinline__ void pair_boundary_block(const KParams& p, int i, int
     if constexpr (Pop<T>::kRounds) skey = pair_seed_key(p, false);
     double fxs = 0.0, fys = 0.0;
     if (j < p.nbpairs) {
-        const int n0 = p.bpairs[j];
-        const int y = (int)((unsigned)n0 / (unsigned)p.nx), x0 = n0 - y * p.nx;
-        const uint2 fl = __ldg(reinterpret_cast<const uint2*>(p.flags + n0));
-        pair_step<T, false, false>(p, x0, y, skey, fl, fxs, fys);
+        const unsigned n0 = (unsigned)p.bpairs[j];  // a flat pair
+        int xa, ya, xb, yb;
+        bool has_b;
+        uint2 fl;
+        flat_pair(p, n0, xa, ya, xb, yb, has_b, fl);
+        pair_step<T, false, false>(p, n0, xa, ya, xb, yb, has_b, skey, fl, fxs, fys);
     }
     pair_block_slots(p, ntiles + i, fxs, fys);
 }

@@ -131,7 +131,10 @@ struct KParams {
     // (c+1)*bchunk) from device memory before its tiles, which skip them
     int nbpairs;
     const int* bpairs;
-    int bchunk, bpad;
+    int bchunk;
+    // batched paired kernel: tiles of (threads per block) flat node pairs
+    // (2k, 2k + 1) of the node index, any width; 0: 2-D tiles of row pairs
+    int ftiles;
 };
 static_assert(sizeof(KParams) % 16 == 0, "KParams is staged with 16-byte copies");
 

@@ -115,16 +115,14 @@ __global__ void __launch_bounds__(512, 2) batch_step_pair_kernel(const KParams* 
     __shared__ KParams sp;
     int local;
     if (!batch_block_begin(inst, block_map, sp, local)) return;
-    const int tiles = sp.gx * ((sp.ny + (int)blockDim.y - 1) / (int)blockDim.y);
+    // a member on this kernel always has flat tiles and its boundary pairs
+    // in its boundary blocks (none when it has no boundary node)
+    const int tiles = sp.ftiles;
     if (local < 0) {  // boundary block -(local + 1)
         pair_boundary_block<T>(sp, -(local + 1), tiles);
         return;
     }
-    // a member's boundary pairs are all in its boundary blocks (a batch
-    // member on this kernel always has its slots laid out for them; none
-    // when it has no boundary node)
-    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
-        step_pair_block<T, false, true>(sp, t % sp.gx, t / sp.gx, sp.gx);
+    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t) step_flat_pair_block<T>(sp, t);
 }
 
 // The thermal form: twice the populations, so no register cap.

@@ -335,20 +335,21 @@ __global__ void __launch_bounds__(kResMaxThreads<T, KIND>, kResMinBlocks<T, KIND
         if (tid == 0) s_u[cb] = un < total ? first + atomicAdd(ctr, 1) : total;
         const KParams& p = sp[cb];
         const int local = u - s_st[staged[cb]];
-        const int tiles = p.gx * ((p.ny + (int)blockDim.y - 1) / (int)blockDim.y);
         if constexpr (KIND == 0) {
             if constexpr (!std::is_same<T, double>::value) {
+                // flat tiles, then the member's boundary blocks (its
+                // boundary pairs: none when it has no boundary node)
+                const int tiles = p.ftiles;
                 const int reg = (tiles + kBatchTiles - 1) / kBatchTiles;
                 if (local >= reg) {
                     pair_boundary_block<T>(p, local - reg, tiles);
                 } else {
-                    // a paired member's boundary pairs are all in its
-                    // boundary blocks (none when it has no boundary node)
                     for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
-                        step_pair_block<T, false, true>(p, t % p.gx, t / p.gx, p.gx);
+                        step_flat_pair_block<T>(p, t);
                 }
             }
         } else {
+            const int tiles = p.gx * ((p.ny + (int)blockDim.y - 1) / (int)blockDim.y);
             for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
                 step_block<T, KIND == 2>(p, t % p.gx, t / p.gx, p.gx);
         }

@@ -145,7 +145,7 @@ void apply_collide(KParams& p, const CollideParams& c);
 int ensure_populations(lbm2d_solver* h);
 int ensure_stage(lbm2d_solver* h, bool want_g);
 int upload_geometry(lbm2d_solver* h);
-int ensure_slots(lbm2d_solver* h);
+int ensure_slots(lbm2d_solver* h, bool batch = false);
 KParams rebuild_params(const lbm2d_solver* h);
 int materialize(lbm2d_solver* h);
 int before_setting_change(lbm2d_solver* h);
@@ -173,10 +173,11 @@ bool use_pair(const lbm2d_solver* h);
 // own row-pipeline launches inside the batch's step.
 enum KernelKind : int { KERNEL_SCALAR = 0, KERNEL_PAIR = 1, KERNEL_ROWS = 2, KERNEL_TILES = 3 };
 constexpr long long kBatchSoloNodes = 1LL << 21;
-int kernel_kind(const lbm2d_solver* h);
+int kernel_kind(const lbm2d_solver* h);              // a plain step's kernel
+int kernel_kind(const lbm2d_solver* h, bool batch);  // batch: stepped by a batch or the resident loop
 // Bring a handle to the COLLIDED state for steps with (tau, u) and fill the
 // kernel parameters of the next step (fin = current buffer); returns status.
-int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p);
+int prepare_steps(lbm2d_solver* h, double tau, double u_inflow, KParams& p, bool batch = false);
 // Launch one step from buffer h->cur (step kernel with its force reduction
 // into p.partials, immersed-boundary kernels); advance() then moves the host
 // state on by n steps.  e0 / e1 (optional) bracket the step kernel.

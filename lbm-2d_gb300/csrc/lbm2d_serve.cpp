@@ -143,15 +143,16 @@ int prepare_entry(Active& a) {
     h->in_batch = true;
     h->resident = true;
     KParams p;
-    int rc = rt::prepare_steps(h, a.tau, a.u_bc, p);
+    int rc = rt::prepare_steps(h, a.tau, a.u_bc, p, true);
     if (rc) return rc;
-    if (h->thermal && p.pair) return LBM2D_ERR_INVALID;  // the loop has no paired thermal kernel
+    const bool paired = h->slot_kind == rt::KERNEL_PAIR;
+    if (h->thermal && paired) return LBM2D_ERR_INVALID;  // the loop has no paired thermal kernel
     auto e = std::make_shared<ResEntry>();
     std::memset(e.get(), 0, sizeof(ResEntry));
-    const int kind = h->thermal ? 2 : (p.pair ? 0 : 1);
+    const int kind = h->thermal ? 2 : (paired ? 0 : 1);
     e->combo = 3 * h->storage + kind;
     const int gy = (h->ny + h->by - 1) / h->by;
-    long long units = ((long long)p.gx * gy + kBatchTiles - 1) / kBatchTiles;
+    long long units = ((long long)(p.ftiles > 0 ? p.ftiles : (long long)p.gx * gy) + kBatchTiles - 1) / kBatchTiles;
     if (kind == 0 && p.nbpairs > 0) units += (p.nbpairs + p.bchunk - 1) / p.bchunk;
     e->units = (int)units;
     e->p[0] = p;

@@ -221,3 +221,38 @@ def test_batch_autotune_preserves_state_and_budgets(product, oracle_lib):
         x.close()
     b.close()
     ref_b.close()
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_odd_widths_pair_when_node_count_even(product, oracle_lib, storage):
+    """Batch members of odd width are stepped by the paired kernel on flat
+    node pairs (2k, 2k + 1) when their node count is even (every plane's pair
+    stores stay aligned), by the one-node kernel otherwise; both agree with
+    the same solve stepped alone (one node per thread) to FP32 rounding."""
+    import copy
+    sizes = [(97, 40), (97, 41), (64, 33)]  # odd width, even N; odd width, odd N; even width, even N
+    specs = []
+    for nx, ny in sizes:
+        sp = copy.deepcopy(CS.CASES["cylinder_mei"])
+        sp["nx"], sp["ny"] = nx, ny
+        sp["geometry"] = [("cylinder", nx // 4, ny // 2, max(2, ny // 10))]
+        sp["init"] = ("wake", 0.1, nx // 4, 42, 1e-4)
+        specs.append(sp)
+    b = product.Batch()
+    mem = [gpu_solver(product, oracle_lib, sp, storage) for sp in specs]
+    for s, sp in zip(mem, specs):
+        b.add(s, sp["tau"], sp["u"])
+    kinds = [s.info().kernel for s in mem]
+    assert kinds == [product.KERNEL_PAIR, product.KERNEL_SCALAR, product.KERNEL_PAIR], kinds
+    b.step(30)
+    b.synchronize()
+    tol = {"fp32": 1e-6, "fp16": 2e-4}[storage]  # FP16: stochastic rounding apart, see test_serve_gpu
+    for s, sp in zip(mem, specs):
+        a = gpu_solver(product, oracle_lib, sp, storage)
+        a.step(sp["tau"], sp["u"], 30)
+        a.synchronize()
+        assert rel_l2(s.f, a.f) <= tol, (sp["nx"], sp["ny"])
+        a.close()
+    b.close()
+    for s in mem:
+        s.close()
