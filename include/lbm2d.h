@@ -239,12 +239,15 @@ int lbm2d_set_block(lbm2d_solver *h, int bx, int by);
 /* Step-kernel variant.  0 (default): the fastest kernel the configuration
  * allows -- the row pipeline (non-thermal FP32 with nx a multiple of 4, or
  * FP16/BF16 with nx a multiple of 8; in a batch only members of at least
- * 2^20 nodes), else the tile pipeline for the thermal DDF and for batch
- * members (FP32/FP16/BF16), else two x-neighbours per thread with packed
- * FP32x2 arithmetic (nx even), else one node per thread.  1: one node per
- * thread.  2: two x-neighbours per thread where nx is even.  3: the tile
- * pipeline (FP32/FP16/BF16).  Same results to rounding; lbm2d_get_info
- * reports the kernel in use. */
+ * 2^21 nodes), else two nodes per thread with packed FP32x2 arithmetic
+ * (non-thermal, nx even; in a batch or the resident serving loop: flat
+ * node pairs, any nx with an even node count), else one node per thread
+ * (the thermal DDF: six 256-thread blocks per SM).  1: one node per
+ * thread.  2: two x-neighbours per thread where nx is even (thermal
+ * included).  3: the tile pipeline (FP32/FP16/BF16).  Same results to
+ * rounding; lbm2d_get_info reports the kernel in use (for a batch member,
+ * the kernel its batch steps it with; a plain lbm2d_step of a member runs
+ * the single-solve kernels). */
 int lbm2d_set_kernel_variant(lbm2d_solver *h, int variant);
 /* Limit, in SM cycles, of the staging pipelines' (row and tile kernels)
  * consumer-side waits for their staged tiles (0, the default: about one

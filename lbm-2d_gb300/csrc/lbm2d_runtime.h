@@ -104,9 +104,9 @@ struct lbm2d_solver {
     long long steps_done = 0;
     long long launches = 0;
     int bx = 128, by = 2;
-    // 0: fastest kernel the configuration allows (row pipeline; the tile
-    // pipeline for the thermal DDF; else paired, else one node per thread),
-    // 1: one node per thread, 2: paired nodes, 3: the tile pipeline
+    // 0: fastest kernel the configuration allows (row pipeline; else
+    // paired, flat pairs in a batch; else one node per thread, the thermal
+    // DDF's), 1: one node per thread, 2: paired nodes, 3: the tile pipeline
     int variant = 0;
     bool in_batch = false;  // a batch member is stepped by the batched kernels
     bool resident = false;  // a member of the resident serving loop (never the row pipeline)

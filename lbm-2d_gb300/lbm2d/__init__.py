@@ -400,10 +400,11 @@ class Solver:
 
     def set_kernel_variant(self, variant: int):
         """0 (default): fastest kernel the configuration allows (row pipeline;
-        the tile pipeline for the thermal DDF; else paired nodes, else one node
-        per thread); 1: one node per thread; 2: paired nodes per thread; 3: the
-        tile pipeline.  `info().kernel` reports the kernel in use
-        (KERNEL_SCALAR / KERNEL_PAIR / KERNEL_ROWS / KERNEL_TILES)."""
+        else paired nodes, flat node pairs in a batch; else one node per
+        thread, which the thermal DDF runs); 1: one node per thread; 2: paired
+        nodes per thread; 3: the tile pipeline.  `info().kernel` reports the
+        kernel in use (KERNEL_SCALAR / KERNEL_PAIR / KERNEL_ROWS /
+        KERNEL_TILES)."""
         self._ck(self.L.lbm2d_set_kernel_variant(self.h, int(variant)))
 
     def set_wait_limit(self, cycles: int):
