@@ -829,7 +829,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (default: --steps)")
-    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "precision", "frame", "ibm"])
+    ap.add_argument("--mode", default="step",
+                    choices=["step", "batch", "serve", "precision", "frame", "ibm", "thermal"])
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--batch-storage", default="fp32")
     ap.add_argument("--autotune", action="store_true")
@@ -850,6 +851,7 @@ def main():
     ap.add_argument("--precision-steps", type=int, default=1000)
     ap.add_argument("--batch-steps", type=int, default=5000)
     ap.add_argument("--thermal-n", type=int, default=4096)
+    ap.add_argument("--thermal-steps", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -864,6 +866,13 @@ def main():
         return run_frame(args)
     if args.mode == "ibm":
         return run_ibm(args)
+    if args.mode == "thermal":
+        import torch
+
+        import lbm2d
+        lbm2d.build(quiet=True)
+        print(json.dumps(thermal_block(lbm2d, torch, args.thermal_n, args.thermal_steps)), flush=True)
+        return 0
 
     import torch
 
@@ -1013,7 +1022,7 @@ def main():
         for st, res in pe.get("results", {}).items():
             if st in prec:
                 prec[st].update({k: res[k] for k in ("velocity_rel_l2_vs_fp64", "drag_rel_err_vs_fp64")})
-        line["thermal"] = guarded(lambda: thermal_block(lbm2d, torch, args.thermal_n))
+        line["thermal"] = guarded(lambda: thermal_block(lbm2d, torch, args.thermal_n, args.thermal_steps))
         line["batch"] = {st: guarded(lambda st=st: batch_block(args, lbm2d, st, args.batch_steps))
                          for st in ("fp32", "fp16")}
         line["serving"] = guarded(lambda: serve_block(args, lbm2d))
