@@ -279,7 +279,8 @@ __global__ void __launch_bounds__(kResMaxThreads<T, KIND>, kResMinBlocks<T, KIND
     res_step_kernel(ResDev d, int b, int c) {
     __shared__ __align__(16) KParams sp[2];
     __shared__ int s_st[kResMaxSlots + 1];
-    __shared__ int s_u[2];
+    __shared__ int s_next, s_next_m, s_next_buf;  // the block's next unit, its member and buffer
+    __shared__ int s_staged[2];                    // the member whose parameters sp[k] holds
     const int n = d.count[b * kResCombos + c];
     if (n == 0) return;
     const int* st = d.start + (size_t)(b * kResCombos + c) * (d.cap + 1);
@@ -288,17 +289,10 @@ __global__ void __launch_bounds__(kResMaxThreads<T, KIND>, kResMinBlocks<T, KIND
     if ((int)blockIdx.x >= total) return;
     const int first = min((int)gridDim.x, total);  // units handed out by block index
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    const int warp = tid >> 5, lane = tid & 31;
     for (int i = tid; i <= n; i += nt) s_st[i] = st[i];
     const KParams* const* pp = d.params + (size_t)(b * kResCombos + c) * d.cap;
     int* ctr = d.ctr + b * kResCombos + c;
-    // the others are taken one at a time from the combo's counter (the block
-    // scheduler's dynamic balance); the next one is taken, and its member's
-    // parameters staged into the other buffer, while the current one runs
-    if (tid == 0) {
-        s_u[0] = (int)blockIdx.x;
-        s_u[1] = first + atomicAdd(ctr, 1);
-    }
-    __syncthreads();
     auto member_of = [&](int u) {  // last member whose first unit is <= u
         int lo = 0, hi = n - 1;
         while (lo < hi) {
@@ -309,32 +303,63 @@ __global__ void __launch_bounds__(kResMaxThreads<T, KIND>, kResMinBlocks<T, KIND
         return lo;
     };
     constexpr int kChunks = (int)(sizeof(KParams) / 16);
-    auto stage = [&](int m, int buf) {  // 16-byte asynchronous copies
-        if (tid < kChunks) {
-            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char*>(&sp[buf]) + 16 * tid);
-            const char* src = reinterpret_cast<const char*>(pp[m]) + 16 * tid;
+    auto stage = [&](int m, int buf) {  // warp 0: 16-byte asynchronous copies
+        for (int k = lane; k < kChunks; k += 32) {
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char*>(&sp[buf]) + 16 * k);
+            const char* src = reinterpret_cast<const char*>(pp[m]) + 16 * k;
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    int u = s_u[0], cb = 0;
-    if (u >= total) return;
-    int staged[2] = {member_of(u), -1};
-    stage(staged[0], 0);
-    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();  // s_st
+    if (warp == 0) {
+        const int m0 = member_of((int)blockIdx.x);
+        stage(m0, 0);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (lane == 0) {
+            s_next = (int)blockIdx.x;
+            s_next_m = m0;
+            s_next_buf = 0;
+            s_staged[0] = m0;
+            s_staged[1] = -1;
+        }
+    }
     __syncthreads();
-    for (;;) {
-        const int un = s_u[cb ^ 1];
+    // Units are taken one at a time from the combo's counter, as the block
+    // scheduler hands out launch blocks: warp 0 takes the next one when the
+    // current unit starts its last tile and stages that member's parameters
+    // in the other buffer meanwhile, so a block never holds a unit another
+    // block could have started.
+    int cb = 0;
+    auto take_next = [&]() {
+        if (warp != 0) return;
+        int un = 0;
+        if (lane == 0) un = first + atomicAdd(ctr, 1);
+        un = __shfl_sync(0xffffffffu, un, 0);
+        int mn = -1, nb = cb;
         if (un < total) {
-            const int mn = member_of(un);
-            if (mn != staged[cb ^ 1]) {
-                staged[cb ^ 1] = mn;
-                stage(mn, cb ^ 1);
+            mn = member_of(un);
+            if (mn != s_staged[cb]) {
+                nb = cb ^ 1;
+                if (mn != s_staged[nb]) stage(mn, nb);
             }
         }
-        if (tid == 0) s_u[cb] = un < total ? first + atomicAdd(ctr, 1) : total;
+        __syncwarp();
+        if (lane == 0) {
+            s_next = un;
+            s_next_m = mn;
+            s_next_buf = nb;
+            if (mn >= 0) s_staged[nb] = mn;
+        }
+    };
+    for (;;) {
+        const int u = s_next;
+        if (u >= total) break;
+        const int m = s_next_m;
+        cb = s_next_buf;
+        __syncthreads();  // every thread has read the shared words take_next rewrites
         const KParams& p = sp[cb];
-        const int local = u - s_st[staged[cb]];
+        const int local = u - s_st[m];
         if constexpr (KIND == 0) {
             if constexpr (!std::is_same<T, double>::value) {
                 // flat tiles, then the member's boundary blocks (its
@@ -342,22 +367,28 @@ __global__ void __launch_bounds__(kResMaxThreads<T, KIND>, kResMinBlocks<T, KIND
                 const int tiles = p.ftiles;
                 const int reg = (tiles + kBatchTiles - 1) / kBatchTiles;
                 if (local >= reg) {
+                    take_next();
                     pair_boundary_block<T>(p, local - reg, tiles);
                 } else {
-                    for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+                    const int t1 = min(tiles, (local + 1) * kBatchTiles);
+                    for (int t = local * kBatchTiles; t < t1; ++t) {
+                        if (t == t1 - 1) take_next();
                         step_flat_pair_block<T>(p, t);
+                    }
                 }
+            } else {
+                take_next();  // never launched: FP64 is not paired
             }
         } else {
             const int tiles = p.gx * ((p.ny + (int)blockDim.y - 1) / (int)blockDim.y);
-            for (int t = local * kBatchTiles; t < min(tiles, (local + 1) * kBatchTiles); ++t)
+            const int t1 = min(tiles, (local + 1) * kBatchTiles);
+            for (int t = local * kBatchTiles; t < t1; ++t) {
+                if (t == t1 - 1) take_next();
                 step_block<T, KIND == 2>(p, t % p.gx, t / p.gx, p.gx);
+            }
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();  // the next unit's id and parameters are in place
-        if (un >= total) break;
-        u = un;
-        cb ^= 1;
     }
 }
 
