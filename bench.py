@@ -371,11 +371,13 @@ def serve_block(args, lbm2d):
     gaps = rng.exponential(1.0 / args.rate, len(reqs))
     storage = args.serve_storage
 
-    def leg(resident):
+    def leg(resident, fifo=False):
         # resident: the device loop (steps_per_tick bounds one launch of it);
-        # else host ticks of args.tick batched steps
+        # else host ticks of args.tick batched steps, the fewest remaining
+        # steps first (fifo: every active solve in every tick)
         srv = lbm2d.Server(0, budget_bytes=args.serve_budget_gb * (1 << 30), max_active=args.max_active,
-                           steps_per_tick=args.resident_launch if resident else args.tick, resident=resident)
+                           steps_per_tick=args.resident_launch if resident else args.tick, resident=resident,
+                           fifo=fifo)
         t0 = time.perf_counter()
         next_t = t0
         for r, gap in zip(reqs, gaps):
@@ -393,7 +395,8 @@ def serve_block(args, lbm2d):
         status = {}
         for x in res:
             status[str(x["status"])] = status.get(str(x["status"]), 0) + 1
-        out = {"loop": "resident" if resident else "ticks",
+        out = {"loop": "resident" if resident else ("ticks, every solve each tick" if fifo else
+                                                     "ticks, fewest remaining steps first"),
                "requests": len(res), "failed": int(sum(1 for x in res if x["status"] != 0)), "status": status,
                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                "mean_s": float(lat.mean()), "makespan_s": span, "glups": lu / span / 1e9,
@@ -411,6 +414,7 @@ def serve_block(args, lbm2d):
     # the tick loop is the headline (the faster of the two on this mix); the
     # device-resident loop is measured beside it
     serve = leg(False)
+    serve_fifo = leg(False, fifo=True) if not args.no_resident_leg else None
     serve_resident = leg(True) if not args.no_resident_leg else None
     # --- sequential plain solves, FIFO, same arrival times:
     #   "dropin": the reference drivers' loop through the per-solve API, one
@@ -457,7 +461,8 @@ def serve_block(args, lbm2d):
         seq["bulk"]["note"] = "same, but one lbm2d_step call for each request's whole budget"
     line = {"metric": "serving: p50/p99 time-to-solution and aggregate GLUPS", "unit": "GLUPS",
             "value": serve["glups"], "p50_s": serve["p50_s"], "p99_s": serve["p99_s"], "glups": serve["glups"],
-            "budget_scale": scale, "serve": serve, "serve_resident": serve_resident, "sequential": seq or None,
+            "budget_scale": scale, "serve": serve, "serve_fifo": serve_fifo, "serve_resident": serve_resident,
+            "sequential": seq or None,
             "speedup_vs_sequential_dropin": (serve["glups"] / seq["dropin"]["glups"]) if seq else None,
             "speedup_vs_sequential_bulk": (serve["glups"] / seq["bulk"]["glups"]) if seq else None,
             "config": {"workload": f"{len(reqs)} requests, Poisson {args.rate}/s, grids 128x64..2048x768, "
@@ -844,7 +849,7 @@ def main():
     ap.add_argument("--resident-launch", type=int, default=1000,
                     help="serving: iterations of one launch of the resident loop")
     ap.add_argument("--no-resident-leg", action="store_true",
-                    help="serving: skip the device-resident loop's comparison leg")
+                    help="serving: skip the comparison legs (every solve each tick; the device-resident loop)")
     ap.add_argument("--no-sequential", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the precision, thermal, batch and serving blocks of the default line")

@@ -76,7 +76,17 @@ struct Active {
     double tau = 0.0, u_bc = 0.0;
     StateIO io;
     std::shared_ptr<ResEntry> entry;  // resident mode: the solve's table entry
+    bool in_batch = false;            // tick mode: chosen for the current tick
 };
+
+// Tick mode, shortest remaining first: each tick steps the active solves
+// with the fewest remaining steps, as many as it takes to reach this many
+// lattice nodes; the others wait out of the batch.  Per-solve arithmetic
+// does not depend on the company a step keeps, so the results are those of
+// any other order.  On the 200-request serving mix (FP16): 8 Mi nodes gave
+// p50 / p99 1.51 / 10.1 s at 61.9 GLUPS, 16 Mi 1.72 / 9.38 s at 66.2, 32 Mi
+// 2.58 / 9.05 s at 68.6, every solve each tick 3.02 / 8.96 s at 69.2.
+constexpr long long kSaturateNodes = 16LL << 20;
 
 size_t footprint_bytes(const lbm2d_request& r) {
     const size_t n = (size_t)r.nx * r.ny;
@@ -94,6 +104,7 @@ struct lbm2d_server {
     size_t budget = 0;
     int max_active = 0;
     int steps_per_tick = 0;
+    bool fifo = false;  // tick mode: every active solve in every tick
     lbm2d_batch* batch = nullptr;
     std::thread worker;
     std::vector<std::thread> setup_threads;
@@ -301,7 +312,7 @@ void release(lbm2d_server* s, const Active& a, int status) {
 
 void retire(lbm2d_server* s, size_t k, int status) {
     Active a = s->active[k];
-    if (a.h) lbm2d_batch_remove(s->batch, a.h);
+    if (a.h && a.in_batch) lbm2d_batch_remove(s->batch, a.h);
     s->active.erase(s->active.begin() + k);
     release(s, a, status);
 }
@@ -349,23 +360,57 @@ void setup_loop(lbm2d_server* s) {
     }
 }
 
-// Move the solves that are set up into the batch (stepping thread).
+// Move the solves that are set up to the active list (stepping thread);
+// choose_tick puts them into the batch.
 void join_ready(lbm2d_server* s) {
     std::deque<Active> r;
     {
         std::lock_guard<std::mutex> lock(s->mu);
         r.swap(s->ready);
     }
-    for (auto& a : r) {
-        int rc = lbm2d_batch_add(s->batch, a.h, a.tau, a.u_bc);
-        if (!rc) rc = lbm2d_batch_set_budget(s->batch, a.h, a.left);
-        if (rc) {
-            lbm2d_batch_remove(s->batch, a.h);
-            release(s, a, rc);
-            continue;
-        }
-        s->active.push_back(a);
+    for (auto& a : r) s->active.push_back(a);
+}
+
+// The solves the next tick steps (all of them in FIFO mode; else the
+// fewest remaining steps first, up to kSaturateNodes nodes), moved into and
+// out of the batch, with their budgets.  Returns the number chosen.
+size_t choose_tick(lbm2d_server* s) {
+    std::vector<size_t> order(s->active.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    if (!s->fifo)
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            const Active &x = s->active[a], &y = s->active[b];
+            if (x.left != y.left) return x.left < y.left;
+            return (long long)x.req.nx * x.req.ny < (long long)y.req.nx * y.req.ny;
+        });
+    std::vector<char> want(s->active.size(), 0);
+    long long nodes = 0;
+    size_t chosen = 0;
+    for (size_t i : order) {
+        if (!s->fifo && chosen > 0 && nodes >= kSaturateNodes) break;
+        want[i] = 1;
+        nodes += (long long)s->active[i].req.nx * s->active[i].req.ny;
+        ++chosen;
     }
+    for (size_t i = s->active.size(); i-- > 0;) {
+        Active& a = s->active[i];
+        if (!want[i] && a.in_batch) {
+            lbm2d_batch_remove(s->batch, a.h);
+            a.in_batch = false;
+        } else if (want[i]) {
+            int rc = LBM2D_OK;
+            if (!a.in_batch) {
+                rc = lbm2d_batch_add(s->batch, a.h, a.tau, a.u_bc);
+                a.in_batch = rc == LBM2D_OK;
+            }
+            if (!rc) rc = lbm2d_batch_set_budget(s->batch, a.h, a.left);
+            if (rc) {
+                retire(s, i, rc);
+                --chosen;
+            }
+        }
+    }
+    return chosen;
 }
 
 void worker_loop(lbm2d_server* s) {
@@ -379,13 +424,18 @@ void worker_loop(lbm2d_server* s) {
             if (s->stop) return;
             continue;
         }
+        // the solves of this tick; solves joining below wait for the next one
+        const double tc = now_s();
+        const size_t n_tick = choose_tick(s);
+        s->join_s += now_s() - tc;
+        if (n_tick == 0) continue;
         // every solve carries its own budget into the batch, so a tick can be
         // long: a solve whose budget runs out mid-tick sits out the rest
         long long k = 0;
-        for (auto& a : s->active) k = std::max(k, a.left);
+        for (auto& a : s->active)
+            if (a.in_batch) k = std::max(k, a.left);
         k = std::min<long long>(k, s->steps_per_tick);
-        // the members of this tick; solves joining below wait for the next one
-        const size_t n_tick = s->active.size();
+        const size_t n_active = s->active.size();
         const double t0 = now_s();
         cudaStream_t bs = static_cast<cudaStream_t>(lbm2d_batch_stream(s->batch));
         if (s->ev0) cudaEventRecord(s->ev0, bs);
@@ -406,16 +456,17 @@ void worker_loop(lbm2d_server* s) {
         ++s->ticks;
         s->member_ticks += (long long)n_tick;
         s->busy_s += now_s() - t0;
-        for (size_t i = 0; i < n_tick; ++i) {
+        for (size_t i = 0; i < n_active; ++i) {
             Active& a = s->active[i];
+            if (!a.in_batch) continue;
             const long long taken = std::min(a.left, k);
             a.left -= taken;
             s->lattice_updates += taken * (long long)a.req.nx * a.req.ny;
         }
         const double t4 = now_s();
-        for (size_t i = n_tick; i-- > 0;) {
+        for (size_t i = n_active; i-- > 0;) {
             Active& a = s->active[i];
-            if (a.left <= 0 || rc) {
+            if (a.in_batch && (a.left <= 0 || rc)) {
                 int st = rc;
                 if (!st && a.h) st = lbm2d_synchronize(a.h);  // non-finite density -> LBM2D_ERR_NAN
                 retire(s, i, st);
@@ -584,10 +635,12 @@ int lbm2d_server_create_ex(int device, double budget_bytes, int max_active, int 
                            lbm2d_server** out) {
     if (!out || max_active < 1 || steps_per_tick < 1) return LBM2D_ERR_INVALID;
     const bool resident = (flags & LBM2D_SERVE_RESIDENT) != 0;
+    const bool fifo = (flags & LBM2D_SERVE_FIFO) != 0;
     if (resident && max_active > kResMaxSlots) return LBM2D_ERR_INVALID;
     auto* s = new lbm2d_server();
     s->device = device;
     s->resident = resident;
+    s->fifo = fifo;
     s->budget = budget_bytes > 0 ? (size_t)budget_bytes : (size_t)64 << 30;
     s->max_active = max_active;
     s->steps_per_tick = steps_per_tick;

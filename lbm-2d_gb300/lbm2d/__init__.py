@@ -641,14 +641,17 @@ class Server:
     """Serving loop: concurrent solves admitted by device-memory footprint and
     stepped together (see include/lbm2d.h, lbm2d_server_*)."""
 
-    def __init__(self, device=0, budget_bytes=64 << 30, max_active=512, steps_per_tick=200, resident=False):
+    def __init__(self, device=0, budget_bytes=64 << 30, max_active=512, steps_per_tick=200, resident=False,
+                 fifo=False):
         """resident: step the solves with the device-resident loop
         (LBM2D_SERVE_RESIDENT; steps_per_tick then bounds one launch of the
-        loop) instead of host ticks of steps_per_tick batched steps."""
+        loop) instead of host ticks of steps_per_tick batched steps.  fifo
+        (ticks): every active solve in every tick, instead of the fewest
+        remaining steps first (LBM2D_SERVE_FIFO)."""
         L = lib()
         h = _P()
         rc = L.lbm2d_server_create_ex(int(device), float(budget_bytes), int(max_active), int(steps_per_tick),
-                                      1 if resident else 0, C.byref(h))
+                                      (1 if resident else 0) | (2 if fifo else 0), C.byref(h))
         if rc:
             raise LBMError(rc, "server create")
         self.L, self.h = L, h

@@ -24,7 +24,9 @@ admitted, stepped together and retired exactly at their budgets.
 * Admission respects the device-memory budget.
 * The device-resident loop (resident=True) serves every request with
   bit-for-bit the same final state and drag/lift as the tick loop; each
-  test above runs in both modes."""
+  test above runs in both modes.  So does the tick loop that steps every
+  solve in every tick (fifo=True) against its default, the fewest remaining
+  steps first."""
 import time
 
 import numpy as np
@@ -95,8 +97,9 @@ def test_served_results_match_alone(product, storage, resident):
         assert abs(x["fx"] - fx) <= tol * scale and abs(x["fy"] - fy) <= tol * scale, (r, x, fx, fy)
 
 
-def _serve(product, reqs, storage, tick, f_inits=None, resident=False):
-    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=tick, resident=resident)
+def _serve(product, reqs, storage, tick, f_inits=None, resident=False, fifo=False):
+    srv = product.Server(0, budget_bytes=8 << 30, max_active=64, steps_per_tick=tick, resident=resident,
+                         fifo=fifo)
     f_inits = f_inits or [None] * len(reqs)
     ids = [srv.submit(r["nx"], r["ny"], r["geometry"], r["re"], r["steps"], storage, r["param"], f_init=fi,
                       keep_state=True) for r, fi in zip(reqs, f_inits)]
@@ -161,6 +164,19 @@ def test_resident_equals_ticks(product, storage):
     ticks = _serve(product, REQS, storage, 64)
     res = _serve(product, REQS, storage, 37, resident=True)
     for r, x, a in zip(REQS, res, ticks):
+        assert x["status"] == 0 and a["status"] == 0
+        assert x["steps"] == a["steps"] == r["steps"]
+        _same_state(x, a)
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_shortest_first_equals_fifo(product, storage):
+    """The tick loop steps the solves with the fewest remaining steps first
+    (the others wait out of the batch); every request ends bit-identical to
+    the loop that steps all of them in every tick."""
+    srpt = _serve(product, REQS, storage, 64)
+    fifo = _serve(product, REQS, storage, 64, fifo=True)
+    for r, x, a in zip(REQS, srpt, fifo):
         assert x["status"] == 0 and a["status"] == 0
         assert x["steps"] == a["steps"] == r["steps"]
         _same_state(x, a)
