@@ -467,7 +467,8 @@ def serve_block(args, lbm2d):
             "speedup_vs_sequential_bulk": (serve["glups"] / seq["bulk"]["glups"]) if seq else None,
             "config": {"workload": f"{len(reqs)} requests, Poisson {args.rate}/s, grids 128x64..2048x768, "
                                    f"{{cavity, step, cylinder, side-by-side}}, Re 50-2000, budgets 1k-50k x {scale}",
-                       "storage": storage, "loop": "ticks", "resident_launch": args.resident_launch,
+                       "storage": storage, "loop": "ticks, fewest remaining steps first (16 Mi nodes per tick)",
+                       "resident_launch": args.resident_launch,
                        "tick": args.tick, "budget_gb": args.serve_budget_gb}}
     return line
 
