@@ -316,8 +316,8 @@ bool use_pair(const lbm2d_solver* h) {
 
 // The kernel a step of h runs.  batch: stepped by a batch (or the resident
 // serving loop), whose paired kernel walks flat pairs (2k, 2k + 1) of the
-// node index, so any width with an even node count pairs there; a plain step
-// of the same solver runs the single-solve kernels.
+// node index, so any width pairs there; a plain step of the same solver runs
+// the single-solve kernels.
 int kernel_kind(const lbm2d_solver* h, bool batch) {
     const bool tiles_ok = h->storage != ST_FP64;
     if (h->variant == 3 && tiles_ok) return KERNEL_TILES;
@@ -326,9 +326,9 @@ int kernel_kind(const lbm2d_solver* h, bool batch) {
             (!batch || (long long)h->N >= kBatchSoloNodes))
             return KERNEL_ROWS;
     }
-    // flat pairs store 8-byte (FP32) / 4-byte (16-bit) pairs at node index
-    // j*N + 2k of plane j: aligned only when the node count N is even
-    const bool flat = batch && !h->thermal && h->storage != ST_FP64 && h->variant != 1 && h->N % 2 == 0;
+    // flat pairs: any width (a lattice with an odd node count stores its
+    // odd planes' pairs as two single-node stores, and its last node alone)
+    const bool flat = batch && !h->thermal && h->storage != ST_FP64 && h->variant != 1;
     if (!use_pair(h) && !flat) return KERNEL_SCALAR;
     return KERNEL_PAIR;
 }

@@ -1148,6 +1148,11 @@ struct PairStore<float> {
     }
     // one node (the last of a lattice with an odd node count)
     static __device__ __forceinline__ void st1(float* p, size_t i, float a, uint32_t) { __stcs(p + i, a); }
+    // the pair's values as two single-node stores (i odd: no pair alignment)
+    static __device__ __forceinline__ void st_split(float* p, size_t i, float a, float b, uint32_t) {
+        __stcs(p + i, a);
+        __stcs(p + i + 1, b);
+    }
 };
 template <>
 struct PairStore<__half> {
@@ -1157,6 +1162,12 @@ struct PairStore<__half> {
     static __device__ __forceinline__ void st1(__half* p, size_t i, float a, uint32_t rb) {
         p[i] = __ushort_as_half((unsigned short)(cvt_rs_f16x2(a, a, rb) & 0xFFFFu));
     }
+    // the bits st would store, as two 2-byte stores (i odd)
+    static __device__ __forceinline__ void st_split(__half* p, size_t i, float a, float b, uint32_t rb) {
+        const uint32_t w = cvt_rs_f16x2(a, b, rb);
+        p[i] = __ushort_as_half((unsigned short)(w & 0xFFFFu));
+        p[i + 1] = __ushort_as_half((unsigned short)(w >> 16));
+    }
 };
 template <>
 struct PairStore<__nv_bfloat16> {
@@ -1165,6 +1176,11 @@ struct PairStore<__nv_bfloat16> {
     }
     static __device__ __forceinline__ void st1(__nv_bfloat16* p, size_t i, float a, uint32_t rb) {
         p[i] = __ushort_as_bfloat16((unsigned short)(cvt_rs_bf16x2(a, a, rb) & 0xFFFFu));
+    }
+    static __device__ __forceinline__ void st_split(__nv_bfloat16* p, size_t i, float a, float b, uint32_t rb) {
+        const uint32_t w = cvt_rs_bf16x2(a, b, rb);
+        p[i] = __ushort_as_bfloat16((unsigned short)(w & 0xFFFFu));
+        p[i + 1] = __ushort_as_bfloat16((unsigned short)(w >> 16));
     }
 };
 
@@ -1265,9 +1281,19 @@ __device__ __forceinline__ void pair_step(const KParams& p, unsigned n0, int xa,
         const size_t N = (size_t)p.N;
         uint32_t rb[9] = {};
         if constexpr (Pop<T>::kRounds) rand9(skey + n0, rb);
+        // n0 is even, so element j*N + n0 is odd -- a pair store there
+        // misaligned -- exactly in the odd planes of a lattice with an odd
+        // node count (flat pairs of an odd width and height): two
+        // single-node stores of the same values there
+        const bool split_odd = (N & 1) != 0;
         if (has_b) {
 #pragma unroll
-            for (int j = 0; j < 9; ++j) PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
+            for (int j = 0; j < 9; ++j) {
+                if (split_odd && (j & 1))
+                    PairStore<T>::st_split(Fo + j * N, n0, fa[j], fb[j], rb[j]);
+                else
+                    PairStore<T>::st(Fo + j * N, n0, fa[j], fb[j], rb[j]);
+            }
         } else {
 #pragma unroll
             for (int j = 0; j < 9; ++j) PairStore<T>::st1(Fo + j * N, n0, fa[j], rb[j]);
@@ -1276,7 +1302,12 @@ __device__ __forceinline__ void pair_step(const KParams& p, unsigned n0, int xa,
             T* __restrict__ Go = static_cast<T*>(p.gout);
             if constexpr (Pop<T>::kRounds) rand9((skey + n0) ^ 0x6A09E667u, rb);
 #pragma unroll
-            for (int j = 0; j < 9; ++j) PairStore<T>::st(Go + j * N, n0, ea[j], eb[j], rb[j]);
+            for (int j = 0; j < 9; ++j) {
+                if (split_odd && (j & 1))
+                    PairStore<T>::st_split(Go + j * N, n0, ea[j], eb[j], rb[j]);
+                else
+                    PairStore<T>::st(Go + j * N, n0, ea[j], eb[j], rb[j]);
+            }
         }
     }
 }
@@ -1352,8 +1383,7 @@ __device__ __forceinline__ void flat_pair(const KParams& p, unsigned n0, int& xa
 
 // Flat tile t of a batched paired instance: its pairs [t*B, (t+1)*B), B the
 // block's threads, one pair (2k, 2k + 1) of the node index per thread, so
-// any width pairs (the node count N is even: a pair store at j*N + 2k is
-// aligned in every plane j).  The instance's boundary pairs are stepped by its
+// any width pairs (pair_step splits the stores a pair would misalign).  The instance's boundary pairs are stepped by its
 // boundary blocks (pair_boundary_block); this tile skips them.
 template <class T>
 __device__ __forceinline__ void step_flat_pair_block(const KParams& p, int t) {
