@@ -7,11 +7,11 @@
 //   pre-launch schedule  ->  while (cond) { S0 -> T0 -> S1 -> T1 }
 //
 //   * S_b: one step kernel per member kind in use ("combo": storage x
-//     paired / one-node / one-node thermal), a fixed grid walking the work
-//     units of the members listed in list buffer b.  A unit is one launch
-//     block of the batched kernels (kBatchTiles tiles of a member's block
-//     grid, or one boundary block of a paired member), so a member's step is
-//     computed exactly as lbm2d_batch_step computes it.
+//     paired / one-node / one-node thermal), a fixed grid whose blocks take
+//     the work units of the members listed in list buffer b from a counter.
+//     A unit is one launch block of the batched kernels (kBatchTiles tiles
+//     of a member, or one boundary block of a paired member), so a member's
+//     step is computed exactly as lbm2d_batch_step computes it.
 //   * T_b: the tail.  Blocks 1.. reduce the force partials of the members
 //     stepped from buffer b (same order and width as the batched reduction);
 //     block 0 schedules the next iteration into buffer 1 - b: it admits the
